@@ -1,0 +1,298 @@
+"""Benchmark of the CDI phase-retrieval path on one GB300.
+
+Workload (the large single-pattern configuration): one 2048x2048 complex64
+pattern of a phase object (amplitude U[0.5,1], phase in [0,pi] from smoothed
+noise, 512-px support with a random smooth boundary), Poisson noise at 1e9
+photons; RAAR beta = 0.9 with a shrinkwrap every 50 iterations.  One bench
+step = one shrinkwrap period (50 RAAR iterations + 1 shrinkwrap) of that
+pattern; the full job (2000 iterations) is 40 steps.
+
+  value    iterations/s with the pattern already resident in HBM (cdx_run_async
+           on device buffers; L2 flushed between steps, each step timed with
+           CUDA events on the context's stream)
+  e2e      iterations/s of the whole 2000-iteration job through the host-buffer
+           C-ABI call cdx_phase_retrieve_host (H2D of I and Psi0, D2H of rho, Psi
+           and the support inside the timed region)
+  roofline algorithmic bytes of one fused iteration (21 B/px: read rho 8 + I 4 +
+           support 1, write rho 8) / the measured duration of one iteration (its
+           column + row pass), against the measured HBM copy bandwidth.
+
+`--impl reference` times the CPU restatement of the reference path (the
+oracle, float32, multi-threaded scipy FFT) on a bounded sample of the same
+workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N = 2048
+PHOTONS = 1e9
+SEED = 20260101
+BETA = 0.9
+SW_EVERY = 50
+STEP_ALGO = f"{SW_EVERY}*RAAR+1*shrinkWrap"
+JOB_ALGO = f"40*({SW_EVERY}*RAAR+1*shrinkWrap)"
+JOB_ITERS = 40 * SW_EVERY
+ALG_BYTES_PER_PX_ITER = 21.0
+METRIC = "iter/s"
+WORKLOAD = "2048x2048 complex64 phase object, 1e9 photons, RAAR beta=0.9, shrinkwrap every 50"
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu=0):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(smax)) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_inputs():
+    from cdixx_gb300 import synth
+    obj, sup, I = synth.config1_case(seed=SEED, n=N, photons=PHOTONS)
+    psi0 = synth.random_phase_start(I, SEED)
+    return I, psi0
+
+
+def cpu_sample(I, psi0, iters, threads):
+    """Oracle (float32 CPU restatement) on `iters` RAAR iterations: iterations/s."""
+    from oracle import cdi_oracle as O
+    O.set_fft_workers(threads)
+    t0 = time.perf_counter()
+    O.phase_retrieve(psi0, I, f"{iters}*RAAR", oversampling_spt=4.0, beta=BETA, shrink_threshold=0.1,
+                     dtype=np.complex64)
+    dt = time.perf_counter() - t0
+    return iters / dt, dt
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    I, psi0 = make_inputs()
+    threads = os.cpu_count() or 1
+    iters = 2
+    cpu_sample(I, psi0, 1, threads)   # warm the FFT plans
+    vals = []
+    t_all = 0.0
+    for _ in range(args.warmup):
+        cpu_sample(I, psi0, iters, threads)
+    for _ in range(args.steps):
+        v, dt = cpu_sample(I, psi0, iters, threads)
+        vals.append(v)
+        t_all += dt
+    v = float(np.median(vals))
+    line = {
+        "metric": METRIC, "value": v, "unit": "iter/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000 * t_all / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "impl": "reference",
+        "config": {"workload": WORKLOAD, "sample": f"{iters} RAAR iterations per step"},
+        "cpu_baseline": {"value": v, "unit": "iter/s", "cores": threads, "kind": "port",
+                         "sample": f"{iters} RAAR iterations of the 2048^2 pattern per step, float32 oracle, "
+                                   f"scipy.fft with {threads} workers"},
+        "e2e": {"value": v, "unit": "iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_gpu(args):
+    import torch
+    from cdixx_gb300 import native as cdx
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    I, psi0 = make_inputs()
+    p = cdx.default_params(N, N, oversampling_spt=4.0, beta=BETA, shrink_threshold=0.1)
+    stream = torch.cuda.Stream()
+    ctx = cdx.Context(p, stream=stream.cuda_stream)
+    ctx.set_pattern(0, I)
+    ctx.set_initial(0, psi0)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def step():
+        ctx.run_async(STEP_ALGO)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    launches_per_step = ctx.stats()["launches"]
+
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    for i in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            ev[i][0].record(stream)
+        step()
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = float(sum(step_ms))
+    clk = clocks.stop()
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    iters = SW_EVERY * args.steps
+    value = world * iters / (total_ms / 1000.0)
+
+    # roofline: pure iterations, events around each block of 50, L2 flushed before each
+    it_ms = []
+    for _ in range(5):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        ctx.run_async(f"{SW_EVERY}*RAAR")
+        b.record(stream)
+        torch.cuda.synchronize()
+        it_ms.append(a.elapsed_time(b) / SW_EVERY)
+    t_iter = float(np.median(it_ms)) / 1000.0
+    peak, peak_kind = peaks()
+    achieved = ALG_BYTES_PER_PX_ITER * N * N / t_iter / 1e9
+    traffic = None
+    tf = ROOT / "profiles" / "traffic_2048.json"
+    if tf.exists():
+        traffic = json.loads(tf.read_text()).get("dram_bytes_per_iteration")
+
+    # e2e: the whole job through the host-buffer C-ABI call
+    e2e_vals = []
+    h2d = I.nbytes + psi0.nbytes
+    d2h = 2 * psi0.nbytes + I.nbytes
+    pe = cdx.default_params(N, N, oversampling_spt=4.0, beta=BETA, shrink_threshold=0.1, use_graph=0)
+    for k in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        cdx.phase_retrieve_host(pe, JOB_ALGO, I, psi0)
+        dt = time.perf_counter() - t0
+        if k > 0:
+            e2e_vals.append(JOB_ITERS / dt)
+    e2e = float(np.median(e2e_vals))
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        cpu_sample(I, psi0, 1, threads)
+        v, dt = cpu_sample(I, psi0, 2, threads)
+        cpu = {"value": v, "unit": "iter/s", "cores": threads, "kind": "port",
+               "sample": "2 RAAR iterations of the 2048^2 pattern, float32 oracle, "
+                         f"scipy.fft with {threads} workers ({dt:.2f} s)"}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "iter/s", "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "step": STEP_ALGO, "patterns": 1, "rows": N, "cols": N,
+                       "l2": "flushed (512 MB write) before every step", "parallelism": "replicas",
+                       "patterns_per_s": value / JOB_ITERS, "path": "fused FP32 (column pass + row pass)"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "kernel": "one fused iteration (col_pass_kernel<2048> + row_pass_kernel<2048>)",
+                         "t_iter_us": t_iter * 1e6},
+            "e2e": {"value": e2e, "unit": "iter/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "step": "whole 2000-iteration job via cdx_phase_retrieve_host"},
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "gpu_launches": launches_per_step * args.steps,
+        }
+        print(json.dumps(line))
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

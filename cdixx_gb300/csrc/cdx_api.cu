@@ -1,0 +1,763 @@
+// C ABI of the CDI phase-retrieval path (include/cdx.h).
+//
+// A context owns one device arena per (size, batch): the real-space iterate
+// rho, the work buffer W (X = rowFFT(rho) between iterations), Psi, the
+// pattern I and sqrt(I), the float support field, the support bits, twiddle
+// tables, reduction partials and per-pattern state.  cdx_run turns the
+// algorithm string into a step list and enqueues it on the context's stream,
+// captured once into a CUDA graph and replayed.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/cdx.h"
+#include "cdx_fft.cuh"
+#include "cdx_host.h"
+#include "cdx_misc.h"
+#include "cdx_types.h"
+
+using namespace cdx;
+
+#define CDX_CK(call)                                                                      \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      return set_error(CDX_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+namespace {
+
+constexpr int kRedBlocks = 152;   // reduction CTAs per pattern (one per SM)
+
+// ---------------------------------------------------------------- twiddles
+// W_n^t = exp(-2 pi i t/n) in double, rounded once to float; one table per
+// (device, n), kept for the life of the process.
+std::mutex g_tw_mu;
+std::map<std::pair<int, int>, float2*> g_tw;
+
+int twiddles(int n, float2** out) {
+  int dev = 0;
+  CDX_CK(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_tw_mu);
+  auto it = g_tw.find({dev, n});
+  if (it != g_tw.end()) { *out = it->second; return CDX_OK; }
+  std::vector<float2> h(n);
+  const double two_pi = 6.283185307179586476925286766559;
+  for (int t = 0; t < n; ++t) {
+    const double a = two_pi * (double)t / (double)n;
+    h[t] = make_float2((float)std::cos(a), (float)-std::sin(a));
+  }
+  float2* d = nullptr;
+  CDX_CK(cudaMalloc(&d, sizeof(float2) * n));
+  CDX_CK(cudaMemcpy(d, h.data(), sizeof(float2) * n, cudaMemcpyHostToDevice));
+  g_tw[{dev, n}] = d;
+  *out = d;
+  return CDX_OK;
+}
+
+int check_len(int n) {
+  if (!size_supported(n) || n > 4096 || !prep_launcher(n))
+    return set_error(CDX_ERR_SIZE, "unsupported length " + std::to_string(n) +
+                                       " (supported: 2^a 3^b in [16, 4096])");
+  return CDX_OK;
+}
+
+}  // namespace
+
+struct cdx_ctx {
+  cdx_params p{};
+  int rows = 0, cols = 0, batch = 0;
+  long long npx = 0;
+  int wpr = 0;
+  cudaStream_t st = nullptr;
+  bool own_stream = false;
+  int device = 0;
+
+  float2 *rho = nullptr, *work = nullptr, *psi = nullptr;
+  float *inten = nullptr, *amp = nullptr, *spt = nullptr, *bs = nullptr;
+  uint32_t* mask = nullptr;
+  float2 *tw_r = nullptr, *tw_c = nullptr;   // lengths rows (column pass) and cols (row pass)
+  double* part = nullptr;                    // [batch][part_per_pat]
+  float* pmax = nullptr;                     // [batch][kRedBlocks]
+  int part_per_pat = 0;
+  int col_blocks = 0;
+  PatState* dstate = nullptr;
+  float* weights = nullptr;
+  size_t weights_cap = 0;
+  void* arena = nullptr;
+
+  // host state
+  std::vector<char> have_pattern;
+  std::vector<char> fresh;    // initial iterate set since the last run
+  bool have_initial = false;
+  bool psi_in_work = false;   // W holds Psi0: the next iteration starts from it
+  bool psi_valid = false;     // psi holds the Psi of the current state
+  int sx = 0, sy = 0, ex = 0, ey = 0;
+
+  // graph cache
+  std::string gkey;
+  cudaGraphExec_t gexec = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int last_steps = 0, last_iters = 0, last_sw = 0, last_launches = 0;
+};
+
+namespace {
+
+void rect_of(cdx_ctx* c) {
+  // createSupport (src/post_gpu/cdi.cc:240-245): double arithmetic, truncated to int
+  const double o = c->p.oversampling_spt;
+  c->sx = (int)((o - 1) / 2 * c->rows / o - 1);
+  c->sy = (int)((o - 1) / 2 * c->cols / o - 1);
+  c->ex = c->rows - c->sx;
+  c->ey = c->cols - c->sy;
+}
+
+int reset_support(cdx_ctx* c, int idx, int count) {
+  const long long off = (long long)idx * c->npx;
+  CDX_CK(rect_support(c->spt + off, c->rows, c->cols, count, c->sx, c->sy, c->ex, c->ey, c->st));
+  // bits with the current threshold of each pattern
+  CDX_CK(support_bits(c->spt + off, c->dstate + idx, 0.f, c->mask + (long long)idx * c->rows * c->wpr, c->rows,
+                      c->cols, count, c->st));
+  return CDX_OK;
+}
+
+int copy_in(void* dst, const void* src, size_t bytes, int where, cudaStream_t st) {
+  CDX_CK(cudaMemcpyAsync(dst, src, bytes, where == CDX_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
+  return CDX_OK;
+}
+int copy_out(void* dst, const void* src, size_t bytes, int where, cudaStream_t st) {
+  CDX_CK(cudaMemcpyAsync(dst, src, bytes, where == CDX_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+  CDX_CK(cudaStreamSynchronize(st));
+  return CDX_OK;
+}
+
+// Shrinkwrap width schedule and the 1-D kernels of every shrinkwrap of a run.
+struct SwPlan {
+  std::vector<float> w;       // concatenated weights
+  std::vector<int> offx, radx, offy, rady;
+};
+
+// Periodic kernel equal to the inverse DFT of the sampled frequency Gaussian
+// exp(-f^2/(2 sf^2)) (f in FFT order) that applyGaussMult multiplies Psi by
+// (src/gpu/cudaConfig.cu:380-395); truncated where it falls below 1e-10 of
+// its peak.
+void fourier_kernel(int n, double sf, std::vector<float>& w, int& off, int& rad) {
+  const int mmax = std::min(n - 1, 64);   // the kernel is far below 1e-10 of its peak by then
+  std::vector<double> k(mmax + 1), ct(n), g(n);
+  const double two_pi = 6.283185307179586476925286766559;
+  for (int t = 0; t < n; ++t) ct[t] = std::cos(two_pi * (double)t / n);
+  for (int f = 0; f < n; ++f) {
+    const int fr = f >= n / 2 ? f - n : f;
+    g[f] = std::exp(-(double)fr * fr / (2.0 * sf * sf));
+  }
+  for (int m = 0; m <= mmax; ++m) {
+    double s = 0.0;
+    for (int f = 0; f < n; ++f) s += g[f] * ct[(int)(((long long)f * m) % n)];
+    k[m] = s / n;
+  }
+  int r = 0;
+  const int rmax = std::min((n - 1) / 2, mmax);
+  while (r < rmax && std::fabs(k[r + 1]) > 1e-10 * std::fabs(k[0])) ++r;
+  off = (int)w.size();
+  rad = r;
+  // the kernel is even in m (G is even up to its f = -n/2 sample)
+  for (int d = -r; d <= r; ++d) w.push_back((float)k[d < 0 ? -d : d]);
+}
+
+// Normalised sampled Gaussian of width sigma px, radius floor(6 sigma)/2 as
+// applyGaussConv sizes it (src/post_gpu/misc.cc:80-86).
+void spatial_kernel(int n, double sigma, std::vector<float>& w, int& off, int& rad) {
+  int r = ((int)std::floor(sigma * 6)) >> 1;
+  r = std::max(0, std::min(r, (n - 1) / 2));
+  std::vector<double> k(2 * r + 1);
+  double s = 0.0;
+  for (int d = -r; d <= r; ++d) s += (k[d + r] = std::exp(-(double)d * d / (2.0 * sigma * sigma)));
+  off = (int)w.size();
+  rad = r;
+  for (int d = -r; d <= r; ++d) w.push_back((float)(k[d + r] / s));
+}
+
+void plan_shrinkwrap(const cdx_ctx* c, int count, SwPlan& P) {
+  float g = c->p.sigma0;
+  for (int i = 0; i < count; ++i) {
+    int ox, rx, oy, ry;
+    if (c->p.shrink_mode == CDX_SHRINK_FOURIER) {
+      // sigma_f = Real(row>>2)/gaussianSigma in float (cdi.cc:327), same for both axes
+      const float sf = (float)(c->rows >> 2) / g;
+      fourier_kernel(c->rows, sf, P.w, ox, rx);
+      fourier_kernel(c->cols, sf, P.w, oy, ry);
+    } else {
+      spatial_kernel(c->rows, g, P.w, ox, rx);
+      spatial_kernel(c->cols, g, P.w, oy, ry);
+    }
+    P.offx.push_back(ox); P.radx.push_back(rx); P.offy.push_back(oy); P.rady.push_back(ry);
+    if (g > c->p.sigma_min) g = (float)((double)g * (double)c->p.sigma_decay);   // gaussianSigma*=0.99
+  }
+}
+
+int col_iter(cdx_ctx* c, bool from_psi, bool rf) {
+  ColArgs a{};
+  a.in = c->work;
+  a.out = c->work;
+  a.psi_out = nullptr;
+  a.amp = c->amp;
+  a.inten = c->inten;
+  a.bs = c->bs;
+  a.rf_partials = rf ? c->part : nullptr;
+  a.tw = c->tw_r;
+  a.cols = c->cols;
+  a.mode = COL_ITER;
+  a.from_psi = from_psi;
+  a.proj = c->p.sim_ccd_bit ? PROJ_CCD : PROJ_MODABS;
+  a.noise_level = c->p.noise_level;
+  a.pat_stride = c->npx;
+  a.scale = 1.f;
+  a.ccd_scale = 1.f / c->p.exposure;
+  a.ccd_rcolor = (float)c->p.rcolor;
+  CDX_CK(col_launcher(c->rows)(a, c->batch, c->st));
+  return CDX_OK;
+}
+
+int row_iter(cdx_ctx* c, int algo) {
+  RowArgs a{};
+  a.in = c->work;
+  a.out = c->work;
+  a.rho = c->rho;
+  a.mask = c->mask;
+  a.tw = c->tw_c;
+  a.rows = c->rows;
+  a.mode = ROW_ITER;
+  a.algo = algo;
+  a.pat_stride = c->npx;
+  a.mask_stride = (long long)c->rows * c->wpr;
+  a.scale = 1.f;
+  a.inv_n = (float)(1.0 / ((double)c->rows * c->cols));   // applyNorm(.., 1./(row*column)), cdi.cc:353
+  a.beta = c->p.beta;
+  CDX_CK(row_launcher(c->cols)(a, c->batch, c->st));
+  return CDX_OK;
+}
+
+// Generic 2-D transform of `batch` patterns: rows then columns.
+int fft2_enqueue(const float2* in, float2* out, int rows, int cols, int batch, bool inv, float scale,
+                 const float2* tw_rows_len, const float2* tw_cols_len, cudaStream_t st) {
+  RowArgs r{};
+  r.in = in;
+  r.out = out;
+  r.tw = tw_cols_len;
+  r.rows = rows;
+  r.mode = ROW_FFT;
+  r.inv = inv;
+  r.pat_stride = (long long)rows * cols;
+  r.scale = 1.f;
+  CDX_CK(row_launcher(cols)(r, batch, st));
+  ColArgs c{};
+  c.in = out;
+  c.out = out;
+  c.tw = tw_rows_len;
+  c.cols = cols;
+  c.mode = COL_FFT;
+  c.inv = inv;
+  c.pat_stride = (long long)rows * cols;
+  c.scale = scale;
+  CDX_CK(col_launcher(rows)(c, batch, st));
+  return CDX_OK;
+}
+
+// Enqueue one whole phaseRetrieve on c->st (no synchronisation).
+int enqueue_run(cdx_ctx* c, const std::vector<int>& steps, const SwPlan& sw, bool psi_in_work) {
+  const long long n_all = c->npx * c->batch;
+  const float sqn = (float)std::sqrt((double)c->rows * c->cols);
+  int nl = 0;   // kernels enqueued
+  CDX_CK(run_begin(c->dstate, c->batch, c->st));
+  ++nl;
+  // applyNorm(cuda_gkp1, 1./sqrt(row*column)) at the start (cdi.cc:313)
+  CDX_CK(scale_complex(c->rho, (float)(1.0 / std::sqrt((double)c->rows * c->cols)), n_all, c->st));
+  ++nl;
+  bool from_psi = psi_in_work;
+  int it = 0, swi = 0;
+  for (int a : steps) {
+    if (a == ALGO_SHRINKWRAP) {
+      const bool m2 = c->p.shrink_mode == CDX_SHRINK_SPATIAL;
+      CDX_CK(shrinkwrap(c->rho, c->psi, c->spt, c->weights + sw.offx[swi], sw.radx[swi], c->weights + sw.offy[swi],
+                        sw.rady[swi], c->rows, c->cols, c->batch, m2, (float)((double)c->rows * c->cols), c->pmax,
+                        c->part, kRedBlocks, c->dstate, c->p.shrink_threshold, c->st));
+      CDX_CK(support_bits(c->spt, c->dstate, 0.f, c->mask, c->rows, c->cols, c->batch, c->st));
+      nl += 4;
+      ++swi;
+      continue;
+    }
+    const bool rf = c->p.rf_every > 0 && (it % c->p.rf_every) == 0;
+    int e = col_iter(c, from_psi, rf);
+    if (e) return e;
+    if (rf) CDX_CK(rfactor_from_partials(c->part, c->col_blocks, c->batch, c->dstate, c->st));
+    e = row_iter(c, a);
+    if (e) return e;
+    nl += rf ? 3 : 2;
+    from_psi = false;
+    ++it;
+  }
+  // final Psi = FFT(rho): W holds rowFFT(rho) unless no iteration ran
+  if (it == 0 && psi_in_work) {
+    CDX_CK(cudaMemcpyAsync(c->psi, c->work, sizeof(float2) * n_all, cudaMemcpyDeviceToDevice, c->st));
+  } else {
+    ColArgs a{};
+    a.in = c->work;
+    a.out = c->psi;
+    a.tw = c->tw_r;
+    a.cols = c->cols;
+    a.mode = COL_FFT;
+    a.inv = 0;
+    a.pat_stride = c->npx;
+    a.scale = 1.f;
+    CDX_CK(col_launcher(c->rows)(a, c->batch, c->st));
+    ++nl;
+  }
+  // applyNorm(cuda_gkp1, sqrt(row*column)) (cdi.cc:406)
+  CDX_CK(scale_complex(c->rho, sqn, n_all, c->st));
+  CDX_CK(residual(c->psi, c->inten, c->npx, c->batch, c->part, kRedBlocks, c->dstate, c->st));
+  CDX_CK(rfactor(c->psi, c->amp, c->npx, c->batch, c->part, kRedBlocks, c->dstate, c->st));
+  nl += 5;
+  c->last_launches = nl;
+  return CDX_OK;
+}
+
+int prepare_run(cdx_ctx* c, const char* algorithm, std::vector<int>& steps, SwPlan& sw) {
+  if (!c) return set_error(CDX_ERR_ARG, "null context");
+  for (int i = 0; i < c->batch; ++i)
+    if (!c->have_pattern[i]) return set_error(CDX_ERR_STATE, "pattern " + std::to_string(i) + " not set");
+  if (!c->have_initial) return set_error(CDX_ERR_STATE, "no initial iterate (cdx_set_initial / cdx_random_start)");
+  int nfresh = 0;
+  for (char f : c->fresh) nfresh += f;
+  if (nfresh != 0 && nfresh != c->batch)
+    return set_error(CDX_ERR_STATE, "a batch restarts together: set the initial iterate of every pattern");
+  int e = algo_expand(algorithm, steps, 50000000);
+  if (e) return e;
+  int nsw = 0;
+  for (int a : steps) {
+    if (a == ALGO_TV) return set_error(CDX_ERR_ALGO, "TV step (FISTA denoising) is not part of this path");
+    nsw += a == ALGO_SHRINKWRAP;
+  }
+  plan_shrinkwrap(c, nsw, sw);
+  if (!sw.w.empty()) {
+    if (sw.w.size() > c->weights_cap) {
+      if (c->weights) cudaFree(c->weights);
+      c->weights = nullptr;
+      c->weights_cap = 0;
+      CDX_CK(cudaMalloc(&c->weights, sizeof(float) * sw.w.size()));
+      c->weights_cap = sw.w.size();
+    }
+    CDX_CK(cudaMemcpyAsync(c->weights, sw.w.data(), sizeof(float) * sw.w.size(), cudaMemcpyHostToDevice, c->st));
+    CDX_CK(cudaStreamSynchronize(c->st));
+  }
+  c->last_steps = (int)steps.size();
+  c->last_sw = nsw;
+  c->last_iters = (int)steps.size() - nsw;
+  return CDX_OK;
+}
+
+int run_impl(cdx_ctx* c, const char* algorithm) {
+  std::vector<int> steps;
+  SwPlan sw;
+  int e = prepare_run(c, algorithm, steps, sw);
+  if (e) return e;
+  CDX_CK(cudaSetDevice(c->device));
+  const bool piw = c->psi_in_work;
+  if (c->p.use_graph) {
+    char key[64];
+    snprintf(key, sizeof key, "|%d|%p", (int)piw, (void*)c->weights);
+    std::string k = std::string(algorithm) + key;
+    if (k != c->gkey || !c->gexec) {
+      if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }
+      c->gkey.clear();
+      cudaGraph_t g = nullptr;
+      CDX_CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+      e = enqueue_run(c, steps, sw, piw);
+      cudaError_t ce = cudaStreamEndCapture(c->st, &g);
+      if (e) { if (g) cudaGraphDestroy(g); return e; }
+      if (ce != cudaSuccess) return set_error(CDX_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+      ce = cudaGraphInstantiate(&c->gexec, g, 0);
+      cudaGraphDestroy(g);
+      if (ce != cudaSuccess) return set_error(CDX_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce));
+      c->gkey = k;
+    }
+    CDX_CK(cudaEventRecord(c->ev0, c->st));
+    CDX_CK(cudaGraphLaunch(c->gexec, c->st));
+    CDX_CK(cudaEventRecord(c->ev1, c->st));
+  } else {
+    CDX_CK(cudaEventRecord(c->ev0, c->st));
+    e = enqueue_run(c, steps, sw, piw);
+    if (e) return e;
+    CDX_CK(cudaEventRecord(c->ev1, c->st));
+  }
+  if (c->last_iters > 0) c->psi_in_work = false;
+  c->fresh.assign(c->batch, 0);
+  c->psi_valid = true;
+  return CDX_OK;
+}
+
+int fill_stats(cdx_ctx* c, int idx, cdx_stats* s) {
+  if (!s) return CDX_OK;
+  PatState h;
+  CDX_CK(cudaMemcpyAsync(&h, c->dstate + idx, sizeof h, cudaMemcpyDeviceToHost, c->st));
+  CDX_CK(cudaStreamSynchronize(c->st));
+  memset(s, 0, sizeof *s);
+  s->steps = c->last_steps;
+  s->iterations = c->last_iters;
+  s->shrinkwraps = c->last_sw;
+  s->residual = h.residual;
+  s->rfactor = h.rfactor;
+  s->threshold = h.threshold;
+  s->flags = h.flags;
+  s->launches = c->last_launches;
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, c->ev0, c->ev1) == cudaSuccess) s->gpu_ms = ms;
+  else cudaGetLastError();
+  return CDX_OK;
+}
+
+}  // namespace
+
+// ====================================================================== C ABI
+extern "C" {
+
+int cdx_params_default(cdx_params* p) {
+  if (!p) return set_error(CDX_ERR_ARG, "null params");
+  memset(p, 0, sizeof *p);
+  p->batch = 1;
+  p->beta = 1.f;               // vars.beta_HIO (src/gpu/cdi.cu:22)
+  p->shrink_threshold = 0.f;   // readConfig default
+  p->oversampling_spt = 2.f;   // html/default/cdi.cfg
+  p->exposure = 1.f;
+  p->rcolor = 65535;           // include/format.hpp:20
+  p->shrink_mode = CDX_SHRINK_FOURIER;
+  p->sigma0 = 3.f;             // cdi.cc:314
+  p->sigma_min = 2.f;          // cdi.cc:338
+  p->sigma_decay = 0.99f;      // cdi.cc:339
+  p->use_graph = 1;
+  p->rf_every = 0;
+  return CDX_OK;
+}
+
+int cdx_size_supported(int n) { return size_supported(n) && n <= 4096 ? 1 : 0; }
+
+const char* cdx_last_error(void) { return last_error(); }
+const char* cdx_version(void) { return "cdx 0.1 (sm_103a)"; }
+
+int cdx_create(const cdx_params* p, void* stream, cdx_ctx** out) {
+  if (!p || !out) return set_error(CDX_ERR_ARG, "null argument");
+  *out = nullptr;
+  int e = check_len(p->rows);
+  if (e) return e;
+  if ((e = check_len(p->cols))) return e;
+  if (p->rows % 2 || p->cols % 2) return set_error(CDX_ERR_SIZE, "rows and cols must be even");
+  if (p->batch < 1 || p->batch > 65535) return set_error(CDX_ERR_ARG, "batch must be in [1, 65535]");
+  if (!(p->exposure > 0)) return set_error(CDX_ERR_ARG, "exposure must be > 0");
+  if (!(p->oversampling_spt > 0)) return set_error(CDX_ERR_ARG, "oversampling_spt must be > 0");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return set_error(CDX_ERR_NOLIB, "no CUDA device");
+  }
+  cdx_ctx* c = new cdx_ctx();
+  c->p = *p;
+  c->rows = p->rows;
+  c->cols = p->cols;
+  c->batch = p->batch;
+  c->npx = (long long)p->rows * p->cols;
+  c->wpr = (p->cols + 31) >> 5;
+  c->have_pattern.assign(p->batch, 0);
+  c->fresh.assign(p->batch, 0);
+  cudaGetDevice(&c->device);
+  auto fail = [&](int code) { cdx_destroy(c); return code; };
+  if (stream) {
+    c->st = (cudaStream_t)stream;
+  } else {
+    if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess)
+      return fail(set_error(CDX_ERR_CUDA, "stream create failed"));
+    c->own_stream = true;
+  }
+  if (prep_launcher(c->rows)() != cudaSuccess || prep_launcher(c->cols)() != cudaSuccess)
+    return fail(set_error(CDX_ERR_CUDA, std::string("kernel attributes: ") + cudaGetErrorString(cudaGetLastError())));
+  if ((e = twiddles(c->rows, &c->tw_r)) || (e = twiddles(c->cols, &c->tw_c))) return fail(e);
+  c->col_blocks = (c->cols + lines_per_cta(c->rows) - 1) / lines_per_cta(c->rows);
+  c->part_per_pat = std::max(kRedBlocks, c->col_blocks);
+  // one arena: 3 complex + 3 real arrays, bits, partials, state
+  const size_t B = (size_t)c->batch, N = (size_t)c->npx;
+  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  size_t off = 0;
+  const size_t o_rho = off; off += al(sizeof(float2) * B * N);
+  const size_t o_work = off; off += al(sizeof(float2) * B * N);
+  const size_t o_psi = off; off += al(sizeof(float2) * B * N);
+  const size_t o_int = off; off += al(sizeof(float) * B * N);
+  const size_t o_amp = off; off += al(sizeof(float) * B * N);
+  const size_t o_spt = off; off += al(sizeof(float) * B * N);
+  const size_t o_mask = off; off += al(sizeof(uint32_t) * B * c->rows * c->wpr);
+  const size_t o_part = off; off += al(sizeof(double) * B * c->part_per_pat);
+  const size_t o_pmax = off; off += al(sizeof(float) * B * kRedBlocks);
+  const size_t o_state = off; off += al(sizeof(PatState) * B);
+  if (cudaMalloc(&c->arena, off) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(set_error(CDX_ERR_NOMEM, "device arena of " + std::to_string(off) + " bytes"));
+  }
+  char* a = (char*)c->arena;
+  c->rho = (float2*)(a + o_rho);
+  c->work = (float2*)(a + o_work);
+  c->psi = (float2*)(a + o_psi);
+  c->inten = (float*)(a + o_int);
+  c->amp = (float*)(a + o_amp);
+  c->spt = (float*)(a + o_spt);
+  c->mask = (uint32_t*)(a + o_mask);
+  c->part = (double*)(a + o_part);
+  c->pmax = (float*)(a + o_pmax);
+  c->dstate = (PatState*)(a + o_state);
+  if (cudaMemsetAsync(c->arena, 0, off, c->st) != cudaSuccess)
+    return fail(set_error(CDX_ERR_CUDA, "arena clear failed"));
+  // vars.threshold starts at 0.5 (src/gpu/cdi.cu:21)
+  if (state_init(c->dstate, c->batch, 0.5f, c->st) != cudaSuccess)
+    return fail(set_error(CDX_ERR_CUDA, "state init failed"));
+  rect_of(c);
+  if ((e = reset_support(c, 0, c->batch))) return fail(e);
+  if (cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess)
+    return fail(set_error(CDX_ERR_CUDA, "event create failed"));
+  if (cudaStreamSynchronize(c->st) != cudaSuccess)
+    return fail(set_error(CDX_ERR_CUDA, std::string("context init: ") + cudaGetErrorString(cudaGetLastError())));
+  *out = c;
+  return CDX_OK;
+}
+
+int cdx_destroy(cdx_ctx* c) {
+  if (!c) return CDX_OK;
+  if (c->st) cudaStreamSynchronize(c->st);
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  if (c->weights) cudaFree(c->weights);
+  if (c->bs) cudaFree(c->bs);
+  if (c->arena) cudaFree(c->arena);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->own_stream && c->st) cudaStreamDestroy(c->st);
+  delete c;
+  return CDX_OK;
+}
+
+int cdx_get_params(const cdx_ctx* c, cdx_params* out) {
+  if (!c || !out) return set_error(CDX_ERR_ARG, "null argument");
+  *out = c->p;
+  return CDX_OK;
+}
+
+int cdx_device_arrays(cdx_ctx* c, float** pattern, void** fourier, void** object, float** support) {
+  if (!c) return set_error(CDX_ERR_ARG, "null context");
+  if (pattern) *pattern = c->inten;
+  if (fourier) *fourier = c->psi;
+  if (object) *object = c->rho;
+  if (support) *support = c->spt;
+  return CDX_OK;
+}
+
+int cdx_set_pattern(cdx_ctx* c, int idx, const float* inten, int where, int layout, float scale) {
+  if (!c || !inten || idx < 0 || idx >= c->batch) return set_error(CDX_ERR_ARG, "bad pattern argument");
+  const long long off = (long long)idx * c->npx;
+  int e = copy_in(c->inten + off, inten, sizeof(float) * c->npx, where, c->st);
+  if (e) return e;
+  if (layout == CDX_CENTERED) CDX_CK(convert_fo_real(c->inten + off, c->inten + off, c->rows, c->cols, 1, c->st));
+  if (scale != 1.f) CDX_CK(scale_real(c->inten + off, scale, c->npx, c->st));
+  CDX_CK(amp_from_pattern(c->inten + off, c->amp + off, c->npx, c->st));
+  CDX_CK(pattern_amp_sum(c->amp + off, c->npx, 1, c->part, kRedBlocks, c->dstate + idx, c->st));
+  CDX_CK(cudaStreamSynchronize(c->st));
+  c->have_pattern[idx] = 1;
+  return CDX_OK;
+}
+
+int cdx_set_beamstop(cdx_ctx* c, int idx, const float* bs, int where, int layout) {
+  if (!c || idx < 0 || idx >= c->batch) return set_error(CDX_ERR_ARG, "bad beamstop argument");
+  if (!bs) return CDX_OK;
+  if (!c->bs) {
+    CDX_CK(cudaMalloc(&c->bs, sizeof(float) * c->npx * c->batch));
+    CDX_CK(cudaMemsetAsync(c->bs, 0, sizeof(float) * c->npx * c->batch, c->st));
+  }
+  const long long off = (long long)idx * c->npx;
+  int e = copy_in(c->bs + off, bs, sizeof(float) * c->npx, where, c->st);
+  if (e) return e;
+  if (layout == CDX_CENTERED) CDX_CK(convert_fo_real(c->bs + off, c->bs + off, c->rows, c->cols, 1, c->st));
+  c->gkey.clear();
+  CDX_CK(cudaStreamSynchronize(c->st));
+  return CDX_OK;
+}
+
+static int init_rho_from_work(cdx_ctx* c, int idx, int count) {
+  // rho0 = IFFT(Psi0) * (1/sqrt(N)) (cdi.cc:225-226)
+  const long long off = (long long)idx * c->npx;
+  const float f = (float)(1.0 / std::sqrt((double)c->rows * c->cols));
+  int e = fft2_enqueue(c->work + off, c->rho + off, c->rows, c->cols, count, true, f, c->tw_r, c->tw_c, c->st);
+  if (e) return e;
+  return CDX_OK;
+}
+
+int cdx_set_initial(cdx_ctx* c, int idx, const float* psi0, int where) {
+  if (!c || !psi0 || idx < 0 || idx >= c->batch) return set_error(CDX_ERR_ARG, "bad initial-iterate argument");
+  const long long off = (long long)idx * c->npx;
+  int e = copy_in(c->work + off, psi0, sizeof(float2) * c->npx, where, c->st);
+  if (e) return e;
+  if ((e = init_rho_from_work(c, idx, 1))) return e;
+  if ((e = reset_support(c, idx, 1))) return e;   // initSupport (cdi.cc:227, 252-254)
+  CDX_CK(cudaStreamSynchronize(c->st));
+  // a batch restarts together: W holds Psi0 for every pattern once all are set
+  c->fresh[idx] = 1;
+  int nfresh = 0;
+  for (char f : c->fresh) nfresh += f;
+  c->have_initial = true;
+  c->psi_in_work = nfresh == c->batch;
+  c->psi_valid = false;
+  return CDX_OK;
+}
+
+int cdx_random_start(cdx_ctx* c, unsigned long long seed) {
+  if (!c) return set_error(CDX_ERR_ARG, "null context");
+  for (int i = 0; i < c->batch; ++i)
+    if (!c->have_pattern[i]) return set_error(CDX_ERR_STATE, "pattern " + std::to_string(i) + " not set");
+  PatState h0;
+  CDX_CK(cudaMemcpy(&h0, c->dstate, sizeof h0, cudaMemcpyDeviceToHost));
+  CDX_CK(random_start(c->inten, c->bs, h0.threshold, c->work, c->npx, c->batch, seed, c->st));
+  int e = init_rho_from_work(c, 0, c->batch);
+  if (e) return e;
+  if ((e = reset_support(c, 0, c->batch))) return e;
+  CDX_CK(cudaStreamSynchronize(c->st));
+  c->fresh.assign(c->batch, 1);
+  c->have_initial = true;
+  c->psi_in_work = true;
+  c->psi_valid = false;
+  return CDX_OK;
+}
+
+int cdx_set_support(cdx_ctx* c, int idx, const float* support, int where) {
+  if (!c || !support || idx < 0 || idx >= c->batch) return set_error(CDX_ERR_ARG, "bad support argument");
+  const long long off = (long long)idx * c->npx;
+  int e = copy_in(c->spt + off, support, sizeof(float) * c->npx, where, c->st);
+  if (e) return e;
+  CDX_CK(support_bits(c->spt + off, c->dstate + idx, 0.f, c->mask + (long long)idx * c->rows * c->wpr, c->rows,
+                      c->cols, 1, c->st));
+  CDX_CK(cudaStreamSynchronize(c->st));
+  return CDX_OK;
+}
+
+int cdx_run_async(cdx_ctx* c, const char* algorithm) { return run_impl(c, algorithm); }
+
+int cdx_run(cdx_ctx* c, const char* algorithm, cdx_stats* stats) {
+  int e = run_impl(c, algorithm);
+  if (e) return e;
+  CDX_CK(cudaStreamSynchronize(c->st));
+  return fill_stats(c, 0, stats);
+}
+
+int cdx_get_stats(cdx_ctx* c, int idx, cdx_stats* s) {
+  if (!c || idx < 0 || idx >= c->batch) return set_error(CDX_ERR_ARG, "bad stats argument");
+  return fill_stats(c, idx, s);
+}
+
+int cdx_get_object(cdx_ctx* c, int idx, float* out, int where) {
+  if (!c || !out || idx < 0 || idx >= c->batch) return set_error(CDX_ERR_ARG, "bad output argument");
+  return copy_out(out, c->rho + (long long)idx * c->npx, sizeof(float2) * c->npx, where, c->st);
+}
+int cdx_get_fourier(cdx_ctx* c, int idx, float* out, int where) {
+  if (!c || !out || idx < 0 || idx >= c->batch) return set_error(CDX_ERR_ARG, "bad output argument");
+  const float2* src = c->psi_valid ? c->psi : c->work;   // before any run W holds Psi0
+  return copy_out(out, src + (long long)idx * c->npx, sizeof(float2) * c->npx, where, c->st);
+}
+int cdx_get_support(cdx_ctx* c, int idx, float* out, int where) {
+  if (!c || !out || idx < 0 || idx >= c->batch) return set_error(CDX_ERR_ARG, "bad output argument");
+  return copy_out(out, c->spt + (long long)idx * c->npx, sizeof(float) * c->npx, where, c->st);
+}
+
+int cdx_phase_retrieve_host(const cdx_params* p, const char* algorithm, const float* inten, const float* psi0,
+                            unsigned long long seed, float* rho_out, float* psi_out, float* support_out,
+                            cdx_stats* stats) {
+  if (!p || !inten) return set_error(CDX_ERR_ARG, "null argument");
+  cdx_params q = *p;
+  q.batch = 1;
+  cdx_ctx* c = nullptr;
+  int e = cdx_create(&q, nullptr, &c);
+  if (e) return e;
+  if ((e = cdx_set_pattern(c, 0, inten, CDX_HOST, CDX_FFT_ORDER, 1.f))) goto done;
+  e = psi0 ? cdx_set_initial(c, 0, psi0, CDX_HOST) : cdx_random_start(c, seed);
+  if (e) goto done;
+  if ((e = cdx_run(c, algorithm, stats))) goto done;
+  if (rho_out && (e = cdx_get_object(c, 0, rho_out, CDX_HOST))) goto done;
+  if (psi_out && (e = cdx_get_fourier(c, 0, psi_out, CDX_HOST))) goto done;
+  if (support_out && (e = cdx_get_support(c, 0, support_out, CDX_HOST))) goto done;
+done:
+  cdx_destroy(c);
+  return e;
+}
+
+// ---------------------------------------------------------------- primitives
+int cdx_fft2(const void* in, void* out, int rows, int cols, int batch, int inverse, void* stream) {
+  if (!in || !out || batch < 1) return set_error(CDX_ERR_ARG, "bad fft argument");
+  int e = check_len(rows);
+  if (e) return e;
+  if ((e = check_len(cols))) return e;
+  if (prep_launcher(rows)() != cudaSuccess || prep_launcher(cols)() != cudaSuccess)
+    return set_error(CDX_ERR_CUDA, "kernel attributes");
+  float2 *tr, *tc;
+  if ((e = twiddles(rows, &tr)) || (e = twiddles(cols, &tc))) return e;
+  return fft2_enqueue((const float2*)in, (float2*)out, rows, cols, batch, inverse != 0, 1.f, tr, tc,
+                      (cudaStream_t)stream);
+}
+
+int cdx_apply_mod_abs(void* psi, const float* inten, long long n, void* stream) {
+  if (!psi || !inten || n < 0) return set_error(CDX_ERR_ARG, "bad argument");
+  CDX_CK(mod_abs((float2*)psi, inten, n, (cudaStream_t)stream));
+  return CDX_OK;
+}
+
+int cdx_apply_mod(void* psi, const float* inten, const float* bs, int noise, float scale, int rcolor, long long n,
+                  void* stream) {
+  if (!psi || !inten || n < 0 || rcolor == 0 || scale == 0) return set_error(CDX_ERR_ARG, "bad argument");
+  CDX_CK(mod_ccd((float2*)psi, inten, bs, noise, scale, (float)rcolor, n, (cudaStream_t)stream));
+  return CDX_OK;
+}
+
+int cdx_apply_support(void* rho, const void* rhop, const float* spt, float thr, float beta, int algo, long long n,
+                      void* stream) {
+  if (!rho || !rhop || !spt || n < 0) return set_error(CDX_ERR_ARG, "bad argument");
+  CDX_CK(apply_support((float2*)rho, (const float2*)rhop, spt, thr, beta, algo, n, (cudaStream_t)stream));
+  return CDX_OK;
+}
+
+int cdx_convert_fo(const void* in, void* out, int rows, int cols, int batch, int is_complex, void* stream) {
+  if (!in || !out || rows < 2 || cols < 2 || batch < 1 || rows % 2 || cols % 2)
+    return set_error(CDX_ERR_ARG, "bad argument");
+  if (in != out && is_complex)
+    CDX_CK(cudaMemcpyAsync(out, in, sizeof(float2) * rows * cols * batch, cudaMemcpyDeviceToDevice, (cudaStream_t)stream));
+  if (in != out && !is_complex)
+    CDX_CK(cudaMemcpyAsync(out, in, sizeof(float) * rows * cols * batch, cudaMemcpyDeviceToDevice, (cudaStream_t)stream));
+  if (is_complex) CDX_CK(convert_fo_complex((const float2*)out, (float2*)out, rows, cols, batch, (cudaStream_t)stream));
+  else CDX_CK(convert_fo_real((const float*)out, (float*)out, rows, cols, batch, (cudaStream_t)stream));
+  return CDX_OK;
+}
+
+int cdx_algo_expand(const char* algorithm, int* out, int cap, int* count) {
+  std::vector<int> v;
+  int e = algo_expand(algorithm, v, 50000000);
+  if (e) return e;
+  if (count) *count = (int)v.size();
+  if (out)
+    for (int i = 0; i < (int)v.size() && i < cap; ++i) out[i] = v[i];
+  return CDX_OK;
+}
+
+int cdx_read_bin(const char* path, int* rows, int* cols, int* is_complex, float* data, size_t cap) {
+  if (!path || !rows || !cols || !is_complex) return set_error(CDX_ERR_ARG, "null argument");
+  return read_bin(path, rows, cols, is_complex, data, cap);
+}
+int cdx_write_bin(const char* path, const float* data, int rows, int cols, int is_complex) {
+  if (!path || !data || rows <= 0 || cols <= 0) return set_error(CDX_ERR_ARG, "bad argument");
+  return write_bin(path, data, rows, cols, is_complex);
+}
+
+}  // extern "C"

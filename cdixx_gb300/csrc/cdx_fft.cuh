@@ -1,0 +1,239 @@
+// Shared-memory FFT engine for the CDI phase-retrieval kernels (sm_103a).
+//
+// A CTA holds L lines of length N in shared memory and transforms all of them
+// with a self-sorting (Stockham, decimation-in-time) mixed-radix schedule:
+// pass p with radix R and sub-length NS = R_0*...*R_{p-1} maps butterfly j
+// (k = j mod NS) to
+//     v_r = in[j + r*N/R] * W_{NS*R}^{r*k},   v = DFT_R(v),
+//     out[(j-k)*R + k + r*NS] = v_r,
+// which leaves the result in natural order.  Every pass is done in place:
+// each thread first loads all of its butterflies into registers, the CTA
+// synchronises, then the butterflies are computed and stored.
+//
+// The transform is the unnormalised DFT of cuFFT's C2C plans (forward
+// exp(-2 pi i k n/N), inverse exp(+2 pi i k n/N)), which is what the reference
+// calls through myFFT/myIFFT (src/gpu/cudaConfig.cu:175-180).  Twiddles come
+// from a table W_N^t = exp(-2 pi i t/N) computed in double precision on the
+// host and rounded once to float.
+//
+// Shared-memory layout: element i of line l sits at l*LD + i + (i >> 4), with
+// LD = N + N/16 + 1.  The skew keeps the strided stores of the first pass and
+// the column-tile loads free of bank conflicts for 64-bit accesses.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace cdx {
+
+#define CDX_HD __host__ __device__ __forceinline__
+
+CDX_HD float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+CDX_HD float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+CDX_HD float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// multiply by -i (forward) or +i (inverse)
+template <bool INV>
+CDX_HD float2 rot90(float2 a) {
+  return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+}
+
+// ---------------------------------------------------------------- small DFTs
+template <bool INV>
+CDX_HD void dft2(float2& a, float2& b) {
+  float2 t = a;
+  a = cadd(t, b);
+  b = csub(t, b);
+}
+
+template <bool INV>
+CDX_HD void dft3(float2* v) {
+  const float s3 = 0.866025403784438647f;   // sqrt(3)/2
+  float2 t1 = cadd(v[1], v[2]);
+  float2 t2 = csub(v[1], v[2]);
+  float2 m = make_float2(v[0].x - 0.5f * t1.x, v[0].y - 0.5f * t1.y);
+  float2 r = rot90<INV>(make_float2(s3 * t2.x, s3 * t2.y));
+  v[0] = cadd(v[0], t1);
+  v[1] = cadd(m, r);
+  v[2] = csub(m, r);
+}
+
+template <bool INV>
+CDX_HD void dft4(float2& x0, float2& x1, float2& x2, float2& x3) {
+  float2 a = cadd(x0, x2), b = csub(x0, x2);
+  float2 c = cadd(x1, x3), d = rot90<INV>(csub(x1, x3));
+  x0 = cadd(a, c);
+  x2 = csub(a, c);
+  x1 = cadd(b, d);
+  x3 = csub(b, d);
+}
+
+template <bool INV>
+CDX_HD void dft8(float2* v) {
+  const float h = 0.707106781186547524f;
+  // even / odd radix-4 halves
+  float2 e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
+  float2 o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
+  dft4<INV>(e0, e1, e2, e3);
+  dft4<INV>(o0, o1, o2, o3);
+  // W8^k, k = 1..3 (forward: exp(-i pi k/4))
+  float2 w1 = INV ? make_float2(h * (o1.x - o1.y), h * (o1.x + o1.y))
+                  : make_float2(h * (o1.x + o1.y), h * (o1.y - o1.x));
+  float2 w2 = rot90<INV>(o2);
+  float2 w3 = INV ? make_float2(-h * (o3.x + o3.y), h * (o3.x - o3.y))
+                  : make_float2(h * (o3.y - o3.x), -h * (o3.x + o3.y));
+  v[0] = cadd(e0, o0); v[4] = csub(e0, o0);
+  v[1] = cadd(e1, w1); v[5] = csub(e1, w1);
+  v[2] = cadd(e2, w2); v[6] = csub(e2, w2);
+  v[3] = cadd(e3, w3); v[7] = csub(e3, w3);
+}
+
+template <bool INV>
+CDX_HD void dft16(float2* v) {
+  // 16 = 4 x 4: n = 4*n1 + n2, k = k1 + 4*k2
+  const float c1 = 0.923879532511286756f;   // cos(pi/8)
+  const float s1 = 0.382683432365089772f;   // sin(pi/8)
+  const float h = 0.707106781186547524f;
+#pragma unroll
+  for (int n2 = 0; n2 < 4; ++n2) dft4<INV>(v[n2], v[4 + n2], v[8 + n2], v[12 + n2]);
+  // after the inner DFTs, v[4*k1 + n2] holds A[n2][k1]; twiddle by W16^(n2*k1)
+  const float sg = INV ? 1.f : -1.f;
+  // (n2,k1) = (1,1): W16^1, (1,2): W16^2, (1,3): W16^3, (2,1): W16^2, (2,2): W16^4,
+  // (2,3): W16^6, (3,1): W16^3, (3,2): W16^6, (3,3): W16^9
+  const float2 w1 = make_float2(c1, sg * s1);
+  const float2 w2 = make_float2(h, sg * h);
+  const float2 w3 = make_float2(s1, sg * c1);
+  const float2 w6 = make_float2(-h, sg * h);
+  const float2 w9 = make_float2(-c1, -sg * s1);
+  v[4 + 1] = cmul(v[4 + 1], w1);
+  v[8 + 1] = cmul(v[8 + 1], w2);
+  v[12 + 1] = cmul(v[12 + 1], w3);
+  v[4 + 2] = cmul(v[4 + 2], w2);
+  v[8 + 2] = rot90<INV>(v[8 + 2]);
+  v[12 + 2] = cmul(v[12 + 2], w6);
+  v[4 + 3] = cmul(v[4 + 3], w3);
+  v[8 + 3] = cmul(v[8 + 3], w6);
+  v[12 + 3] = cmul(v[12 + 3], w9);
+  // outer DFTs over n2 for each k1; result X[k1 + 4*k2]
+  float2 t[16];
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) {
+    float2 a0 = v[4 * k1 + 0], a1 = v[4 * k1 + 1], a2 = v[4 * k1 + 2], a3 = v[4 * k1 + 3];
+    dft4<INV>(a0, a1, a2, a3);
+    t[k1 + 0] = a0; t[k1 + 4] = a1; t[k1 + 8] = a2; t[k1 + 12] = a3;
+  }
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = t[i];
+}
+
+template <int R, bool INV>
+CDX_HD void dftR(float2* v) {
+  if constexpr (R == 2) dft2<INV>(v[0], v[1]);
+  else if constexpr (R == 3) dft3<INV>(v);
+  else if constexpr (R == 4) dft4<INV>(v[0], v[1], v[2], v[3]);
+  else if constexpr (R == 8) dft8<INV>(v);
+  else if constexpr (R == 16) dft16<INV>(v);
+  else static_assert(R == 2, "unsupported radix");
+}
+
+// ---------------------------------------------------------------- plans
+// radix of pass p for length N: as many 16s as divide N, then 8, 4, 2, then 3s.
+__host__ __device__ constexpr int plan_radix(int n, int p) {
+  int m = n;
+  int q = 0;
+  while (m % 16 == 0) { if (q == p) return 16; m /= 16; ++q; }
+  const int rs[3] = {8, 4, 2};
+  for (int i = 0; i < 3; ++i)
+    while (m % rs[i] == 0) { if (q == p) return rs[i]; m /= rs[i]; ++q; }
+  while (m % 3 == 0) { if (q == p) return 3; m /= 3; ++q; }
+  return 0;  // past the last pass
+}
+__host__ __device__ constexpr int plan_ns(int n, int p) {
+  int ns = 1;
+  for (int i = 0; i < p; ++i) ns *= plan_radix(n, i);
+  return ns;
+}
+__host__ __device__ constexpr bool size_supported(int n) {
+  if (n < 16) return false;
+  int m = n;
+  while (m % 2 == 0) m /= 2;
+  while (m % 3 == 0) m /= 3;
+  return m == 1;
+}
+
+template <int N>
+struct Layout {
+  static constexpr int LD = N + (N >> 4) + 1;
+  __device__ __forceinline__ static int idx(int l, int i) { return l * LD + i + (i >> 4); }
+};
+
+// One Stockham pass over L lines with T threads.
+template <int N, int L, int T, int P, bool INV>
+__device__ __forceinline__ void fft_pass(float2* buf, const float2* tw) {
+  constexpr int R = plan_radix(N, P);
+  constexpr int NS = plan_ns(N, P);
+  constexpr int NR = N / R;
+  constexpr int NB = L * NR;
+  constexpr int B = (NB + T - 1) / T;
+  using LY = Layout<N>;
+  float2 v[B][R];
+#pragma unroll
+  for (int b = 0; b < B; ++b) {
+    const int g = threadIdx.x + b * T;
+    if ((NB % T) == 0 || g < NB) {
+      const int l = g / NR, j = g - l * NR;
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[b][r] = buf[LY::idx(l, j + r * NR)];
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int b = 0; b < B; ++b) {
+    const int g = threadIdx.x + b * T;
+    if ((NB % T) == 0 || g < NB) {
+      const int l = g / NR, j = g - l * NR;
+      const int k = j % NS;
+      if constexpr (NS > 1) {
+        constexpr int STEP = N / (NS * R);
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+          float2 w = tw[r * k * STEP];
+          if (INV) w.y = -w.y;
+          v[b][r] = cmul(v[b][r], w);
+        }
+      }
+      dftR<R, INV>(v[b]);
+      const int base = (j - k) * R + k;
+#pragma unroll
+      for (int r = 0; r < R; ++r) buf[LY::idx(l, base + r * NS)] = v[b][r];
+    }
+  }
+  __syncthreads();
+}
+
+template <int N, int L, int T, int P, bool INV>
+__device__ __forceinline__ void fft_passes(float2* buf, const float2* tw) {
+  if constexpr (plan_radix(N, P) != 0) {
+    fft_pass<N, L, T, P, INV>(buf, tw);
+    fft_passes<N, L, T, P + 1, INV>(buf, tw);
+  }
+}
+
+// Transform all L lines in place.  Callers synchronise before the call (the
+// lines must be fully written); the call ends with a barrier.
+template <int N, int L, int T, bool INV>
+__device__ __forceinline__ void fft_lines(float2* buf, const float2* tw) {
+  fft_passes<N, L, T, 0, INV>(buf, tw);
+}
+
+// Launch geometry per length: L lines per CTA and T threads, so that each
+// thread holds about 16 complex values per pass.
+template <int N>
+struct Geom {
+  static constexpr int T = N >= 768 ? 512 : 256;
+  static constexpr int ELEMS = 16 * T;
+  static constexpr int L = (ELEMS / N) < 1 ? 1 : (ELEMS / N);
+  static constexpr int SMEM = (N + L * Layout<N>::LD) * (int)sizeof(float2);
+};
+
+}  // namespace cdx

@@ -1,0 +1,385 @@
+// Element-wise primitives, shrinkwrap stencil, deterministic reductions and
+// initialisation kernels of the CDI path (sm_103a).
+#include "cdx_misc.h"
+#include "cdx_kernels.cuh"
+
+namespace cdx {
+
+static inline unsigned grid1d(long long n, int t, int cap = 152 * 16) {
+  long long b = (n + t - 1) / t;
+  return (unsigned)(b < 1 ? 1 : (b > cap ? cap : b));
+}
+
+// ---------------------------------------------------------------- element-wise
+// sqrt(I) as applyModAbs forms it (src/gpu/cudaConfig.cu:830-832): I > 0 -> sqrtf(I), else 0.
+__global__ void k_amp(const float* __restrict__ inten, float* __restrict__ amp, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    float v = inten[i];
+    amp[i] = v > 0.f ? sqrtf(v) : 0.f;
+  }
+}
+cudaError_t amp_from_pattern(const float* inten, float* amp, long long n, cudaStream_t st) {
+  k_amp<<<grid1d(n, 256), 256, 0, st>>>(inten, amp, n);
+  return cudaGetLastError();
+}
+
+// applyNorm (src/gpu/cudaConfig.cu:425-429)
+__global__ void k_scale(float2* __restrict__ x, float s, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    float2 v = x[i];
+    v.x *= s;
+    v.y *= s;
+    x[i] = v;
+  }
+}
+cudaError_t scale_complex(float2* x, float s, long long n, cudaStream_t st) {
+  k_scale<<<grid1d(n, 256), 256, 0, st>>>(x, s, n);
+  return cudaGetLastError();
+}
+
+__global__ void k_scale_real(float* __restrict__ x, float s, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    x[i] *= s;
+}
+cudaError_t scale_real(float* x, float s, long long n, cudaStream_t st) {
+  k_scale_real<<<grid1d(n, 256), 256, 0, st>>>(x, s, n);
+  return cudaGetLastError();
+}
+
+// cudaConvertFO (src/gpu/cudaConfig.cu:202-212): swap quadrants (even sizes).
+template <typename V>
+__global__ void k_convert_fo(const V* __restrict__ in, V* __restrict__ out, int rows, int cols, int batch) {
+  const long long half = (long long)rows * cols / 2;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < half * batch;
+       g += (long long)gridDim.x * blockDim.x) {
+    const long long p = g / half, i = g - p * half;
+    const int x = (int)(i / cols), y = (int)(i - (long long)x * cols);
+    const long long j = (long long)(x + (rows >> 1)) * cols + (y >= (cols >> 1) ? y - (cols >> 1) : y + (cols >> 1));
+    const long long base = p * (long long)rows * cols;
+    V a = in[base + i], b = in[base + j];
+    out[base + i] = b;
+    out[base + j] = a;
+  }
+}
+cudaError_t convert_fo_real(const float* in, float* out, int rows, int cols, int batch, cudaStream_t st) {
+  k_convert_fo<float><<<grid1d((long long)rows * cols / 2 * batch, 256), 256, 0, st>>>(in, out, rows, cols, batch);
+  return cudaGetLastError();
+}
+cudaError_t convert_fo_complex(const float2* in, float2* out, int rows, int cols, int batch, cudaStream_t st) {
+  k_convert_fo<float2><<<grid1d((long long)rows * cols / 2 * batch, 256), 256, 0, st>>>(in, out, rows, cols, batch);
+  return cudaGetLastError();
+}
+
+// Unfused primitives with the reference's element-wise semantics.
+__global__ void k_mod_abs(float2* __restrict__ psi, const float* __restrict__ inten, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    float v = inten[i];
+    psi[i] = proj_modabs(psi[i], v > 0.f ? sqrtf(v) : 0.f);
+  }
+}
+cudaError_t mod_abs(float2* psi, const float* inten, long long n, cudaStream_t st) {
+  k_mod_abs<<<grid1d(n, 256), 256, 0, st>>>(psi, inten, n);
+  return cudaGetLastError();
+}
+__global__ void k_mod_ccd(float2* __restrict__ psi, const float* __restrict__ inten, const float* __restrict__ bs,
+                          int noise, float scale, float rcolor, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    psi[i] = proj_ccd(psi[i], inten[i], bs ? bs[i] : 0.f, bs != nullptr, noise, scale, rcolor);
+}
+cudaError_t mod_ccd(float2* psi, const float* inten, const float* bs, int noise, float scale, float rcolor,
+                    long long n, cudaStream_t st) {
+  k_mod_ccd<<<grid1d(n, 256), 256, 0, st>>>(psi, inten, bs, noise, scale, rcolor, n);
+  return cudaGetLastError();
+}
+__global__ void k_support(float2* __restrict__ rho, const float2* __restrict__ rhop, const float* __restrict__ spt,
+                          float thr, float beta, int algo, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    rho[i] = apply_update(algo, spt[i] > thr, rho[i], rhop[i], beta);
+}
+cudaError_t apply_support(float2* rho, const float2* rhop, const float* spt, float thr, float beta, int algo,
+                          long long n, cudaStream_t st) {
+  k_support<<<grid1d(n, 256), 256, 0, st>>>(rho, rhop, spt, thr, beta, algo, n);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ supports
+// createMask<rect> (src/gpu/cudaConfig.cu:1291-1300): 1 inside [sx,ex) x [sy,ey).
+__global__ void k_rect(float* __restrict__ spt, int rows, int cols, int batch, int sx, int sy, int ex, int ey) {
+  const long long npx = (long long)rows * cols;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < npx * batch; g += (long long)gridDim.x * blockDim.x) {
+    const long long i = g % npx;
+    const int x = (int)(i / cols), y = (int)(i - (long long)x * cols);
+    spt[g] = (x >= sx && x < ex && y >= sy && y < ey) ? 1.f : 0.f;
+  }
+}
+cudaError_t rect_support(float* spt, int rows, int cols, int batch, int sx, int sy, int ex, int ey, cudaStream_t st) {
+  k_rect<<<grid1d((long long)rows * cols * batch, 256), 256, 0, st>>>(spt, rows, cols, batch, sx, sy, ex, ey);
+  return cudaGetLastError();
+}
+
+// Support bits: bit = spt > threshold of the pattern (the test of cdi.cu:525).
+// One warp per 32 columns of one row.
+__global__ void k_mask(const float* __restrict__ spt, const PatState* __restrict__ stt, float fixed_thr,
+                       uint32_t* __restrict__ bits, int rows, int cols, int batch) {
+  const int wpr = (cols + 31) >> 5;
+  const long long words = (long long)rows * wpr;
+  const long long nw = words * batch;
+  const int lane = threadIdx.x & 31;
+  for (long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; w < nw;
+       w += ((long long)gridDim.x * blockDim.x) >> 5) {
+    const long long p = w / words, r = (w - p * words) / wpr, cw = (w - p * words) - r * wpr;
+    const int c = (int)cw * 32 + lane;
+    const float thr = stt ? stt[p].threshold : fixed_thr;
+    bool in = false;
+    if (c < cols) in = spt[p * (long long)rows * cols + r * cols + c] > thr;
+    const uint32_t b = __ballot_sync(0xffffffffu, in);
+    if (lane == 0) bits[w] = b;
+  }
+}
+cudaError_t support_bits(const float* spt, const PatState* st_or_null, float fixed_thr, uint32_t* bits, int rows,
+                         int cols, int batch, cudaStream_t st) {
+  const long long nw = (long long)rows * ((cols + 31) >> 5) * batch;
+  k_mask<<<grid1d(nw * 32, 256), 256, 0, st>>>(spt, st_or_null, fixed_thr, bits, rows, cols, batch);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- shrinkwrap
+// Circular separable convolution.  First along the rows index (x), reading rho
+// (or |rho|^2 as a real field), then along the columns index (y), writing the
+// real support field: |s*v|^2 (Fourier-Gaussian mode, s = rows*cols restores
+// the unnormalised IFFT scale of the reference) or Re v (|rho|^2 mode).
+__global__ void k_blur_x(const float2* __restrict__ rho, float2* __restrict__ tmp, const float* __restrict__ w,
+                         int rad, int rows, int cols, int batch, int mod2_first) {
+  const long long npx = (long long)rows * cols;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < npx * batch; g += (long long)gridDim.x * blockDim.x) {
+    const long long p = g / npx, i = g - p * npx;
+    const int x = (int)(i / cols), y = (int)(i - (long long)x * cols);
+    const float2* src = rho + p * npx;
+    float sx = 0.f, sy = 0.f;
+    for (int d = -rad; d <= rad; ++d) {
+      int xx = x + d;
+      xx = xx < 0 ? xx + rows : (xx >= rows ? xx - rows : xx);
+      float2 v = src[(long long)xx * cols + y];
+      const float wd = w[d + rad];
+      if (mod2_first) {
+        sx = fmaf(wd, v.x * v.x + v.y * v.y, sx);
+      } else {
+        sx = fmaf(wd, v.x, sx);
+        sy = fmaf(wd, v.y, sy);
+      }
+    }
+    tmp[g] = make_float2(sx, sy);
+  }
+}
+
+__global__ void k_blur_y(const float2* __restrict__ tmp, float* __restrict__ spt, const float* __restrict__ w,
+                         int rad, int rows, int cols, int batch, int mod2_first, float s,
+                         float* __restrict__ pmax, double* __restrict__ psum, int nblk_per_pat) {
+  // grid: (nblk_per_pat, batch)
+  const long long npx = (long long)rows * cols;
+  const long long p = blockIdx.y;
+  const float2* src = tmp + p * npx;
+  float* out = spt + p * npx;
+  float m = 0.f;   // findMax initialises with 0 (src/gpu/cub_wrap.cu:88-92)
+  double acc = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npx; i += (long long)nblk_per_pat * blockDim.x) {
+    const int x = (int)(i / cols), y = (int)(i - (long long)x * cols);
+    const float2* row = src + (long long)x * cols;
+    float sx = 0.f, sy = 0.f;
+    for (int d = -rad; d <= rad; ++d) {
+      int yy = y + d;
+      yy = yy < 0 ? yy + cols : (yy >= cols ? yy - cols : yy);
+      const float2 v = row[yy];
+      const float wd = w[d + rad];
+      sx = fmaf(wd, v.x, sx);
+      sy = fmaf(wd, v.y, sy);
+    }
+    float o;
+    if (mod2_first) {
+      o = sx;
+    } else {
+      sx *= s;
+      sy *= s;
+      o = sx * sx + sy * sy;
+    }
+    out[i] = o;
+    m = fmaxf(m, o);   // a NaN input is dropped by fmaxf; the finaliser checks the sum
+    acc += (double)o;
+  }
+  __shared__ float sm[32];
+  __shared__ double sd[32];
+  m = warp_max_f(m);
+  acc = warp_sum_d(acc);
+  const int wid = threadIdx.x >> 5, ln = threadIdx.x & 31;
+  if (ln == 0) { sm[wid] = m; sd[wid] = acc; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float mm = 0.f;
+    double ss = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) { mm = fmaxf(mm, sm[i]); ss += sd[i]; }
+    pmax[p * nblk_per_pat + blockIdx.x] = mm;
+    psum[p * nblk_per_pat + blockIdx.x] = ss;
+  }
+}
+
+// Threshold logic of the shrinkwrap block (src/post_gpu/cdi.cc:330-337):
+// maxs = findMax; first time avg = findSum*4/rows/cols; maxs = min(maxs, 5*avg);
+// threshold = maxs*shrinkThreshold.  |rho|^2 mode: threshold = max*shrinkThreshold.
+__global__ void k_shrink_finalize(const float* __restrict__ pmax, const double* __restrict__ psum, int nblk,
+                                  PatState* __restrict__ stt, int rows, int cols, int mod2_first,
+                                  double shrink_threshold) {
+  const int p = blockIdx.x;
+  if (threadIdx.x != 0) return;
+  float m = 0.f;
+  double s = 0.0;
+  for (int i = 0; i < nblk; ++i) { m = fmaxf(m, pmax[p * nblk + i]); s += psum[p * nblk + i]; }
+  PatState& S = stt[p];
+  S.maxv = m;
+  S.sum = (float)s;
+  if (s != s) S.flags |= 1;
+  if (!mod2_first) {
+    if (S.avg == 0.f) S.avg = (float)s * 4.f / (float)rows / (float)cols;
+    if (S.avg * 5.f < m) m = S.avg * 5.f;
+  }
+  if (fabsf(m) < 1e-7f || m != m) S.flags |= 1;
+  S.threshold = (float)((double)m * shrink_threshold);
+}
+
+cudaError_t shrinkwrap(const float2* rho, float2* tmp, float* spt, const float* wx, int radx, const float* wy,
+                       int rady, int rows, int cols, int batch, int mod2_first, float s, float* pmax, double* psum,
+                       int nblk, PatState* stt, double shrink_threshold, cudaStream_t st) {
+  const long long n = (long long)rows * cols * batch;
+  k_blur_x<<<grid1d(n, 256), 256, 0, st>>>(rho, tmp, wx, radx, rows, cols, batch, mod2_first);
+  k_blur_y<<<dim3(nblk, batch), 256, 0, st>>>(tmp, spt, wy, rady, rows, cols, batch, mod2_first, s, pmax, psum, nblk);
+  k_shrink_finalize<<<batch, 32, 0, st>>>(pmax, psum, nblk, stt, rows, cols, mod2_first, shrink_threshold);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- reductions
+// Per pattern: sum sqrt(I) (R-factor denominator).
+__global__ void k_sum_real(const float* __restrict__ x, long long npx, double* __restrict__ part, int nblk) {
+  const long long p = blockIdx.y;
+  double acc = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npx; i += (long long)nblk * blockDim.x)
+    acc += (double)x[p * npx + i];
+  __shared__ double red[8];
+  double t = block_sum_d<256>(acc, red);
+  if (threadIdx.x == 0) part[p * nblk + blockIdx.x] = t;
+}
+// Residual of src/post_gpu/cdi.cc:413-421: sum (|Psi|^2 - I)^2 over I < 0.99.
+__global__ void k_residual(const float2* __restrict__ psi, const float* __restrict__ inten, long long npx,
+                           double* __restrict__ part, int nblk) {
+  const long long p = blockIdx.y;
+  double acc = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npx; i += (long long)nblk * blockDim.x) {
+    const float2 v = psi[p * npx + i];
+    const float I = inten[p * npx + i];
+    float d = v.x * v.x + v.y * v.y;
+    d = I < 0.99f ? d - I : 0.f;
+    acc += (double)d * (double)d;
+  }
+  __shared__ double red[8];
+  double t = block_sum_d<256>(acc, red);
+  if (threadIdx.x == 0) part[p * nblk + blockIdx.x] = t;
+}
+// R-factor of a complete Psi: sum | |Psi| - sqrt(I) |.
+__global__ void k_rdiff(const float2* __restrict__ psi, const float* __restrict__ amp, long long npx,
+                        double* __restrict__ part, int nblk) {
+  const long long p = blockIdx.y;
+  double acc = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npx; i += (long long)nblk * blockDim.x) {
+    const float2 v = psi[p * npx + i];
+    acc += (double)fabsf(hypotf(v.x, v.y) - amp[p * npx + i]);
+  }
+  __shared__ double red[8];
+  double t = block_sum_d<256>(acc, red);
+  if (threadIdx.x == 0) part[p * nblk + blockIdx.x] = t;
+}
+
+// Fixed-order final sums.  what: 0 amp_sum, 1 residual, 2 rfactor (= sum / amp_sum).
+__global__ void k_finalize_sum(const double* __restrict__ part, int nblk, PatState* __restrict__ stt, int what) {
+  const int p = blockIdx.x;
+  if (threadIdx.x != 0) return;
+  double s = 0.0;
+  for (int i = 0; i < nblk; ++i) s += part[p * nblk + i];
+  if (what == 0) stt[p].amp_sum = s;
+  else if (what == 1) stt[p].residual = s;
+  else stt[p].rfactor = stt[p].amp_sum > 0.0 ? s / stt[p].amp_sum : 0.0;
+}
+
+cudaError_t pattern_amp_sum(const float* amp, long long npx, int batch, double* part, int nblk, PatState* stt,
+                            cudaStream_t st) {
+  k_sum_real<<<dim3(nblk, batch), 256, 0, st>>>(amp, npx, part, nblk);
+  k_finalize_sum<<<batch, 32, 0, st>>>(part, nblk, stt, 0);
+  return cudaGetLastError();
+}
+cudaError_t residual(const float2* psi, const float* inten, long long npx, int batch, double* part, int nblk,
+                     PatState* stt, cudaStream_t st) {
+  k_residual<<<dim3(nblk, batch), 256, 0, st>>>(psi, inten, npx, part, nblk);
+  k_finalize_sum<<<batch, 32, 0, st>>>(part, nblk, stt, 1);
+  return cudaGetLastError();
+}
+cudaError_t rfactor(const float2* psi, const float* amp, long long npx, int batch, double* part, int nblk,
+                    PatState* stt, cudaStream_t st) {
+  k_rdiff<<<dim3(nblk, batch), 256, 0, st>>>(psi, amp, npx, part, nblk);
+  k_finalize_sum<<<batch, 32, 0, st>>>(part, nblk, stt, 2);
+  return cudaGetLastError();
+}
+cudaError_t rfactor_from_partials(const double* part, int nblk, int batch, PatState* stt, cudaStream_t st) {
+  k_finalize_sum<<<batch, 32, 0, st>>>(part, nblk, stt, 2);
+  return cudaGetLastError();
+}
+
+// Start of phaseRetrieve: avg and the flags are locals of the call (cdi.cc:315).
+__global__ void k_run_begin(PatState* stt, int batch) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < batch) { stt[p].avg = 0.f; stt[p].flags = 0; }
+}
+cudaError_t run_begin(PatState* stt, int batch, cudaStream_t st) {
+  k_run_begin<<<(batch + 127) / 128, 128, 0, st>>>(stt, batch);
+  return cudaGetLastError();
+}
+__global__ void k_state_init(PatState* stt, int batch, float thr) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < batch) {
+    PatState z = {};
+    z.threshold = thr;
+    stt[p] = z;
+  }
+}
+cudaError_t state_init(PatState* stt, int batch, float thr, cudaStream_t st) {
+  k_state_init<<<(batch + 127) / 128, 128, 0, st>>>(stt, batch, thr);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ random start
+// createWaveFront(I, 0, Psi, 1) then applyRandomPhase (src/gpu/cudaConfig.cu:710-732,
+// src/gpu/cdi.cu:486-502): Psi = sqrt(max(0,I)) e^{i pi b}, b a fair coin per pixel;
+// pixels with beamstop > threshold are zeroed.  The coin is a counter-based hash
+// of (seed, pattern, pixel) (SplitMix64 finaliser), not curand's MRG32k3a stream.
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+  return z ^ (z >> 31);
+}
+__global__ void k_random_start(const float* __restrict__ inten, const float* __restrict__ bs, float bs_thr,
+                               float2* __restrict__ psi, long long npx, int batch, unsigned long long seed) {
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < npx * batch; g += (long long)gridDim.x * blockDim.x) {
+    const float I = inten[g];
+    const float mod = sqrtf(fmaxf(0.f, I));
+    if (bs && bs[g] > bs_thr) { psi[g] = make_float2(0.f, 0.f); continue; }
+    const uint64_t h = mix64(seed * 0x9e3779b97f4a7c15ULL + (uint64_t)g + 1);
+    const float u = (float)((h >> 40) + 1) * (1.0f / 16777216.0f);   // (0,1]
+    const float ph = (u > 0.5f) ? (float)M_PI : 0.f;
+    float s, c;
+    sincosf(ph, &s, &c);
+    psi[g] = make_float2(mod * c, mod * s);
+  }
+}
+cudaError_t random_start(const float* inten, const float* bs, float bs_thr, float2* psi, long long npx, int batch,
+                         unsigned long long seed, cudaStream_t st) {
+  k_random_start<<<grid1d(npx * batch, 256), 256, 0, st>>>(inten, bs, bs_thr, psi, npx, batch, seed);
+  return cudaGetLastError();
+}
+
+}  // namespace cdx

@@ -1,0 +1,80 @@
+// Kernel argument blocks and codes shared by the CUDA translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace cdx {
+
+// Update codes: the reference's Algorithm enum (include/format.hpp:22).
+enum : int {
+  ALGO_RAAR = 0, ALGO_ER = 1, ALGO_POSER = 2, ALGO_HIO = 3, ALGO_POSHIO = 4, ALGO_FHIO = 5,
+  ALGO_SHRINKWRAP = 6, ALGO_XCORRELATION = 7, ALGO_KKT = 8, ALGO_TV = 9, ALGO_CNT = 10
+};
+
+enum : int { ROW_FFT = 0, ROW_ITER = 1 };
+enum : int { COL_FFT = 0, COL_ITER = 1 };
+enum : int { PROJ_MODABS = 0, PROJ_CCD = 1 };
+
+struct RowArgs {
+  const float2* in;        // rows to load (pattern-major, row-major)
+  float2* out;             // rows to store (may alias in)
+  float2* rho;             // ROW_ITER: real-space iterate, updated in place
+  const uint32_t* mask;    // ROW_ITER: support bits, (cols+31)/32 words per row
+  const float2* tw;        // W_N^t, t < N (forward)
+  int rows;                // lines per pattern
+  int mode;                // ROW_FFT / ROW_ITER
+  int inv;                 // ROW_FFT direction
+  int algo;                // ROW_ITER update
+  long long pat_stride;    // complex elements between patterns
+  long long mask_stride;   // mask words between patterns
+  float scale;             // factor applied on store (1 = none)
+  float inv_n;             // 1/(rows*cols) (applyNorm after the inverse FFT)
+  float beta;              // vars.beta_HIO
+};
+
+struct ColArgs {
+  const float2* in;
+  float2* out;             // may alias in
+  float2* psi_out;         // COL_ITER: optional copy of Psi before the projection
+  const float* amp;        // sqrt(max(I,0)), row-major FFT order
+  const float* inten;      // I (PROJ_CCD)
+  const float* bs;         // beamstop (PROJ_CCD), may be null
+  double* rf_partials;     // optional: per-CTA sum | |Psi| - sqrt(I) |
+  const float2* tw;
+  int cols;                // lines per pattern
+  int mode;                // COL_FFT / COL_ITER
+  int inv;                 // COL_FFT direction
+  int from_psi;            // COL_ITER: input already holds Psi (skip the forward FFT)
+  int proj;                // PROJ_MODABS / PROJ_CCD
+  int noise_level;
+  long long pat_stride;    // elements between patterns (complex and real arrays alike)
+  float scale;
+  float ccd_scale;         // vars.scale
+  float ccd_rcolor;        // vars.rcolor
+};
+
+// Per-pattern device state of the shrinkwrap (the reference keeps it in host
+// locals of phaseRetrieve and in __constant__ vars.threshold).
+struct PatState {
+  float threshold;   // vars.threshold
+  float avg;         // avg of phaseRetrieve (0 until the first shrinkwrap)
+  float maxv;        // last max of the blurred support
+  float sum;         // last sum of the blurred support
+  double rfactor;    // last R-factor
+  double amp_sum;    // sum sqrt(I)
+  double residual;   // final residual
+  int flags;         // bit 0: NaN/zero max seen at a shrinkwrap
+  int pad;
+};
+
+// Launch helpers exported by the per-size translation units.
+typedef cudaError_t (*PrepLaunch)();
+typedef cudaError_t (*RowLaunch)(const RowArgs&, int batch, cudaStream_t);
+typedef cudaError_t (*ColLaunch)(const ColArgs&, int batch, cudaStream_t);
+
+PrepLaunch prep_launcher(int n);   // nullptr: unsupported length
+RowLaunch row_launcher(int n);
+ColLaunch col_launcher(int n);
+int lines_per_cta(int n);          // lines (rows or columns) per CTA for length n
+
+}  // namespace cdx

@@ -1,0 +1,172 @@
+/* cdx.h -- C ABI of the GB300-native CDI phase-retrieval path.
+ *
+ * Replaces the GPU side of liboyang0112/CDIxx's CDI iteration: the cuFFT
+ * wrapper, the modulus projections, the real-space updates and the
+ * shrinkwrap of CDI::phaseRetrieve.  Plain pointers and sizes only; every
+ * call returns a status code (CDX_OK == 0) instead of aborting, and
+ * cdx_last_error() describes the last failure of the calling thread.
+ *
+ * Complex arrays are interleaved float pairs (the reference's
+ * complexFormat = _Complex float, include/format.hpp:25-26), row-major,
+ * rows x cols per pattern, patterns back to back.  Fourier-space arrays are
+ * in FFT (unshifted) order, as the reference keeps patternData/patternWave.
+ * `where` selects host (CDX_HOST) or device (CDX_DEVICE) memory for a buffer.
+ */
+#ifndef CDX_H
+#define CDX_H
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
+enum {
+  CDX_OK = 0,
+  CDX_ERR_ARG = 1,       /* bad argument (null pointer, index out of range) */
+  CDX_ERR_SIZE = 2,      /* unsupported pattern size (rows, cols must be 2^a 3^b in [16, 4096]) */
+  CDX_ERR_CUDA = 3,      /* a CUDA call failed; cdx_last_error() has the CUDA message */
+  CDX_ERR_ALGO = 4,      /* algorithm string rejected (unknown token, TV step) */
+  CDX_ERR_STATE = 5,     /* call order: no pattern / no initial iterate yet */
+  CDX_ERR_IO = 6,        /* .bin file missing, short or of the wrong type */
+  CDX_ERR_NOMEM = 7,     /* device allocation failed */
+  CDX_ERR_CONFIG = 8,    /* config file could not be parsed */
+  CDX_ERR_NOLIB = 9      /* the CUDA device or kernels are unavailable */
+};
+enum { CDX_HOST = 0, CDX_DEVICE = 1 };
+enum { CDX_FFT_ORDER = 0, CDX_CENTERED = 1 };
+
+/* Algorithm codes = the reference's Algorithm enum (include/format.hpp:22). */
+enum { CDX_RAAR = 0, CDX_ER = 1, CDX_POSER = 2, CDX_HIO = 3, CDX_POSHIO = 4, CDX_FHIO = 5,
+       CDX_SHRINKWRAP = 6, CDX_XCORRELATION = 7, CDX_KKT = 8, CDX_TV = 9 };
+
+/* Shrinkwrap kernels. */
+enum {
+  CDX_SHRINK_FOURIER = 0,  /* CDI::phaseRetrieve (cdi.cc:326-341): |IFFT(G_sf Psi)|^2, sf = (rows/4)/g,
+                              g = sigma0 then *= decay while > sigma_min; thr = min(max, 5 avg0) * shrinkThreshold */
+  CDX_SHRINK_SPATIAL = 1   /* holo::iterate (holo.cc:125-148): G_sigma (*) |rho|^2 in pixels,
+                              sigma = sigma0 then *= decay while > sigma_min; thr = max * shrinkThreshold */
+};
+
+typedef struct cdx_params {
+  int rows, cols;            /* pattern size (row, column of the reference) */
+  int batch;                 /* patterns of this size held by the context */
+  float beta;                /* vars.beta_HIO (src/gpu/cdi.cu:22; the reference fixes it at 1) */
+  float shrink_threshold;    /* shrinkThreshold */
+  float oversampling_spt;    /* oversampling_spt: initial rect support (cdi.cc:240-251) */
+  float exposure;            /* exposure: vars.scale = 1/exposure (cdi.cc:52) */
+  int rcolor;                /* vars.rcolor (65535) */
+  int sim_ccd_bit;           /* simCCDbit: applyMod instead of applyModAbs (cdi.cc:349-350) */
+  int noise_level;           /* noiseLevel */
+  int shrink_mode;           /* CDX_SHRINK_* */
+  float sigma0, sigma_min, sigma_decay;  /* shrinkwrap width schedule (defaults 3, 2, 0.99) */
+  int use_graph;             /* capture each cdx_run in a CUDA graph (default 1) */
+  int rf_every;              /* compute the R-factor every k iterations inside the loop (0 = only at the end) */
+} cdx_params;
+
+typedef struct cdx_stats {
+  int steps;                 /* algorithm steps executed (iterations + shrinkwraps) */
+  int iterations;            /* projection iterations */
+  int shrinkwraps;
+  double residual;           /* pattern 0: the reference's residual (cdi.cc:413-421) */
+  double rfactor;            /* pattern 0: sum| |Psi|-sqrt(I) | / sum sqrt(I) of the final Psi */
+  float threshold;           /* pattern 0: vars.threshold after the run */
+  int flags;                 /* pattern 0: bit 0 = a shrinkwrap saw max ~ 0 or NaN (cdi.cc:334-337) */
+  double gpu_ms;             /* device time of the run (CUDA events) */
+  int launches;              /* kernels the run enqueued */
+} cdx_stats;
+
+typedef struct cdx_ctx cdx_ctx;
+
+/* ---------------------------------------------------------------- context */
+/* Fill *p with the reference's defaults (readConfig.hpp:25-35 plus beta = 1). */
+int cdx_params_default(cdx_params* p);
+/* Allocate a context for `p->batch` patterns of p->rows x p->cols on the
+ * current device.  `stream` is a cudaStream_t (NULL: the context creates one).
+ * Replaces CDI::allocateMem / init_fft / init_cuda_image (cdi.cc:42-61,
+ * cudaConfig.cu:137-159, cdi.cu:16-30). */
+int cdx_create(const cdx_params* p, void* stream, cdx_ctx** out);
+int cdx_destroy(cdx_ctx* ctx);
+int cdx_get_params(const cdx_ctx* ctx, cdx_params* out);
+/* Device pointers of the context's arrays (the CDI class exposes them as
+ * patternData, patternWave, objectWave, support).  Any may be NULL. */
+int cdx_device_arrays(cdx_ctx* ctx, float** pattern, void** fourier, void** object, float** support);
+
+/* ---------------------------------------------------------------- inputs */
+/* Pattern intensity of pattern `idx` (rows x cols floats), multiplied by
+ * `scale` on the device (applyNorm(patternData, 1/exposure), cdi.cc:106).
+ * layout CDX_CENTERED applies cudaConvertFO first (cdi.cc:105).  Also resets
+ * the support of that pattern to the rect of oversampling_spt. */
+int cdx_set_pattern(cdx_ctx* ctx, int idx, const float* intensity, int where, int layout, float scale);
+/* Optional beamstop (useBS; cdi.cc:131-148), same layout rules, NULL clears it. */
+int cdx_set_beamstop(cdx_ctx* ctx, int idx, const float* bs, int where, int layout);
+/* Restart iterate Psi0 (prepareIter with restart, cdi.cc:201-227):
+ * rho0 = IFFT(Psi0)/sqrt(N).  Also resets the support to the rect (initSupport). */
+int cdx_set_initial(cdx_ctx* ctx, int idx, const float* psi0, int where);
+/* Random-phase start for every pattern (cdi.cc:222-227): Psi0 = sqrt(I) e^{i pi b}. */
+int cdx_random_start(cdx_ctx* ctx, unsigned long long seed);
+/* Float support of pattern idx (inside = value > current threshold). */
+int cdx_set_support(cdx_ctx* ctx, int idx, const float* support, int where);
+
+/* ---------------------------------------------------------------- the loop */
+/* CDI::phaseRetrieve (cdi.cc:297-449) on every pattern of the context, with
+ * the reference's algorithm grammar (readConfig.cc:82-163), e.g.
+ * "100*(3*POSHIO+20*RAAR+1*POSHIO+1*shrinkWrap)+20*RAAR+1*ER".
+ * Nested parentheses are accepted too.  Ends with rho scaled by sqrt(N), Psi
+ * = FFT(rho) and the residual.  Synchronises the context's stream. */
+int cdx_run(cdx_ctx* ctx, const char* algorithm, cdx_stats* stats);
+/* Same without the final synchronisation or statistics (device timing). */
+int cdx_run_async(cdx_ctx* ctx, const char* algorithm);
+/* Statistics of pattern idx after a run (synchronises). */
+int cdx_get_stats(cdx_ctx* ctx, int idx, cdx_stats* stats);
+
+/* ---------------------------------------------------------------- outputs */
+int cdx_get_object(cdx_ctx* ctx, int idx, float* out, int where);   /* objectWave (complex) */
+int cdx_get_fourier(cdx_ctx* ctx, int idx, float* out, int where);  /* patternWave (complex) */
+int cdx_get_support(cdx_ctx* ctx, int idx, float* out, int where);  /* support (float field) */
+
+/* ---------------------------------------------------------------- one call, host buffers */
+/* Whole path for one pattern with HOST buffers: create, set pattern, set
+ * Psi0 (or a random start when psi0 is NULL), run, copy rho/Psi/support
+ * back, destroy.  Outputs may be NULL. */
+int cdx_phase_retrieve_host(const cdx_params* p, const char* algorithm, const float* intensity,
+                            const float* psi0, unsigned long long seed, float* rho_out, float* psi_out,
+                            float* support_out, cdx_stats* stats);
+
+/* ---------------------------------------------------------------- primitives (device pointers) */
+/* myFFT / myIFFT (cudaConfig.cu:175-180): unnormalised 2-D C2C transform of
+ * `batch` patterns, in place allowed.  inverse != 0 uses exp(+2 pi i). */
+int cdx_fft2(const void* in, void* out, int rows, int cols, int batch, int inverse, void* stream);
+/* applyModAbs(source, target) with state NULL (cudaConfig.cu:827-841). */
+int cdx_apply_mod_abs(void* psi, const float* intensity, long long n, void* stream);
+/* applyMod(source, target, bs, noiseLevel) (cdi.cu:438-485); scale = vars.scale. */
+int cdx_apply_mod(void* psi, const float* intensity, const float* beamstop, int noise_level, float scale,
+                  int rcolor, long long n, void* stream);
+/* applySupport(gkp1, gkprime, algo, spt) (cdi.cc:25-36, cdi.cu:518-616). */
+int cdx_apply_support(void* rho, const void* rho_prime, const float* support, float threshold, float beta,
+                      int algo, long long n, void* stream);
+/* cudaConvertFO for complex or real arrays (cudaConfig.cu:202-216). */
+int cdx_convert_fo(const void* in, void* out, int rows, int cols, int batch, int is_complex, void* stream);
+
+/* ---------------------------------------------------------------- helpers */
+/* AlgoParser (readConfig.cc:82-163): expand `algorithm` into step codes.
+ * Writes up to `cap` codes to `out` (may be NULL) and the total to *count. */
+int cdx_algo_expand(const char* algorithm, int* out, int cap, int* count);
+/* .bin image files (imgio.c:23-43, 223-243).  cdx_read_bin with data NULL
+ * returns the header only; *is_complex set from the file type. */
+int cdx_read_bin(const char* path, int* rows, int* cols, int* is_complex, float* data, size_t cap_floats);
+int cdx_write_bin(const char* path, const float* data, int rows, int cols, int is_complex);
+/* Lengths the kernels support (2^a 3^b, 16..4096). */
+int cdx_size_supported(int n);
+const char* cdx_last_error(void);
+const char* cdx_version(void);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+#ifdef __cplusplus
+}
+#endif
+#endif /* CDX_H */

@@ -1,0 +1,326 @@
+"""GPU parity of the CUDA path against the oracle (calls go through the C ABI).
+
+Tolerances (FP32 path vs the FP64 oracle):
+  * 2-D FFT: relative L2 <= 2e-6 (FP32 rounding grows ~ log N),
+  * one iterate (rho after k iterations, k <= 10): relative L2 <= 1e-5,
+  * shrinkwrap: support masks agree on >= 99.9 % of pixels, threshold rel. 1e-4,
+  * element-wise primitives: relative 2e-6 per element against the float32 oracle.
+"""
+import numpy as np
+import pytest
+
+from cdixx_gb300 import synth
+from oracle import cdi_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.complex128)
+    b = np.asarray(b, np.complex128)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def blob_case(n=256, seed=11, photons=1e6):
+    obj, sup, I = synth.config0_case(seed=seed, n=n, photons=photons)
+    psi0 = synth.random_phase_start(I, seed)
+    return I, psi0
+
+
+SIZES = [16, 24, 32, 48, 64, 96, 128, 192, 256, 384, 512, 768, 1024, 1536, 2048, 3072, 4096]
+
+
+@pytest.mark.parametrize("n", SIZES)
+def test_fft2_square(cdx, torch_cuda, n):
+    torch = torch_cuda
+    rng = np.random.default_rng(n)
+    batch = 2 if n <= 1024 else 1
+    x = (rng.standard_normal((batch, n, n)) + 1j * rng.standard_normal((batch, n, n))).astype(np.complex64)
+    xd = torch.from_numpy(x).cuda()
+    out = torch.empty_like(xd)
+    cdx.fft2(xd, out, inverse=False)
+    torch.cuda.synchronize()
+    ref = np.fft.fft2(x.astype(np.complex128))
+    assert rel_l2(out.cpu().numpy(), ref) < 2e-6
+    cdx.fft2(xd, out, inverse=True)
+    torch.cuda.synchronize()
+    ref = np.fft.ifft2(x.astype(np.complex128)) * n * n
+    assert rel_l2(out.cpu().numpy(), ref) < 2e-6
+
+
+@pytest.mark.parametrize("shape", [(128, 256), (256, 128), (192, 384), (512, 2048), (48, 16)])
+def test_fft2_rect_and_inplace(cdx, torch_cuda, shape):
+    torch = torch_cuda
+    rng = np.random.default_rng(7)
+    x = (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(np.complex64)
+    xd = torch.from_numpy(x).cuda()
+    cdx.fft2(xd, xd)   # in place
+    torch.cuda.synchronize()
+    assert rel_l2(xd.cpu().numpy(), np.fft.fft2(x.astype(np.complex128))) < 2e-6
+
+
+def test_fft2_delta_and_tone(cdx, torch_cuda):
+    torch = torch_cuda
+    n = 256
+    x = np.zeros((n, n), np.complex64)
+    x[0, 0] = 1
+    xd = torch.from_numpy(x).cuda()
+    o = torch.empty_like(xd)
+    cdx.fft2(xd, o)
+    assert np.allclose(o.cpu().numpy(), 1, atol=1e-6)
+    k = np.arange(n)
+    tone = np.exp(2j * np.pi * (3 * k[:, None] + 5 * k[None, :]) / n).astype(np.complex64)
+    cdx.fft2(torch.from_numpy(tone).cuda(), o)
+    r = o.cpu().numpy()
+    assert abs(r[3, 5] - n * n) / (n * n) < 1e-5
+    r[3, 5] = 0
+    assert np.abs(r).max() / (n * n) < 1e-5
+
+
+def test_primitives_vs_oracle(cdx, torch_cuda):
+    torch = torch_cuda
+    rng = np.random.default_rng(2)
+    n = 1 << 14
+    psi = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(np.complex64)
+    I = (rng.random(n) * 4).astype(np.float32)
+    psi[:16] = 0                      # |psi| == 0 branch
+    I[16:32] = -1                     # I <= 0 branch
+    I[32] = np.nan
+    d = torch.from_numpy(psi).cuda()
+    cdx.apply_mod_abs(d, torch.from_numpy(I).cuda())
+    ref = O.apply_mod_abs(psi, I)
+    got = d.cpu().numpy()
+    assert np.allclose(got, ref, rtol=2e-6, atol=1e-12)
+    assert np.all(got[:16].imag == 0) and np.all(got[16:33] == 0)
+    # noise-tolerant projection with a beamstop, overexposure and zero-modulus pixels
+    psi2 = psi.copy()
+    psi2[40:48] = 0
+    I2 = (rng.random(n) * 2).astype(np.float32)
+    I2[100:200] = 5.0                 # >= 0.95 * scale
+    bs = (rng.random(n) > 0.9).astype(np.float32)
+    d2 = torch.from_numpy(psi2).cuda()
+    cdx.apply_mod(d2, torch.from_numpy(I2).cuda(), torch.from_numpy(bs).cuda(), noise_level=24, scale=4.0,
+                  rcolor=65535)
+    ref2 = O.apply_mod(psi2, I2, bs, 24, 4.0, 65535)
+    assert np.allclose(d2.cpu().numpy(), ref2, rtol=2e-6, atol=1e-12)
+    # real-space updates, every algorithm, pixels exactly at the threshold
+    rho = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(np.complex64)
+    rp = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(np.complex64)
+    spt = rng.random(n).astype(np.float32)
+    spt[:64] = 0.25
+    for algo in [O.HIO, O.RAAR, O.ER, O.POSER, O.POSHIO, O.FHIO, O.KKT]:
+        r = torch.from_numpy(rho.copy()).cuda()
+        cdx.apply_support(r, torch.from_numpy(rp).cuda(), torch.from_numpy(spt).cuda(), 0.25, 0.9, algo)
+        ref = O.apply_support(rho, rp, spt, 0.25, algo, beta=0.9)
+        assert np.allclose(r.cpu().numpy(), ref, rtol=2e-6, atol=1e-6), algo
+
+
+def test_convert_fo(cdx, torch_cuda):
+    torch = torch_cuda
+    a = np.arange(64 * 32, dtype=np.float32).reshape(64, 32)
+    d = torch.from_numpy(a.copy()).cuda()
+    cdx.convert_fo(d)
+    assert np.array_equal(d.cpu().numpy(), np.fft.fftshift(a))
+
+
+@pytest.mark.parametrize("algo,beta", [("HIO", 1.0), ("HIO", 0.9), ("RAAR", 0.9), ("ER", 1.0), ("POSHIO", 1.0),
+                                       ("FHIO", 1.0), ("POSER", 1.0)])
+def test_iterates_match_fp64_oracle(cdx, algo, beta):
+    I, psi0 = blob_case()
+    p = cdx.default_params(256, 256, oversampling_spt=4.0, beta=beta)
+    with cdx.Context(p) as ctx:
+        ctx.set_pattern(0, I)
+        for k in (1, 2, 5, 10):
+            ctx.set_initial(0, psi0)
+            ctx.run(f"{k}*{algo}")
+            got = ctx.get_object(0)
+            ref = O.phase_retrieve(psi0, I, f"{k}*{algo}", oversampling_spt=4.0, beta=beta)
+            assert rel_l2(got, ref.rho) <= 1e-5, (algo, k, rel_l2(got, ref.rho))
+            assert rel_l2(ctx.get_fourier(0), ref.psi) <= 1e-5
+
+
+def test_first_step_from_restart_iterate(cdx):
+    # the first projection uses Psi0 itself (cdi.cc:349 after prepareIter)
+    I, psi0 = blob_case(n=128)
+    p = cdx.default_params(128, 128, oversampling_spt=2.0)
+    with cdx.Context(p) as ctx:
+        ctx.set_pattern(0, I)
+        ctx.set_initial(0, psi0)
+        assert rel_l2(ctx.get_fourier(0), psi0) == 0
+        ref = O.prepare_from_restart(psi0)[1] * 128   # rho0 * sqrt(N): undo cdi.cc:313 scaling
+        assert rel_l2(ctx.get_object(0) / np.sqrt(128 * 128) * 128, ref) < 1e-5
+
+
+def test_shrinkwrap_matches_oracle(cdx):
+    I, psi0 = blob_case()
+    alg = "20*HIO+1*shrinkWrap+20*HIO+1*shrinkWrap+5*ER"
+    p = cdx.default_params(256, 256, oversampling_spt=4.0, shrink_threshold=0.1)
+    with cdx.Context(p) as ctx:
+        ctx.set_pattern(0, I)
+        ctx.set_initial(0, psi0)
+        s = ctx.run(alg)
+        spt = ctx.get_support(0)
+        rho = ctx.get_object(0)
+    ref = O.phase_retrieve(psi0, I, alg, oversampling_spt=4.0, shrink_threshold=0.1)
+    assert abs(s["threshold"] - ref.threshold) <= 1e-4 * abs(ref.threshold)
+    assert rel_l2(spt, ref.support) < 1e-4
+    agree = np.mean((spt > s["threshold"]) == (ref.support > ref.threshold))
+    assert agree >= 0.999
+    assert rel_l2(rho, ref.rho) < 1e-3
+    assert s["shrinkwraps"] == 2 and s["iterations"] == 45
+
+
+def test_shrinkwrap_first_step_and_spatial_mode(cdx):
+    I, psi0 = blob_case(n=128)
+    p = cdx.default_params(128, 128, oversampling_spt=2.0, shrink_threshold=0.05)
+    with cdx.Context(p) as ctx:
+        ctx.set_pattern(0, I)
+        ctx.set_initial(0, psi0)
+        s = ctx.run("1*shrinkWrap+3*HIO")
+        ref = O.phase_retrieve(psi0, I, "1*shrinkWrap+3*HIO", oversampling_spt=2.0, shrink_threshold=0.05)
+        assert abs(s["threshold"] - ref.threshold) <= 1e-4 * abs(ref.threshold)
+        assert rel_l2(ctx.get_object(0), ref.rho) < 1e-4
+    # |rho|^2 blur (holo::iterate style): threshold = max * shrinkThreshold
+    p = cdx.default_params(128, 128, oversampling_spt=2.0, shrink_threshold=0.1, shrink_mode=cdx.SHRINK_SPATIAL,
+                           sigma0=3.0, sigma_min=1.5)
+    with cdx.Context(p) as ctx:
+        ctx.set_pattern(0, I)
+        ctx.set_initial(0, psi0)
+        s = ctx.run("5*HIO+1*shrinkWrap")
+        rho = ctx.get_object(0) / 128.0   # undo the final sqrt(N) scaling
+        spt = ctx.get_support(0)
+    m2 = np.abs(rho.astype(np.complex128)) ** 2
+    r = int(np.floor(3.0 * 6)) >> 1
+    d = np.arange(-r, r + 1)
+    w = np.exp(-d * d / 18.0)
+    w /= w.sum()
+    k = np.zeros(128)
+    k[d % 128] = w
+    ref = np.real(np.fft.ifft2(np.fft.fft2(m2) * np.outer(np.fft.fft(k), np.fft.fft(k))))
+    assert rel_l2(spt, ref) < 1e-4
+    assert abs(s["threshold"] - 0.1 * ref.max()) < 1e-4 * ref.max()
+
+
+def test_ccd_projection_iterates(cdx):
+    I, psi0 = blob_case(n=128, photons=1e5)
+    p = cdx.default_params(128, 128, oversampling_spt=2.0, sim_ccd_bit=1, noise_level=3, exposure=0.5)
+    with cdx.Context(p) as ctx:
+        ctx.set_pattern(0, I)
+        ctx.set_initial(0, psi0)
+        ctx.run("5*HIO")
+        got = ctx.get_object(0)
+    ref = O.phase_retrieve(psi0, I, "5*HIO", oversampling_spt=2.0, sim_ccd_bit=True, noise_level=3, exposure=0.5)
+    assert rel_l2(got, ref.rho) <= 1e-5
+
+
+def test_residual_and_rfactor(cdx):
+    I, psi0 = blob_case(n=128)
+    p = cdx.default_params(128, 128, oversampling_spt=2.0)
+    with cdx.Context(p) as ctx:
+        ctx.set_pattern(0, I)
+        ctx.set_initial(0, psi0)
+        s = ctx.run("10*HIO")
+        psi = ctx.get_fourier(0)
+    ref = O.phase_retrieve(psi0, I, "10*HIO", oversampling_spt=2.0)
+    assert abs(s["residual"] - ref.residual) <= 1e-4 * ref.residual
+    assert abs(s["rfactor"] - O.r_factor(psi, I)) <= 1e-6
+    assert abs(s["rfactor"] - O.r_factor(ref.psi, I)) <= 1e-4
+
+
+def test_batch_equals_single_and_graph_equals_stream(cdx):
+    cases = [blob_case(n=192, seed=s) for s in (1, 2, 3)]
+    alg = "8*HIO+1*shrinkWrap+4*RAAR"
+    outs = []
+    for use_graph in (1, 0):
+        p = cdx.default_params(192, 192, batch=3, oversampling_spt=3.0, shrink_threshold=0.1, beta=0.9,
+                               use_graph=use_graph)
+        with cdx.Context(p) as ctx:
+            for i, (I, psi0) in enumerate(cases):
+                ctx.set_pattern(i, I)
+                ctx.set_initial(i, psi0)
+            ctx.run(alg)
+            outs.append([ctx.get_object(i) for i in range(3)])
+    for a, b in zip(*outs):
+        assert np.array_equal(a, b)
+    for i, (I, psi0) in enumerate(cases):
+        p = cdx.default_params(192, 192, oversampling_spt=3.0, shrink_threshold=0.1, beta=0.9)
+        with cdx.Context(p) as ctx:
+            ctx.set_pattern(0, I)
+            ctx.set_initial(0, psi0)
+            ctx.run(alg)
+            assert np.array_equal(ctx.get_object(0), outs[0][i])
+
+
+def test_host_buffer_entry_matches_context(cdx):
+    I, psi0 = blob_case(n=128)
+    p = cdx.default_params(128, 128, oversampling_spt=2.0, shrink_threshold=0.1)
+    rho, psi, spt, st = cdx.phase_retrieve_host(p, "10*HIO+1*shrinkWrap+5*ER", I, psi0)
+    with cdx.Context(p) as ctx:
+        ctx.set_pattern(0, I)
+        ctx.set_initial(0, psi0)
+        ctx.run("10*HIO+1*shrinkWrap+5*ER")
+        assert np.array_equal(ctx.get_object(0), rho)
+        assert np.array_equal(ctx.get_fourier(0), psi)
+        assert np.array_equal(ctx.get_support(0), spt)
+
+
+def test_random_start_is_binary_phase(cdx):
+    I, _ = blob_case(n=128)
+    p = cdx.default_params(128, 128, oversampling_spt=2.0)
+    with cdx.Context(p) as ctx:
+        ctx.set_pattern(0, I)
+        ctx.random_start(1234)
+        psi0 = ctx.get_fourier(0)
+    a = np.sqrt(np.maximum(I, 0))
+    assert np.allclose(np.abs(psi0), a, rtol=1e-6)
+    assert np.all(np.abs(psi0.imag) <= 1e-6 * np.maximum(a, 1e-30))
+    frac = np.mean(psi0.real < 0)
+    assert 0.45 < frac < 0.55
+
+
+def test_errors_do_not_abort(cdx):
+    I, psi0 = blob_case(n=128)
+    p = cdx.default_params(128, 128)
+    with cdx.Context(p) as ctx:
+        with pytest.raises(cdx.CdxError) as e:
+            ctx.run("5*HIO")
+        assert e.value.code == cdx.CDX_ERR_STATE
+        ctx.set_pattern(0, I)
+        ctx.set_initial(0, psi0)
+        for bad in ["5*TV", "5*NOPE", "1*(2*HIO"]:
+            with pytest.raises(cdx.CdxError) as e:
+                ctx.run(bad)
+            assert e.value.code == cdx.CDX_ERR_ALGO
+        ctx.run("2*HIO")   # the context is still usable
+
+
+def test_large_pattern_properties(cdx, torch_cuda):
+    """2048^2: round trip FFT/IFFT/N and Parseval (size-independent properties)."""
+    torch = torch_cuda
+    n = 2048
+    g = torch.Generator(device="cuda").manual_seed(0)
+    x = torch.randn(n, n, dtype=torch.complex64, device="cuda", generator=g)
+    y = torch.empty_like(x)
+    z = torch.empty_like(x)
+    cdx.fft2(x, y)
+    cdx.fft2(y, z, inverse=True)
+    torch.cuda.synchronize()
+    err = (torch.linalg.vector_norm(z / (n * n) - x) / torch.linalg.vector_norm(x)).item()
+    assert err < 2e-6
+    ex = torch.sum(torch.abs(x.to(torch.complex128)) ** 2).item()
+    ey = torch.sum(torch.abs(y.to(torch.complex128)) ** 2).item() / (n * n)
+    assert abs(ex - ey) / ex < 1e-5
+
+
+def test_large_pattern_iterates(cdx):
+    """2048^2 phase object, RAAR beta 0.9: 3 iterates against the FP64 oracle."""
+    obj, sup, I = synth.config1_case(seed=5)
+    psi0 = synth.random_phase_start(I, 5)
+    p = cdx.default_params(2048, 2048, oversampling_spt=4.0, beta=0.9)
+    with cdx.Context(p) as ctx:
+        ctx.set_pattern(0, I)
+        ctx.set_initial(0, psi0)
+        ctx.run("3*RAAR")
+        got = ctx.get_object(0)
+    ref = O.phase_retrieve(psi0, I, "3*RAAR", oversampling_spt=4.0, beta=0.9)
+    assert rel_l2(got, ref.rho) <= 1e-5
