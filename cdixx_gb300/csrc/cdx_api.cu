@@ -36,8 +36,8 @@ namespace {
 constexpr int kRedBlocks = 152;   // reduction CTAs per pattern (one per SM)
 
 // ---------------------------------------------------------------- twiddles
-// W_n^t = exp(-2 pi i t/n) in double, rounded once to float; one table per
-// (device, n), kept for the life of the process.
+// Per-pass twiddle table of length n (cdx_dispatch.cu), one per (device, n),
+// kept for the life of the process.
 std::mutex g_tw_mu;
 std::map<std::pair<int, int>, float2*> g_tw;
 
@@ -47,15 +47,12 @@ int twiddles(int n, float2** out) {
   std::lock_guard<std::mutex> lk(g_tw_mu);
   auto it = g_tw.find({dev, n});
   if (it != g_tw.end()) { *out = it->second; return CDX_OK; }
-  std::vector<float2> h(n);
-  const double two_pi = 6.283185307179586476925286766559;
-  for (int t = 0; t < n; ++t) {
-    const double a = two_pi * (double)t / (double)n;
-    h[t] = make_float2((float)std::cos(a), (float)-std::sin(a));
-  }
+  const int cnt = std::max(1, twiddle_count(n));
+  std::vector<float2> h(cnt, make_float2(1.f, 0.f));
+  twiddle_table(n, h.data());
   float2* d = nullptr;
-  CDX_CK(cudaMalloc(&d, sizeof(float2) * n));
-  CDX_CK(cudaMemcpy(d, h.data(), sizeof(float2) * n, cudaMemcpyHostToDevice));
+  CDX_CK(cudaMalloc(&d, sizeof(float2) * cnt));
+  CDX_CK(cudaMemcpy(d, h.data(), sizeof(float2) * cnt, cudaMemcpyHostToDevice));
   g_tw[{dev, n}] = d;
   *out = d;
   return CDX_OK;
@@ -79,8 +76,13 @@ struct cdx_ctx {
   bool own_stream = false;
   int device = 0;
 
-  float2 *rho = nullptr, *work = nullptr, *psi = nullptr;
-  float *inten = nullptr, *amp = nullptr, *spt = nullptr, *bs = nullptr;
+  // rho, psi, tmp, inten, spt, bs: row-major (npx per pattern);
+  // work, amp_t, inten_t, bs_t: column-tiled, tile width 2^tl (wstride per pattern)
+  float2 *rho = nullptr, *work = nullptr, *psi = nullptr, *tmp = nullptr;
+  float *inten = nullptr, *amp_t = nullptr, *inten_t = nullptr, *spt = nullptr, *bs = nullptr, *bs_t = nullptr;
+  int tl = 0;              // log2 of the column-pass lines per CTA
+  int cp = 0;              // cols padded to a multiple of 2^tl
+  long long wstride = 0;   // rows * cp
   uint32_t* mask = nullptr;
   float2 *tw_r = nullptr, *tw_c = nullptr;   // lengths rows (column pass) and cols (row pass)
   double* part = nullptr;                    // [batch][part_per_pat]
@@ -96,8 +98,7 @@ struct cdx_ctx {
   std::vector<char> have_pattern;
   std::vector<char> fresh;    // initial iterate set since the last run
   bool have_initial = false;
-  bool psi_in_work = false;   // W holds Psi0: the next iteration starts from it
-  bool psi_valid = false;     // psi holds the Psi of the current state
+  bool psi_in_work = false;   // psi holds Psi0 and W nothing yet: the next iteration starts from psi
   int sx = 0, sy = 0, ex = 0, ey = 0;
 
   // graph cache
@@ -203,12 +204,18 @@ void plan_shrinkwrap(const cdx_ctx* c, int count, SwPlan& P) {
 
 int col_iter(cdx_ctx* c, bool from_psi, bool rf) {
   ColArgs a{};
-  a.in = c->work;
+  // the first iteration after a restart reads Psi0 (row-major) from psi
+  a.in = from_psi ? c->psi : c->work;
+  a.in_tiled = from_psi ? 0 : 1;
+  a.in_stride = from_psi ? c->npx : c->wstride;
   a.out = c->work;
+  a.out_tiled = 1;
+  a.out_stride = c->wstride;
   a.psi_out = nullptr;
-  a.amp = c->amp;
-  a.inten = c->inten;
-  a.bs = c->bs;
+  a.amp = c->amp_t;
+  a.inten = c->inten_t;
+  a.bs = c->bs_t;
+  a.aux_stride = c->wstride;
   a.rf_partials = rf ? c->part : nullptr;
   a.tw = c->tw_r;
   a.cols = c->cols;
@@ -216,7 +223,6 @@ int col_iter(cdx_ctx* c, bool from_psi, bool rf) {
   a.from_psi = from_psi;
   a.proj = c->p.sim_ccd_bit ? PROJ_CCD : PROJ_MODABS;
   a.noise_level = c->p.noise_level;
-  a.pat_stride = c->npx;
   a.scale = 1.f;
   a.ccd_scale = 1.f / c->p.exposure;
   a.ccd_rcolor = (float)c->p.rcolor;
@@ -228,14 +234,17 @@ int row_iter(cdx_ctx* c, int algo) {
   RowArgs a{};
   a.in = c->work;
   a.out = c->work;
+  a.in_tiled = a.out_tiled = 1;
+  a.tile_log2 = c->tl;
+  a.in_stride = a.out_stride = c->wstride;
   a.rho = c->rho;
+  a.rho_stride = c->npx;
   a.mask = c->mask;
+  a.mask_stride = (long long)c->rows * c->wpr;
   a.tw = c->tw_c;
   a.rows = c->rows;
   a.mode = ROW_ITER;
   a.algo = algo;
-  a.pat_stride = c->npx;
-  a.mask_stride = (long long)c->rows * c->wpr;
   a.scale = 1.f;
   a.inv_n = (float)(1.0 / ((double)c->rows * c->cols));   // applyNorm(.., 1./(row*column)), cdi.cc:353
   a.beta = c->p.beta;
@@ -243,27 +252,28 @@ int row_iter(cdx_ctx* c, int algo) {
   return CDX_OK;
 }
 
-// Generic 2-D transform of `batch` patterns: rows then columns.
+// Generic 2-D transform of `batch` row-major patterns: rows then columns.
 int fft2_enqueue(const float2* in, float2* out, int rows, int cols, int batch, bool inv, float scale,
                  const float2* tw_rows_len, const float2* tw_cols_len, cudaStream_t st) {
+  const long long n = (long long)rows * cols;
   RowArgs r{};
   r.in = in;
   r.out = out;
+  r.in_stride = r.out_stride = n;
   r.tw = tw_cols_len;
   r.rows = rows;
   r.mode = ROW_FFT;
   r.inv = inv;
-  r.pat_stride = (long long)rows * cols;
   r.scale = 1.f;
   CDX_CK(row_launcher(cols)(r, batch, st));
   ColArgs c{};
   c.in = out;
   c.out = out;
+  c.in_stride = c.out_stride = n;
   c.tw = tw_rows_len;
   c.cols = cols;
   c.mode = COL_FFT;
   c.inv = inv;
-  c.pat_stride = (long long)rows * cols;
   c.scale = scale;
   CDX_CK(col_launcher(rows)(c, batch, st));
   return CDX_OK;
@@ -284,7 +294,7 @@ int enqueue_run(cdx_ctx* c, const std::vector<int>& steps, const SwPlan& sw, boo
   for (int a : steps) {
     if (a == ALGO_SHRINKWRAP) {
       const bool m2 = c->p.shrink_mode == CDX_SHRINK_SPATIAL;
-      CDX_CK(shrinkwrap(c->rho, c->psi, c->spt, c->weights + sw.offx[swi], sw.radx[swi], c->weights + sw.offy[swi],
+      CDX_CK(shrinkwrap(c->rho, c->tmp, c->spt, c->weights + sw.offx[swi], sw.radx[swi], c->weights + sw.offy[swi],
                         sw.rady[swi], c->rows, c->cols, c->batch, m2, (float)((double)c->rows * c->cols), c->pmax,
                         c->part, kRedBlocks, c->dstate, c->p.shrink_threshold, c->st));
       CDX_CK(support_bits(c->spt, c->dstate, 0.f, c->mask, c->rows, c->cols, c->batch, c->st));
@@ -302,18 +312,19 @@ int enqueue_run(cdx_ctx* c, const std::vector<int>& steps, const SwPlan& sw, boo
     from_psi = false;
     ++it;
   }
-  // final Psi = FFT(rho): W holds rowFFT(rho) unless no iteration ran
-  if (it == 0 && psi_in_work) {
-    CDX_CK(cudaMemcpyAsync(c->psi, c->work, sizeof(float2) * n_all, cudaMemcpyDeviceToDevice, c->st));
-  } else {
+  // final Psi = FFT(rho): W holds rowFFT(rho); with no iteration psi still holds Psi0
+  if (!(it == 0 && psi_in_work)) {
     ColArgs a{};
     a.in = c->work;
+    a.in_tiled = 1;
+    a.in_stride = c->wstride;
     a.out = c->psi;
+    a.out_tiled = 0;
+    a.out_stride = c->npx;
     a.tw = c->tw_r;
     a.cols = c->cols;
     a.mode = COL_FFT;
     a.inv = 0;
-    a.pat_stride = c->npx;
     a.scale = 1.f;
     CDX_CK(col_launcher(c->rows)(a, c->batch, c->st));
     ++nl;
@@ -321,7 +332,7 @@ int enqueue_run(cdx_ctx* c, const std::vector<int>& steps, const SwPlan& sw, boo
   // applyNorm(cuda_gkp1, sqrt(row*column)) (cdi.cc:406)
   CDX_CK(scale_complex(c->rho, sqn, n_all, c->st));
   CDX_CK(residual(c->psi, c->inten, c->npx, c->batch, c->part, kRedBlocks, c->dstate, c->st));
-  CDX_CK(rfactor(c->psi, c->amp, c->npx, c->batch, c->part, kRedBlocks, c->dstate, c->st));
+  CDX_CK(rfactor(c->psi, c->inten, c->npx, c->batch, c->part, kRedBlocks, c->dstate, c->st));
   nl += 5;
   c->last_launches = nl;
   return CDX_OK;
@@ -397,7 +408,6 @@ int run_impl(cdx_ctx* c, const char* algorithm) {
   }
   if (c->last_iters > 0) c->psi_in_work = false;
   c->fresh.assign(c->batch, 0);
-  c->psi_valid = true;
   return CDX_OK;
 }
 
@@ -485,17 +495,25 @@ int cdx_create(const cdx_params* p, void* stream, cdx_ctx** out) {
   if (prep_launcher(c->rows)() != cudaSuccess || prep_launcher(c->cols)() != cudaSuccess)
     return fail(set_error(CDX_ERR_CUDA, std::string("kernel attributes: ") + cudaGetErrorString(cudaGetLastError())));
   if ((e = twiddles(c->rows, &c->tw_r)) || (e = twiddles(c->cols, &c->tw_c))) return fail(e);
-  c->col_blocks = (c->cols + lines_per_cta(c->rows) - 1) / lines_per_cta(c->rows);
+  const int lc = lines_per_cta(c->rows);
+  c->tl = 0;
+  while ((1 << c->tl) < lc) ++c->tl;
+  c->cp = (c->cols + lc - 1) / lc * lc;
+  c->wstride = (long long)c->rows * c->cp;
+  c->col_blocks = c->cp / lc;
   c->part_per_pat = std::max(kRedBlocks, c->col_blocks);
-  // one arena: 3 complex + 3 real arrays, bits, partials, state
-  const size_t B = (size_t)c->batch, N = (size_t)c->npx;
+  // one arena: row-major rho, psi, tmp, I, support; tiled W, sqrt(I), I;
+  // bits, partials, state
+  const size_t B = (size_t)c->batch, N = (size_t)c->npx, W = (size_t)c->wstride;
   auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
   size_t off = 0;
   const size_t o_rho = off; off += al(sizeof(float2) * B * N);
-  const size_t o_work = off; off += al(sizeof(float2) * B * N);
+  const size_t o_work = off; off += al(sizeof(float2) * B * W);
   const size_t o_psi = off; off += al(sizeof(float2) * B * N);
+  const size_t o_tmp = off; off += al(sizeof(float2) * B * N);
   const size_t o_int = off; off += al(sizeof(float) * B * N);
-  const size_t o_amp = off; off += al(sizeof(float) * B * N);
+  const size_t o_amp = off; off += al(sizeof(float) * B * W);
+  const size_t o_intt = off; off += al(sizeof(float) * B * W);
   const size_t o_spt = off; off += al(sizeof(float) * B * N);
   const size_t o_mask = off; off += al(sizeof(uint32_t) * B * c->rows * c->wpr);
   const size_t o_part = off; off += al(sizeof(double) * B * c->part_per_pat);
@@ -509,8 +527,10 @@ int cdx_create(const cdx_params* p, void* stream, cdx_ctx** out) {
   c->rho = (float2*)(a + o_rho);
   c->work = (float2*)(a + o_work);
   c->psi = (float2*)(a + o_psi);
+  c->tmp = (float2*)(a + o_tmp);
   c->inten = (float*)(a + o_int);
-  c->amp = (float*)(a + o_amp);
+  c->amp_t = (float*)(a + o_amp);
+  c->inten_t = (float*)(a + o_intt);
   c->spt = (float*)(a + o_spt);
   c->mask = (uint32_t*)(a + o_mask);
   c->part = (double*)(a + o_part);
@@ -537,6 +557,7 @@ int cdx_destroy(cdx_ctx* c) {
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
   if (c->weights) cudaFree(c->weights);
   if (c->bs) cudaFree(c->bs);
+  if (c->bs_t) cudaFree(c->bs_t);
   if (c->arena) cudaFree(c->arena);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
@@ -562,13 +583,14 @@ int cdx_device_arrays(cdx_ctx* c, float** pattern, void** fourier, void** object
 
 int cdx_set_pattern(cdx_ctx* c, int idx, const float* inten, int where, int layout, float scale) {
   if (!c || !inten || idx < 0 || idx >= c->batch) return set_error(CDX_ERR_ARG, "bad pattern argument");
-  const long long off = (long long)idx * c->npx;
+  const long long off = (long long)idx * c->npx, toff = (long long)idx * c->wstride;
   int e = copy_in(c->inten + off, inten, sizeof(float) * c->npx, where, c->st);
   if (e) return e;
   if (layout == CDX_CENTERED) CDX_CK(convert_fo_real(c->inten + off, c->inten + off, c->rows, c->cols, 1, c->st));
   if (scale != 1.f) CDX_CK(scale_real(c->inten + off, scale, c->npx, c->st));
-  CDX_CK(amp_from_pattern(c->inten + off, c->amp + off, c->npx, c->st));
-  CDX_CK(pattern_amp_sum(c->amp + off, c->npx, 1, c->part, kRedBlocks, c->dstate + idx, c->st));
+  CDX_CK(to_tiled(c->inten + off, c->inten_t + toff, c->rows, c->cols, c->tl, c->wstride, 1, c->st));
+  CDX_CK(amp_from_pattern(c->inten_t + toff, c->amp_t + toff, c->wstride, c->st));
+  CDX_CK(pattern_amp_sum(c->amp_t + toff, c->wstride, 1, c->part, kRedBlocks, c->dstate + idx, c->st));
   CDX_CK(cudaStreamSynchronize(c->st));
   c->have_pattern[idx] = 1;
   return CDX_OK;
@@ -580,40 +602,41 @@ int cdx_set_beamstop(cdx_ctx* c, int idx, const float* bs, int where, int layout
   if (!c->bs) {
     CDX_CK(cudaMalloc(&c->bs, sizeof(float) * c->npx * c->batch));
     CDX_CK(cudaMemsetAsync(c->bs, 0, sizeof(float) * c->npx * c->batch, c->st));
+    CDX_CK(cudaMalloc(&c->bs_t, sizeof(float) * c->wstride * c->batch));
+    CDX_CK(cudaMemsetAsync(c->bs_t, 0, sizeof(float) * c->wstride * c->batch, c->st));
   }
-  const long long off = (long long)idx * c->npx;
+  const long long off = (long long)idx * c->npx, toff = (long long)idx * c->wstride;
   int e = copy_in(c->bs + off, bs, sizeof(float) * c->npx, where, c->st);
   if (e) return e;
   if (layout == CDX_CENTERED) CDX_CK(convert_fo_real(c->bs + off, c->bs + off, c->rows, c->cols, 1, c->st));
+  CDX_CK(to_tiled(c->bs + off, c->bs_t + toff, c->rows, c->cols, c->tl, c->wstride, 1, c->st));
   c->gkey.clear();
   CDX_CK(cudaStreamSynchronize(c->st));
   return CDX_OK;
 }
 
-static int init_rho_from_work(cdx_ctx* c, int idx, int count) {
-  // rho0 = IFFT(Psi0) * (1/sqrt(N)) (cdi.cc:225-226)
+// rho0 = IFFT(Psi0) * (1/sqrt(N)) (cdi.cc:225-226); Psi0 stays in psi, where
+// the first projection reads it.
+static int init_rho_from_psi(cdx_ctx* c, int idx, int count) {
   const long long off = (long long)idx * c->npx;
   const float f = (float)(1.0 / std::sqrt((double)c->rows * c->cols));
-  int e = fft2_enqueue(c->work + off, c->rho + off, c->rows, c->cols, count, true, f, c->tw_r, c->tw_c, c->st);
-  if (e) return e;
-  return CDX_OK;
+  return fft2_enqueue(c->psi + off, c->rho + off, c->rows, c->cols, count, true, f, c->tw_r, c->tw_c, c->st);
 }
 
 int cdx_set_initial(cdx_ctx* c, int idx, const float* psi0, int where) {
   if (!c || !psi0 || idx < 0 || idx >= c->batch) return set_error(CDX_ERR_ARG, "bad initial-iterate argument");
   const long long off = (long long)idx * c->npx;
-  int e = copy_in(c->work + off, psi0, sizeof(float2) * c->npx, where, c->st);
+  int e = copy_in(c->psi + off, psi0, sizeof(float2) * c->npx, where, c->st);
   if (e) return e;
-  if ((e = init_rho_from_work(c, idx, 1))) return e;
+  if ((e = init_rho_from_psi(c, idx, 1))) return e;
   if ((e = reset_support(c, idx, 1))) return e;   // initSupport (cdi.cc:227, 252-254)
   CDX_CK(cudaStreamSynchronize(c->st));
-  // a batch restarts together: W holds Psi0 for every pattern once all are set
+  // a batch restarts together: the first iteration reads Psi0 of every pattern
   c->fresh[idx] = 1;
   int nfresh = 0;
   for (char f : c->fresh) nfresh += f;
   c->have_initial = true;
   c->psi_in_work = nfresh == c->batch;
-  c->psi_valid = false;
   return CDX_OK;
 }
 
@@ -623,15 +646,14 @@ int cdx_random_start(cdx_ctx* c, unsigned long long seed) {
     if (!c->have_pattern[i]) return set_error(CDX_ERR_STATE, "pattern " + std::to_string(i) + " not set");
   PatState h0;
   CDX_CK(cudaMemcpy(&h0, c->dstate, sizeof h0, cudaMemcpyDeviceToHost));
-  CDX_CK(random_start(c->inten, c->bs, h0.threshold, c->work, c->npx, c->batch, seed, c->st));
-  int e = init_rho_from_work(c, 0, c->batch);
+  CDX_CK(random_start(c->inten, c->bs, h0.threshold, c->psi, c->npx, c->batch, seed, c->st));
+  int e = init_rho_from_psi(c, 0, c->batch);
   if (e) return e;
   if ((e = reset_support(c, 0, c->batch))) return e;
   CDX_CK(cudaStreamSynchronize(c->st));
   c->fresh.assign(c->batch, 1);
   c->have_initial = true;
   c->psi_in_work = true;
-  c->psi_valid = false;
   return CDX_OK;
 }
 
@@ -666,8 +688,7 @@ int cdx_get_object(cdx_ctx* c, int idx, float* out, int where) {
 }
 int cdx_get_fourier(cdx_ctx* c, int idx, float* out, int where) {
   if (!c || !out || idx < 0 || idx >= c->batch) return set_error(CDX_ERR_ARG, "bad output argument");
-  const float2* src = c->psi_valid ? c->psi : c->work;   // before any run W holds Psi0
-  return copy_out(out, src + (long long)idx * c->npx, sizeof(float2) * c->npx, where, c->st);
+  return copy_out(out, c->psi + (long long)idx * c->npx, sizeof(float2) * c->npx, where, c->st);
 }
 int cdx_get_support(cdx_ctx* c, int idx, float* out, int where) {
   if (!c || !out || idx < 0 || idx >= c->batch) return set_error(CDX_ERR_ARG, "bad output argument");

@@ -1,4 +1,6 @@
-// Length -> kernel dispatch for the row/column passes.
+// Length -> kernel dispatch for the row/column passes, and the twiddle tables.
+#include <cmath>
+
 #include "cdx_fft.cuh"
 #include "cdx_types.h"
 
@@ -16,6 +18,7 @@ template <int N> cudaError_t launch_col(const ColArgs&, int, cudaStream_t);
 #define CASE_ROW(N) case N: return &launch_row<N>;
 #define CASE_COL(N) case N: return &launch_col<N>;
 #define CASE_L(N) case N: return Geom<N>::L;
+#define CASE_TW(N) case N: return Geom<N>::TWN;
 
 PrepLaunch prep_launcher(int n) {
   switch (n) { CDX_FOR_EACH_SIZE(CASE_PREP) default: return nullptr; }
@@ -28,6 +31,25 @@ ColLaunch col_launcher(int n) {
 }
 int lines_per_cta(int n) {
   switch (n) { CDX_FOR_EACH_SIZE(CASE_L) default: return 0; }
+}
+int twiddle_count(int n) {
+  switch (n) { CDX_FOR_EACH_SIZE(CASE_TW) default: return 0; }
+}
+
+// Entry (r-1)*NS + k of pass p's block = W_n^(r*k*n/(NS*R)), W_n = exp(-2 pi i/n),
+// evaluated in double with the exponent reduced mod n and rounded once to float.
+void twiddle_table(int n, float2* out) {
+  const double two_pi = 6.283185307179586476925286766559;
+  for (int p = 1; plan_radix(n, p) != 0; ++p) {
+    const int R = plan_radix(n, p), NS = plan_ns(n, p), step = n / (NS * R);
+    float2* blk = out + tw_offset(n, p);
+    for (int r = 1; r < R; ++r)
+      for (int k = 0; k < NS; ++k) {
+        const long long t = ((long long)r * k * step) % n;
+        const double a = two_pi * (double)t / (double)n;
+        blk[(r - 1) * NS + k] = make_float2((float)std::cos(a), (float)-std::sin(a));
+      }
+  }
 }
 
 }  // namespace cdx

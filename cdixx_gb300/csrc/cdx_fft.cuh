@@ -136,6 +136,7 @@ CDX_HD void dftR(float2* v) {
   else static_assert(R == 2, "unsupported radix");
 }
 
+
 // ---------------------------------------------------------------- plans
 // radix of pass p for length N: as many 16s as divide N, then 8, 4, 2, then 3s.
 __host__ __device__ constexpr int plan_radix(int n, int p) {
@@ -160,22 +161,65 @@ __host__ __device__ constexpr bool size_supported(int n) {
   while (m % 3 == 0) m /= 3;
   return m == 1;
 }
+// Twiddles of pass p live in a block of (R-1)*NS entries, entry (r-1)*NS + k
+// = W_N^(r*k*N/(NS*R)) for r = 1..R-1, k < NS, so the threads of a warp (k
+// consecutive, r fixed) read consecutive words.  Pass 0 (NS = 1) needs none.
+__host__ __device__ constexpr int tw_offset(int n, int p) {
+  int off = 0;
+  for (int q = 1; q < p; ++q) off += (plan_radix(n, q) - 1) * plan_ns(n, q);
+  return off;
+}
+__host__ __device__ constexpr int tw_count(int n) {
+  int q = 0;
+  while (plan_radix(n, q) != 0) ++q;
+  return tw_offset(n, q);
+}
 
+__host__ __device__ constexpr int pow2_floor(int x) {
+  int p = 1;
+  while (p * 2 <= x) p *= 2;
+  return p;
+}
+
+// Launch geometry per length: T threads, L lines per CTA (a power of two >= 2,
+// so a tile of L columns has a power-of-two width and a row CTA moves at least
+// 32-byte pieces of it), about 16 complex values per thread and pass (32 at
+// N = 4096).  Small CTAs keep three or more resident per SM.
 template <int N>
-struct Layout {
-  static constexpr int LD = N + (N >> 4) + 1;
+struct Geom {
+  static constexpr int T = N >= 3072 ? 512 : 256;
+  static constexpr int MINB = T == 512 ? 1 : 3;   // resident CTAs per SM the register budget targets
+  static constexpr int ELEMS = 16 * T;
+  static constexpr int L = pow2_floor((ELEMS / N) < 2 ? 2 : (ELEMS / N));
+  static constexpr int LOG2L = L == 1 ? 0 : (L == 2 ? 1 : (L == 4 ? 2 : (L == 8 ? 3 : (L == 16 ? 4 : (L == 32 ? 5 :
+                               (L == 64 ? 6 : (L == 128 ? 7 : 8)))))));
+  // line stride in float2: >= N + N/16, and for L < 16 congruent to 16/L mod 16
+  // so a tile row (L consecutive lines at one index) hits distinct bank pairs;
+  // odd otherwise.
+  static constexpr int BASE = N + (N >> 4);
+  static constexpr int WANT = (L < 16) ? (16 / L) : 1;
+  static constexpr int LD = BASE + (((WANT - BASE) % 16) + 16) % 16 + ((L < 16) ? 0 : (((BASE + ((((WANT - BASE) % 16) + 16) % 16)) % 2 == 0) ? 1 : 0));
+  static constexpr int TWN = tw_count(N);
+  // shared memory: the L lines; ROW_ITER adds L rows of rho (8 B/px), COL_ITER
+  // sqrt(I) (4 B/px) and, for the noise-tolerant projection, I and the beamstop
+  static constexpr int SMEM_LINES = L * LD * (int)sizeof(float2);
+  static constexpr int SMEM_ROW_ITER = SMEM_LINES + L * N * (int)sizeof(float2) + L * ((N + 31) >> 5) * 4;
+  static constexpr int SMEM_COL_ITER = SMEM_LINES + L * N * (int)sizeof(float);
+  static constexpr int SMEM_COL_CCD = SMEM_LINES + 3 * L * N * (int)sizeof(float);
+  static constexpr int SMEM_MAX = SMEM_ROW_ITER > SMEM_COL_CCD ? SMEM_ROW_ITER : SMEM_COL_CCD;
   __device__ __forceinline__ static int idx(int l, int i) { return l * LD + i + (i >> 4); }
 };
 
-// One Stockham pass over L lines with T threads.
-template <int N, int L, int T, int P, bool INV>
+// One Stockham pass over the L lines of Geom<N>.
+template <int N, int P, bool INV>
 __device__ __forceinline__ void fft_pass(float2* buf, const float2* tw) {
+  using G = Geom<N>;
+  constexpr int L = G::L, T = G::T;
   constexpr int R = plan_radix(N, P);
   constexpr int NS = plan_ns(N, P);
   constexpr int NR = N / R;
   constexpr int NB = L * NR;
   constexpr int B = (NB + T - 1) / T;
-  using LY = Layout<N>;
   float2 v[B][R];
 #pragma unroll
   for (int b = 0; b < B; ++b) {
@@ -183,7 +227,7 @@ __device__ __forceinline__ void fft_pass(float2* buf, const float2* tw) {
     if ((NB % T) == 0 || g < NB) {
       const int l = g / NR, j = g - l * NR;
 #pragma unroll
-      for (int r = 0; r < R; ++r) v[b][r] = buf[LY::idx(l, j + r * NR)];
+      for (int r = 0; r < R; ++r) v[b][r] = buf[G::idx(l, j + r * NR)];
     }
   }
   __syncthreads();
@@ -194,10 +238,10 @@ __device__ __forceinline__ void fft_pass(float2* buf, const float2* tw) {
       const int l = g / NR, j = g - l * NR;
       const int k = j % NS;
       if constexpr (NS > 1) {
-        constexpr int STEP = N / (NS * R);
+        const float2* twp = tw + tw_offset(N, P);
 #pragma unroll
         for (int r = 1; r < R; ++r) {
-          float2 w = tw[r * k * STEP];
+          float2 w = __ldg(twp + (r - 1) * NS + k);
           if (INV) w.y = -w.y;
           v[b][r] = cmul(v[b][r], w);
         }
@@ -205,35 +249,25 @@ __device__ __forceinline__ void fft_pass(float2* buf, const float2* tw) {
       dftR<R, INV>(v[b]);
       const int base = (j - k) * R + k;
 #pragma unroll
-      for (int r = 0; r < R; ++r) buf[LY::idx(l, base + r * NS)] = v[b][r];
+      for (int r = 0; r < R; ++r) buf[G::idx(l, base + r * NS)] = v[b][r];
     }
   }
   __syncthreads();
 }
 
-template <int N, int L, int T, int P, bool INV>
+template <int N, int P, bool INV>
 __device__ __forceinline__ void fft_passes(float2* buf, const float2* tw) {
   if constexpr (plan_radix(N, P) != 0) {
-    fft_pass<N, L, T, P, INV>(buf, tw);
-    fft_passes<N, L, T, P + 1, INV>(buf, tw);
+    fft_pass<N, P, INV>(buf, tw);
+    fft_passes<N, P + 1, INV>(buf, tw);
   }
 }
 
 // Transform all L lines in place.  Callers synchronise before the call (the
 // lines must be fully written); the call ends with a barrier.
-template <int N, int L, int T, bool INV>
+template <int N, bool INV>
 __device__ __forceinline__ void fft_lines(float2* buf, const float2* tw) {
-  fft_passes<N, L, T, 0, INV>(buf, tw);
+  fft_passes<N, 0, INV>(buf, tw);
 }
-
-// Launch geometry per length: L lines per CTA and T threads, so that each
-// thread holds about 16 complex values per pass.
-template <int N>
-struct Geom {
-  static constexpr int T = N >= 768 ? 512 : 256;
-  static constexpr int ELEMS = 16 * T;
-  static constexpr int L = (ELEMS / N) < 1 ? 1 : (ELEMS / N);
-  static constexpr int SMEM = (N + L * Layout<N>::LD) * (int)sizeof(float2);
-};
 
 }  // namespace cdx

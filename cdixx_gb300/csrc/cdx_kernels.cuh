@@ -115,130 +115,241 @@ __device__ __forceinline__ double block_sum_d(double v, double* red) {
   return r;
 }
 
+// ------------------------------------------------------------ async copies
+// cp.async global -> shared; with `valid` false the destination is zero-filled
+// and nothing is read.
+__device__ __forceinline__ void cp_async8(void* dst, const void* src, bool valid) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(s), "l"(src), "r"(valid ? 8 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, bool valid) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(src), "r"(valid ? 16 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* dst, const void* src, bool valid) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(s), "l"(src), "r"(valid ? 4 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int PENDING>
+__device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(PENDING) : "memory"); }
+
+// ------------------------------------------------------------------ layouts
+// Element (r, c) of a column-tiled array of `rows` rows with tile width 2^tl.
+__device__ __forceinline__ long long tiled_off(int r, int c, int rows, int tl) {
+  return ((((long long)(c >> tl)) * rows + r) << tl) + (c & ((1 << tl) - 1));
+}
+
+// Element e of a row CTA's L rows -> (row l, column c).  For column-tiled
+// global arrays the order is chunk-major: one chunk is the CTA's L rows x one
+// tile width, contiguous in HBM, so consecutive threads fill whole sectors.
+template <int N, int L, int LOG2L>
+__device__ __forceinline__ void row_elem(int e, int tiled, int tl, int& l, int& c) {
+  if (tiled && (N & ((1 << tl) - 1)) == 0) {   // whole tiles per row
+    const int q = e & ((L << tl) - 1);
+    l = q >> tl;
+    c = ((e >> (LOG2L + tl)) << tl) + (q & ((1 << tl) - 1));
+  } else {
+    l = e / N;
+    c = e - l * N;
+  }
+}
+
 // ------------------------------------------------------------------ row pass
 // Lines are rows of length N (= number of columns).  Grid: (ceil(rows/L), batch).
-template <int N>
-__global__ void __launch_bounds__(Geom<N>::T) row_pass_kernel(RowArgs a) {
-  constexpr int L = Geom<N>::L, T = Geom<N>::T;
-  using LY = Layout<N>;
+template <int N, int MODE>
+__global__ void __launch_bounds__(Geom<N>::T, Geom<N>::MINB) row_pass_kernel(RowArgs a) {
+  using G = Geom<N>;
+  constexpr int L = G::L, T = G::T;
   extern __shared__ float2 smem[];
-  float2* tw = smem;
-  float2* buf = smem + N;
+  const float2* __restrict__ tw = a.tw;   // read through L1, shared by the SM's CTAs
+  float2* buf = smem;
   const int row0 = blockIdx.x * L;
   const int nrows = min(L, a.rows - row0);
-  const long long poff = (long long)blockIdx.y * a.pat_stride + (long long)row0 * N;
+  const long long pin = (long long)blockIdx.y * a.in_stride;
+  const long long pout = (long long)blockIdx.y * a.out_stride;
 
-  for (int i = threadIdx.x; i < N; i += T) tw[i] = a.tw[i];
-  // load rows (two complex per 16-byte access)
-  const float4* in4 = reinterpret_cast<const float4*>(a.in + poff);
-  for (int e = threadIdx.x; e < L * N / 2; e += T) {
-    const int l = (2 * e) / N, c = 2 * e - l * N;
-    float4 q = l < nrows ? in4[e] : make_float4(0.f, 0.f, 0.f, 0.f);
-    buf[LY::idx(l, c)] = make_float2(q.x, q.y);
-    buf[LY::idx(l, c + 1)] = make_float2(q.z, q.w);
+  // Every global read is an asynchronous copy issued up front: the rows (one
+  // group), then in ROW_ITER the L rows of rho (a second group, which lands
+  // while the inverse FFT runs).
+  const float2* in = a.in + pin;
+  constexpr bool iter = MODE == ROW_ITER;
+  float2* rho_s = smem + L * G::LD;
+  float2* rho = a.rho + (long long)blockIdx.y * a.rho_stride + (long long)row0 * N;
+#pragma unroll 4
+  for (int e = threadIdx.x; e < L * N; e += T) {
+    int l, c;
+    row_elem<N, L, G::LOG2L>(e, a.in_tiled, a.tile_log2, l, c);
+    const bool ok = l < nrows;
+    const int r = row0 + (ok ? l : 0);
+    const long long o = a.in_tiled ? tiled_off(r, c, a.rows, a.tile_log2) : (long long)r * N + c;
+    cp_async8(buf + G::idx(l, c), in + o, ok);
   }
+  cp_commit();
+  constexpr int WPR = (N + 31) >> 5;
+  uint32_t* mask_s = reinterpret_cast<uint32_t*>(rho_s + L * N);
+  if constexpr (iter) {
+#pragma unroll 4
+    for (int e = threadIdx.x; e < L * N / 2; e += T) {
+      const bool ok = (2 * e) / N < nrows;
+      cp_async16(rho_s + 2 * e, ok ? rho + 2 * e : rho, ok);
+    }
+    const uint32_t* mask = a.mask + (long long)blockIdx.y * a.mask_stride + (long long)row0 * WPR;
+    for (int w = threadIdx.x; w < L * WPR; w += T) {
+      const bool ok = w / WPR < nrows;
+      cp_async4(mask_s + w, ok ? mask + w : mask, ok);
+    }
+  }
+  cp_commit();
+  cp_wait<1>();
   __syncthreads();
 
-  if (a.mode == ROW_FFT) {
-    if (a.inv) fft_lines<N, L, T, true>(buf, tw);
-    else fft_lines<N, L, T, false>(buf, tw);
+  if constexpr (!iter) {
+    if (a.inv) fft_lines<N, true>(buf, tw);
+    else fft_lines<N, false>(buf, tw);
   } else {
-    fft_lines<N, L, T, true>(buf, tw);
+    fft_lines<N, true>(buf, tw);
+    cp_wait<0>();
+    __syncthreads();
     // rho' = IFFT/N, update against rho and the support bits
-    const int wpr = (N + 31) >> 5;
-    float2* rho = a.rho + poff;
-    const uint32_t* mask = a.mask + (long long)blockIdx.y * a.mask_stride + (long long)row0 * wpr;
     for (int e = threadIdx.x; e < L * N; e += T) {
       const int l = e / N, c = e - l * N;
+      float2 r = make_float2(0.f, 0.f);
       if (l < nrows) {
-        float2 p = buf[LY::idx(l, c)];
+        float2 p = buf[G::idx(l, c)];
         p.x *= a.inv_n;
         p.y *= a.inv_n;
-        const float2 x = rho[e];
-        const bool inside = (mask[l * wpr + (c >> 5)] >> (c & 31)) & 1u;
-        const float2 r = apply_update(a.algo, inside, x, p, a.beta);
+        const float2 x = rho_s[e];
+        const bool inside = (mask_s[l * WPR + (c >> 5)] >> (c & 31)) & 1u;
+        r = apply_update(a.algo, inside, x, p, a.beta);
         rho[e] = r;
-        buf[LY::idx(l, c)] = r;
-      } else {
-        buf[LY::idx(l, c)] = make_float2(0.f, 0.f);
       }
+      buf[G::idx(l, c)] = r;
     }
     __syncthreads();
-    fft_lines<N, L, T, false>(buf, tw);
+    fft_lines<N, false>(buf, tw);
   }
   // store rows
-  float4* out4 = reinterpret_cast<float4*>(a.out + poff);
   const float s = a.scale;
   for (int e = threadIdx.x; e < L * N / 2; e += T) {
-    const int l = (2 * e) / N, c = 2 * e - l * N;
+    int l, c;
+    row_elem<N, L, G::LOG2L>(2 * e, a.out_tiled, a.tile_log2, l, c);
     if (l < nrows) {
-      float2 u = buf[LY::idx(l, c)], v = buf[LY::idx(l, c + 1)];
+      float2 u = buf[G::idx(l, c)], v = buf[G::idx(l, c + 1)];
       if (s != 1.f) { u.x *= s; u.y *= s; v.x *= s; v.y *= s; }
-      out4[e] = make_float4(u.x, u.y, v.x, v.y);
+      const int r = row0 + l;
+      const long long o = a.out_tiled ? tiled_off(r, c, a.rows, a.tile_log2) : (long long)r * N + c;
+      *reinterpret_cast<float4*>(a.out + pout + o) = make_float4(u.x, u.y, v.x, v.y);
     }
   }
 }
 
 // --------------------------------------------------------------- column pass
 // Lines are columns of length N (= number of rows).  Grid: (ceil(cols/L), batch).
-template <int N>
-__global__ void __launch_bounds__(Geom<N>::T) col_pass_kernel(ColArgs a) {
-  constexpr int L = Geom<N>::L, T = Geom<N>::T;
-  using LY = Layout<N>;
+// Column-tiled arrays here have tile width L, so the CTA's tile is the
+// contiguous block [blockIdx.x * N * L, +N*L) with element t = r*L + l.
+template <int N, int MODE>
+__global__ void __launch_bounds__(Geom<N>::T, Geom<N>::MINB) col_pass_kernel(ColArgs a) {
+  using G = Geom<N>;
+  constexpr int L = G::L, T = G::T, LL = G::LOG2L;
   extern __shared__ float2 smem[];
   __shared__ double red[T / 32];
-  float2* tw = smem;
-  float2* buf = smem + N;
+  const float2* __restrict__ tw = a.tw;
+  float2* buf = smem;
   const int c0 = blockIdx.x * L;
   const int ncols = min(L, a.cols - c0);
   const long long C = a.cols;
-  const long long poff = (long long)blockIdx.y * a.pat_stride + c0;
+  const long long tile = (long long)blockIdx.x * N * L;
 
-  for (int i = threadIdx.x; i < N; i += T) tw[i] = a.tw[i];
-  const float2* in = a.in + poff;
-  for (int e = threadIdx.x; e < L * N; e += T) {
-    const int r = e / L, l = e - r * L;
-    buf[LY::idx(l, r)] = l < ncols ? in[r * C + l] : make_float2(0.f, 0.f);
+  // Asynchronous copies issued up front: the column tile (one group), then in
+  // COL_ITER the tile's sqrt(I) (and I, beamstop for PROJ_CCD), a second group
+  // that lands while the forward FFT runs.
+  constexpr bool iter = MODE == COL_ITER;
+  const bool ccd = iter && a.proj == PROJ_CCD;
+  float* amp_s = reinterpret_cast<float*>(smem + L * G::LD);
+  float* int_s = amp_s + L * N;
+  float* bs_s = int_s + L * N;
+  {
+    const float2* in = a.in + (long long)blockIdx.y * a.in_stride;
+    if (a.in_tiled) {
+#pragma unroll 4
+      for (int t = threadIdx.x; t < L * N; t += T) {
+        const int r = t >> LL, l = t & (L - 1);
+        cp_async8(buf + G::idx(l, r), in + tile + t, true);
+      }
+    } else {
+#pragma unroll 4
+      for (int t = threadIdx.x; t < L * N; t += T) {
+        const int r = t >> LL, l = t & (L - 1);
+        const bool ok = l < ncols;
+        cp_async8(buf + G::idx(l, r), in + r * C + c0 + (ok ? l : 0), ok);
+      }
+    }
   }
+  cp_commit();
+  const long long aux = (long long)blockIdx.y * a.aux_stride + tile;
+  if constexpr (iter) {
+    // tiled auxiliaries are padded to whole tiles: always in bounds
+#pragma unroll 4
+    for (int q = threadIdx.x; q < L * N / 4; q += T) {
+      cp_async16(amp_s + 4 * q, a.amp + aux + 4 * q, true);
+      if (ccd) {
+        cp_async16(int_s + 4 * q, a.inten + aux + 4 * q, true);
+        if (a.bs) cp_async16(bs_s + 4 * q, a.bs + aux + 4 * q, true);
+      }
+    }
+  }
+  cp_commit();
+  cp_wait<1>();
   __syncthreads();
 
-  if (a.mode == COL_FFT) {
-    if (a.inv) fft_lines<N, L, T, true>(buf, tw);
-    else fft_lines<N, L, T, false>(buf, tw);
+  if constexpr (!iter) {
+    if (a.inv) fft_lines<N, true>(buf, tw);
+    else fft_lines<N, false>(buf, tw);
   } else {
-    if (!a.from_psi) fft_lines<N, L, T, false>(buf, tw);
+    if (!a.from_psi) fft_lines<N, false>(buf, tw);
+    cp_wait<0>();
+    __syncthreads();
     // Psi is complete here: optional copy-out, R-factor partial, projection
     double rsum = 0.0;
-    const long long aoff = (long long)blockIdx.y * a.pat_stride + c0;
-    for (int e = threadIdx.x; e < L * N; e += T) {
-      const int r = e / L, l = e - r * L;
+    for (int t = threadIdx.x; t < L * N; t += T) {
+      const int r = t >> LL, l = t & (L - 1);
       if (l < ncols) {
-        const long long gi = aoff + r * C + l;
-        float2 s = buf[LY::idx(l, r)];
-        if (a.psi_out) a.psi_out[gi] = s;
-        const float amp = a.amp[gi];
+        float2 s = buf[G::idx(l, r)];
+        if (a.psi_out) a.psi_out[(long long)blockIdx.y * a.psi_stride + r * C + c0 + l] = s;
+        const float amp = amp_s[t];
         if (a.rf_partials) rsum += fabsf(hypotf(s.x, s.y) - amp);
         if (a.proj == PROJ_MODABS) s = proj_modabs(s, amp);
-        else s = proj_ccd(s, a.inten[gi], a.bs ? a.bs[gi] : 0.f, a.bs != nullptr,
+        else s = proj_ccd(s, int_s[t], a.bs ? bs_s[t] : 0.f, a.bs != nullptr,
                           a.noise_level, a.ccd_scale, a.ccd_rcolor);
-        buf[LY::idx(l, r)] = s;
+        buf[G::idx(l, r)] = s;
       }
     }
     if (a.rf_partials) {
-      double t = block_sum_d<T>(rsum, red);
-      if (threadIdx.x == 0) a.rf_partials[(long long)blockIdx.y * gridDim.x + blockIdx.x] = t;
+      double tsum = block_sum_d<T>(rsum, red);
+      if (threadIdx.x == 0) a.rf_partials[(long long)blockIdx.y * gridDim.x + blockIdx.x] = tsum;
     }
     __syncthreads();
-    fft_lines<N, L, T, true>(buf, tw);
+    fft_lines<N, true>(buf, tw);
   }
-  float2* out = a.out + poff;
   const float s = a.scale;
-  for (int e = threadIdx.x; e < L * N; e += T) {
-    const int r = e / L, l = e - r * L;
-    if (l < ncols) {
-      float2 v = buf[LY::idx(l, r)];
-      if (s != 1.f) { v.x *= s; v.y *= s; }
-      out[r * C + l] = v;
+  float2* out = a.out + (long long)blockIdx.y * a.out_stride;
+  if (a.out_tiled) {
+    float4* out4 = reinterpret_cast<float4*>(out + tile);
+    for (int e = threadIdx.x; e < L * N / 2; e += T) {
+      const int t = 2 * e, r = t >> LL, l = t & (L - 1);
+      float2 u = buf[G::idx(l, r)], v = buf[G::idx(l + 1, r)];
+      if (s != 1.f) { u.x *= s; u.y *= s; v.x *= s; v.y *= s; }
+      out4[e] = make_float4(u.x, u.y, v.x, v.y);
+    }
+  } else {
+    for (int t = threadIdx.x; t < L * N; t += T) {
+      const int r = t >> LL, l = t & (L - 1);
+      if (l < ncols) {
+        float2 v = buf[G::idx(l, r)];
+        if (s != 1.f) { v.x *= s; v.y *= s; }
+        out[r * C + c0 + l] = v;
+      }
     }
   }
 }

@@ -70,6 +70,30 @@ cudaError_t convert_fo_complex(const float2* in, float2* out, int rows, int cols
   return cudaGetLastError();
 }
 
+// Row-major (rows x cols) -> column-tiled with tile width 2^tl (padding columns
+// of the last tile set to 0).  `out_stride` elements between patterns.
+__global__ void k_to_tiled(const float* __restrict__ in, float* __restrict__ out, int rows, int cols, int tl,
+                           long long out_stride, int batch) {
+  const int tw = 1 << tl;
+  const int cp = ((cols + tw - 1) >> tl) << tl;
+  const long long per = (long long)rows * cp;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < per * batch;
+       g += (long long)gridDim.x * blockDim.x) {
+    const long long p = g / per, i = g - p * per;
+    // i enumerates the tiled array: tile, row, lane
+    const long long tile = i / ((long long)rows << tl);
+    const long long rem = i - tile * ((long long)rows << tl);
+    const int r = (int)(rem >> tl), c = (int)(tile << tl) + (int)(rem & (tw - 1));
+    out[p * out_stride + i] = c < cols ? in[p * (long long)rows * cols + (long long)r * cols + c] : 0.f;
+  }
+}
+cudaError_t to_tiled(const float* in, float* out, int rows, int cols, int tl, long long out_stride, int batch,
+                     cudaStream_t st) {
+  const int cp = ((cols + (1 << tl) - 1) >> tl) << tl;
+  k_to_tiled<<<grid1d((long long)rows * cp * batch, 256), 256, 0, st>>>(in, out, rows, cols, tl, out_stride, batch);
+  return cudaGetLastError();
+}
+
 // Unfused primitives with the reference's element-wise semantics.
 __global__ void k_mod_abs(float2* __restrict__ psi, const float* __restrict__ inten, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
@@ -283,13 +307,14 @@ __global__ void k_residual(const float2* __restrict__ psi, const float* __restri
   if (threadIdx.x == 0) part[p * nblk + blockIdx.x] = t;
 }
 // R-factor of a complete Psi: sum | |Psi| - sqrt(I) |.
-__global__ void k_rdiff(const float2* __restrict__ psi, const float* __restrict__ amp, long long npx,
+__global__ void k_rdiff(const float2* __restrict__ psi, const float* __restrict__ inten, long long npx,
                         double* __restrict__ part, int nblk) {
   const long long p = blockIdx.y;
   double acc = 0.0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npx; i += (long long)nblk * blockDim.x) {
     const float2 v = psi[p * npx + i];
-    acc += (double)fabsf(hypotf(v.x, v.y) - amp[p * npx + i]);
+    const float I = inten[p * npx + i];
+    acc += (double)fabsf(hypotf(v.x, v.y) - (I > 0.f ? sqrtf(I) : 0.f));
   }
   __shared__ double red[8];
   double t = block_sum_d<256>(acc, red);
@@ -319,9 +344,9 @@ cudaError_t residual(const float2* psi, const float* inten, long long npx, int b
   k_finalize_sum<<<batch, 32, 0, st>>>(part, nblk, stt, 1);
   return cudaGetLastError();
 }
-cudaError_t rfactor(const float2* psi, const float* amp, long long npx, int batch, double* part, int nblk,
+cudaError_t rfactor(const float2* psi, const float* inten, long long npx, int batch, double* part, int nblk,
                     PatState* stt, cudaStream_t st) {
-  k_rdiff<<<dim3(nblk, batch), 256, 0, st>>>(psi, amp, npx, part, nblk);
+  k_rdiff<<<dim3(nblk, batch), 256, 0, st>>>(psi, inten, npx, part, nblk);
   k_finalize_sum<<<batch, 32, 0, st>>>(part, nblk, stt, 2);
   return cudaGetLastError();
 }

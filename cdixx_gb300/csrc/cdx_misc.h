@@ -9,6 +9,8 @@ cudaError_t scale_complex(float2* x, float s, long long n, cudaStream_t st);
 cudaError_t scale_real(float* x, float s, long long n, cudaStream_t st);
 cudaError_t convert_fo_real(const float* in, float* out, int rows, int cols, int batch, cudaStream_t st);
 cudaError_t convert_fo_complex(const float2* in, float2* out, int rows, int cols, int batch, cudaStream_t st);
+cudaError_t to_tiled(const float* in, float* out, int rows, int cols, int tl, long long out_stride, int batch,
+                     cudaStream_t st);
 cudaError_t mod_abs(float2* psi, const float* inten, long long n, cudaStream_t st);
 cudaError_t mod_ccd(float2* psi, const float* inten, const float* bs, int noise, float scale, float rcolor,
                     long long n, cudaStream_t st);
@@ -24,7 +26,7 @@ cudaError_t pattern_amp_sum(const float* amp, long long npx, int batch, double* 
                             cudaStream_t st);
 cudaError_t residual(const float2* psi, const float* inten, long long npx, int batch, double* part, int nblk,
                      PatState* stt, cudaStream_t st);
-cudaError_t rfactor(const float2* psi, const float* amp, long long npx, int batch, double* part, int nblk,
+cudaError_t rfactor(const float2* psi, const float* inten, long long npx, int batch, double* part, int nblk,
                     PatState* stt, cudaStream_t st);
 cudaError_t rfactor_from_partials(const double* part, int nblk, int batch, PatState* stt, cudaStream_t st);
 cudaError_t run_begin(PatState* stt, int batch, cudaStream_t st);

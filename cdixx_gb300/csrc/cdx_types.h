@@ -1,4 +1,10 @@
 // Kernel argument blocks and codes shared by the CUDA translation units.
+//
+// HBM layouts.  A rows x cols array is either row-major (element (r,c) at
+// r*cols + c) or column-tiled with tile width TW (a power of two): element
+// (r,c) at ((c/TW)*rows + r)*TW + c%TW, the width padded to a multiple of TW.
+// A column-pass CTA covering TW columns then reads one contiguous block, and
+// a row-pass CTA covering several rows moves whole 32-byte sectors.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -16,16 +22,20 @@ enum : int { COL_FFT = 0, COL_ITER = 1 };
 enum : int { PROJ_MODABS = 0, PROJ_CCD = 1 };
 
 struct RowArgs {
-  const float2* in;        // rows to load (pattern-major, row-major)
-  float2* out;             // rows to store (may alias in)
-  float2* rho;             // ROW_ITER: real-space iterate, updated in place
+  const float2* in;        // rows to load
+  float2* out;             // rows to store (may alias in when the layouts match)
+  float2* rho;             // ROW_ITER: real-space iterate (row-major), updated in place
   const uint32_t* mask;    // ROW_ITER: support bits, (cols+31)/32 words per row
-  const float2* tw;        // W_N^t, t < N (forward)
+  const float2* tw;        // per-pass twiddles of length cols
   int rows;                // lines per pattern
   int mode;                // ROW_FFT / ROW_ITER
   int inv;                 // ROW_FFT direction
   int algo;                // ROW_ITER update
-  long long pat_stride;    // complex elements between patterns
+  int in_tiled, out_tiled; // 0: row-major, 1: column-tiled with width 1 << tile_log2
+  int tile_log2;
+  long long in_stride;     // elements between patterns
+  long long out_stride;
+  long long rho_stride;
   long long mask_stride;   // mask words between patterns
   float scale;             // factor applied on store (1 = none)
   float inv_n;             // 1/(rows*cols) (applyNorm after the inverse FFT)
@@ -33,21 +43,22 @@ struct RowArgs {
 };
 
 struct ColArgs {
-  const float2* in;
-  float2* out;             // may alias in
-  float2* psi_out;         // COL_ITER: optional copy of Psi before the projection
-  const float* amp;        // sqrt(max(I,0)), row-major FFT order
-  const float* inten;      // I (PROJ_CCD)
-  const float* bs;         // beamstop (PROJ_CCD), may be null
+  const float2* in;        // columns to load
+  float2* out;             // columns to store (may alias in when the layouts match)
+  float2* psi_out;         // COL_ITER: optional row-major copy of Psi before the projection
+  const float* amp;        // sqrt(max(I,0)), column-tiled (width = the kernel's L)
+  const float* inten;      // I, column-tiled (PROJ_CCD)
+  const float* bs;         // beamstop, column-tiled (PROJ_CCD), may be null
   double* rf_partials;     // optional: per-CTA sum | |Psi| - sqrt(I) |
-  const float2* tw;
+  const float2* tw;        // per-pass twiddles of length rows
   int cols;                // lines per pattern
   int mode;                // COL_FFT / COL_ITER
   int inv;                 // COL_FFT direction
   int from_psi;            // COL_ITER: input already holds Psi (skip the forward FFT)
   int proj;                // PROJ_MODABS / PROJ_CCD
   int noise_level;
-  long long pat_stride;    // elements between patterns (complex and real arrays alike)
+  int in_tiled, out_tiled; // 0: row-major, 1: column-tiled with width L
+  long long in_stride, out_stride, aux_stride, psi_stride;
   float scale;
   float ccd_scale;         // vars.scale
   float ccd_rcolor;        // vars.rcolor
@@ -76,5 +87,8 @@ PrepLaunch prep_launcher(int n);   // nullptr: unsupported length
 RowLaunch row_launcher(int n);
 ColLaunch col_launcher(int n);
 int lines_per_cta(int n);          // lines (rows or columns) per CTA for length n
+int twiddle_count(int n);          // entries of the per-pass twiddle table of length n
+// host: fill the per-pass twiddle table of length n (double precision, rounded once)
+void twiddle_table(int n, float2* out);
 
 }  // namespace cdx
