@@ -175,7 +175,7 @@ void fourier_kernel(int n, double sf, std::vector<float>& w, int& off, int& rad)
 // applyGaussConv sizes it (src/post_gpu/misc.cc:80-86).
 void spatial_kernel(int n, double sigma, std::vector<float>& w, int& off, int& rad) {
   int r = ((int)std::floor(sigma * 6)) >> 1;
-  r = std::max(0, std::min(r, (n - 1) / 2));
+  r = std::max(0, std::min(std::min(r, (n - 1) / 2), 64));   // 64: the stencil kernels' largest radius
   std::vector<double> k(2 * r + 1);
   double s = 0.0;
   for (int d = -r; d <= r; ++d) s += (k[d + r] = std::exp(-(double)d * d / (2.0 * sigma * sigma)));

@@ -1,5 +1,7 @@
 // Element-wise primitives, shrinkwrap stencil, deterministic reductions and
 // initialisation kernels of the CDI path (sm_103a).
+#include <algorithm>
+
 #include "cdx_misc.h"
 #include "cdx_kernels.cuh"
 
@@ -172,63 +174,88 @@ cudaError_t support_bits(const float* spt, const PatState* st_or_null, float fix
 // (or |rho|^2 as a real field), then along the columns index (y), writing the
 // real support field: |s*v|^2 (Fourier-Gaussian mode, s = rows*cols restores
 // the unnormalised IFFT scale of the reference) or Re v (|rho|^2 mode).
-__global__ void k_blur_x(const float2* __restrict__ rho, float2* __restrict__ tmp, const float* __restrict__ w,
-                         int rad, int rows, int cols, int batch, int mod2_first) {
+constexpr int kBlurRadMax = 64;   // largest stencil radius (host-checked)
+constexpr int kBlurTX = 64;       // output rows per CTA of the x pass
+
+__device__ __forceinline__ int wrap(int i, int n) {
+  i %= n;
+  return i < 0 ? i + n : i;
+}
+
+// x pass: CTA = 32 columns x kBlurTX rows of outputs; the rows it needs (with
+// the periodic halo of `rad` on both sides) are staged in shared memory.
+__global__ void __launch_bounds__(256) k_blur_x(const float2* __restrict__ rho, float2* __restrict__ tmp,
+                                                const float* __restrict__ w, int rad, int rows, int cols,
+                                                int mod2_first) {
+  __shared__ float2 s[(kBlurTX + 2 * kBlurRadMax) * 32];
+  __shared__ float ws[2 * kBlurRadMax + 1];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int y = blockIdx.x * 32 + tx;
+  const int x0 = blockIdx.y * kBlurTX;
   const long long npx = (long long)rows * cols;
-  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < npx * batch; g += (long long)gridDim.x * blockDim.x) {
-    const long long p = g / npx, i = g - p * npx;
-    const int x = (int)(i / cols), y = (int)(i - (long long)x * cols);
-    const float2* src = rho + p * npx;
+  const float2* src = rho + blockIdx.z * npx;
+  for (int i = threadIdx.x; i <= 2 * rad; i += 256) ws[i] = w[i];
+  const int nload = kBlurTX + 2 * rad;
+  for (int j = ty; j < nload; j += 8) {
+    float2 v = make_float2(0.f, 0.f);
+    if (y < cols) v = src[(long long)wrap(x0 - rad + j, rows) * cols + y];
+    if (mod2_first) v = make_float2(v.x * v.x + v.y * v.y, 0.f);
+    s[j * 32 + tx] = v;
+  }
+  __syncthreads();
+  if (y >= cols) return;
+  for (int k = ty; k < kBlurTX && x0 + k < rows; k += 8) {
     float sx = 0.f, sy = 0.f;
-    for (int d = -rad; d <= rad; ++d) {
-      int xx = x + d;
-      xx = xx < 0 ? xx + rows : (xx >= rows ? xx - rows : xx);
-      float2 v = src[(long long)xx * cols + y];
-      const float wd = w[d + rad];
-      if (mod2_first) {
-        sx = fmaf(wd, v.x * v.x + v.y * v.y, sx);
-      } else {
-        sx = fmaf(wd, v.x, sx);
-        sy = fmaf(wd, v.y, sy);
-      }
+    for (int d = 0; d <= 2 * rad; ++d) {
+      const float2 v = s[(k + d) * 32 + tx];
+      sx = fmaf(ws[d], v.x, sx);
+      sy = fmaf(ws[d], v.y, sy);
     }
-    tmp[g] = make_float2(sx, sy);
+    tmp[blockIdx.z * npx + (long long)(x0 + k) * cols + y] = make_float2(sx, sy);
   }
 }
 
-__global__ void k_blur_y(const float2* __restrict__ tmp, float* __restrict__ spt, const float* __restrict__ w,
-                         int rad, int rows, int cols, int batch, int mod2_first, float s,
-                         float* __restrict__ pmax, double* __restrict__ psum, int nblk_per_pat) {
-  // grid: (nblk_per_pat, batch)
+// y pass: CTA = 256-column segments of rows blockIdx.y, +gridDim.y, ...; the
+// segment with its periodic halo is staged in shared memory.  Writes the
+// support field and per-CTA max / sum partials.
+__global__ void __launch_bounds__(256) k_blur_y(const float2* __restrict__ tmp, float* __restrict__ spt,
+                                                const float* __restrict__ w, int rad, int rows, int cols,
+                                                int mod2_first, float s, float* __restrict__ pmax,
+                                                double* __restrict__ psum) {
+  __shared__ float2 seg[256 + 2 * kBlurRadMax];
+  __shared__ float ws[2 * kBlurRadMax + 1];
   const long long npx = (long long)rows * cols;
-  const long long p = blockIdx.y;
+  const long long p = blockIdx.z;
   const float2* src = tmp + p * npx;
   float* out = spt + p * npx;
+  for (int i = threadIdx.x; i <= 2 * rad; i += 256) ws[i] = w[i];
+  const int y0 = blockIdx.x * 256, y = y0 + threadIdx.x;
   float m = 0.f;   // findMax initialises with 0 (src/gpu/cub_wrap.cu:88-92)
   double acc = 0.0;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npx; i += (long long)nblk_per_pat * blockDim.x) {
-    const int x = (int)(i / cols), y = (int)(i - (long long)x * cols);
-    const float2* row = src + (long long)x * cols;
-    float sx = 0.f, sy = 0.f;
-    for (int d = -rad; d <= rad; ++d) {
-      int yy = y + d;
-      yy = yy < 0 ? yy + cols : (yy >= cols ? yy - cols : yy);
-      const float2 v = row[yy];
-      const float wd = w[d + rad];
-      sx = fmaf(wd, v.x, sx);
-      sy = fmaf(wd, v.y, sy);
+  for (int r = blockIdx.y; r < rows; r += gridDim.y) {
+    __syncthreads();
+    for (int j = threadIdx.x; j < 256 + 2 * rad; j += 256)
+      seg[j] = src[(long long)r * cols + wrap(y0 - rad + j, cols)];
+    __syncthreads();
+    if (y < cols) {
+      float sx = 0.f, sy = 0.f;
+      for (int d = 0; d <= 2 * rad; ++d) {
+        const float2 v = seg[threadIdx.x + d];
+        sx = fmaf(ws[d], v.x, sx);
+        sy = fmaf(ws[d], v.y, sy);
+      }
+      float o;
+      if (mod2_first) {
+        o = sx;
+      } else {
+        sx *= s;
+        sy *= s;
+        o = sx * sx + sy * sy;
+      }
+      out[(long long)r * cols + y] = o;
+      m = fmaxf(m, o);   // a NaN input is dropped by fmaxf; the finaliser checks the sum
+      acc += (double)o;
     }
-    float o;
-    if (mod2_first) {
-      o = sx;
-    } else {
-      sx *= s;
-      sy *= s;
-      o = sx * sx + sy * sy;
-    }
-    out[i] = o;
-    m = fmaxf(m, o);   // a NaN input is dropped by fmaxf; the finaliser checks the sum
-    acc += (double)o;
   }
   __shared__ float sm[32];
   __shared__ double sd[32];
@@ -241,8 +268,9 @@ __global__ void k_blur_y(const float2* __restrict__ tmp, float* __restrict__ spt
     float mm = 0.f;
     double ss = 0.0;
     for (int i = 0; i < (int)(blockDim.x >> 5); ++i) { mm = fmaxf(mm, sm[i]); ss += sd[i]; }
-    pmax[p * nblk_per_pat + blockIdx.x] = mm;
-    psum[p * nblk_per_pat + blockIdx.x] = ss;
+    const int nb = gridDim.x * gridDim.y, b = blockIdx.y * gridDim.x + blockIdx.x;
+    pmax[p * nb + b] = mm;
+    psum[p * nb + b] = ss;
   }
 }
 
@@ -272,10 +300,15 @@ __global__ void k_shrink_finalize(const float* __restrict__ pmax, const double* 
 cudaError_t shrinkwrap(const float2* rho, float2* tmp, float* spt, const float* wx, int radx, const float* wy,
                        int rady, int rows, int cols, int batch, int mod2_first, float s, float* pmax, double* psum,
                        int nblk, PatState* stt, double shrink_threshold, cudaStream_t st) {
-  const long long n = (long long)rows * cols * batch;
-  k_blur_x<<<grid1d(n, 256), 256, 0, st>>>(rho, tmp, wx, radx, rows, cols, batch, mod2_first);
-  k_blur_y<<<dim3(nblk, batch), 256, 0, st>>>(tmp, spt, wy, rady, rows, cols, batch, mod2_first, s, pmax, psum, nblk);
-  k_shrink_finalize<<<batch, 32, 0, st>>>(pmax, psum, nblk, stt, rows, cols, mod2_first, shrink_threshold);
+  if (radx > kBlurRadMax || rady > kBlurRadMax || radx < 0 || rady < 0) return cudaErrorInvalidValue;
+  k_blur_x<<<dim3((cols + 31) / 32, (rows + kBlurTX - 1) / kBlurTX, batch), 256, 0, st>>>(rho, tmp, wx, radx, rows,
+                                                                                          cols, mod2_first);
+  // y pass: gx segments per row, gy row groups; gx*gy <= nblk partials per pattern
+  const int gx = (cols + 255) / 256;
+  const int gy = std::max(1, std::min(rows, nblk / gx));
+  if (gx * gy > nblk) return cudaErrorInvalidValue;
+  k_blur_y<<<dim3(gx, gy, batch), 256, 0, st>>>(tmp, spt, wy, rady, rows, cols, mod2_first, s, pmax, psum);
+  k_shrink_finalize<<<batch, 32, 0, st>>>(pmax, psum, gx * gy, stt, rows, cols, mod2_first, shrink_threshold);
   return cudaGetLastError();
 }
 
