@@ -10,13 +10,15 @@
 
 namespace cdx {
 
-static thread_local std::string g_err;
+// Fixed per-thread buffer: recording an error never allocates.
+static thread_local char g_err[512];
 
-int set_error(int code, const std::string& msg) {
-  g_err = msg;
+int set_error_cstr(int code, const char* msg) {
+  snprintf(g_err, sizeof g_err, "%s", msg ? msg : "");
   return code;
 }
-const char* last_error() { return g_err.c_str(); }
+int set_error(int code, const std::string& msg) { return set_error_cstr(code, msg.c_str()); }
+const char* last_error() { return g_err; }
 
 // ------------------------------------------------------------------ AlgoParser
 // Grammar of AlgoParser (src/independant/readConfig.cc:82-163):

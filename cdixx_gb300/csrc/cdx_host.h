@@ -17,6 +17,7 @@ enum {
 };
 
 int set_error(int code, const std::string& msg);
+int set_error_cstr(int code, const char* msg);
 const char* last_error();
 int algo_expand(const char* f, std::vector<int>& out, size_t limit);
 int read_bin(const char* path, int* rows, int* cols, int* is_complex, float* data, size_t cap);

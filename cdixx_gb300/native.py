@@ -79,6 +79,7 @@ _SIGS = {
     "cdx_apply_mod": [_P, _P, _P, _I, _F, _I, _LL, _P],
     "cdx_apply_support": [_P, _P, _P, _F, _F, _I, _LL, _P],
     "cdx_convert_fo": [_P, _P, _I, _I, _I, _I, _P],
+    "cdx_iterate_noalloc": [_I, _I, _I, _F, _I, _P, _P, _F, _P, _P, _P, _P],
     "cdx_algo_expand": [ctypes.c_char_p, ctypes.POINTER(_I), _I, ctypes.POINTER(_I)],
     "cdx_read_bin": [ctypes.c_char_p, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I), _P,
                      ctypes.c_size_t],

@@ -150,6 +150,32 @@ int cdx_apply_support(void* rho, const void* rho_prime, const float* support, fl
 /* cudaConvertFO for complex or real arrays (cudaConfig.cu:202-216). */
 int cdx_convert_fo(const void* in, void* out, int rows, int cols, int batch, int is_complex, void* stream);
 
+/* ---------------------------------------------------------------- no device allocation */
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory: a detector's acquisition loop that cannot afford the device-wide
+ * synchronisation cudaMalloc/cudaFree bring between frames, or a plugin whose
+ * host application owns the whole device-memory budget.
+ *
+ * cdx_iterate_noalloc runs `iterations` fused iterations of update `algo`
+ * (CDX_HIO, CDX_RAAR, CDX_ER, ...; no shrinkwrap) on one rows x cols pattern,
+ * with the projection of applyModAbs: the same kernels and results as
+ * cdx_set_pattern + cdx_set_initial + cdx_set_support + cdx_run("<n>*ALGO").
+ * The caller passes DEVICE buffers: intensity (rows*cols floats, FFT order),
+ * support (floats; inside = value > threshold), psi0 (restart iterate,
+ * complex) and the outputs rho_out (object, scaled like phaseRetrieve leaves
+ * it) and psi_out (final Fourier iterate).  The call allocates nothing: its
+ * scratch is a static device array of CDX_NOALLOC_SCRATCH_BYTES inside this
+ * library, held by every GPU that loads the library until the process exits,
+ * which bounds patterns to CDX_NOALLOC_MAX_PIXELS pixels (512 x 512; larger
+ * sizes return CDX_ERR_SIZE).  All calls share that array: calls that overlap
+ * on the GPU race.  The first call on a device looks the array up on that
+ * device; make it before any stream capture.  Work is queued on `stream`. */
+#define CDX_NOALLOC_MAX_PIXELS (512 * 512)
+#define CDX_NOALLOC_SCRATCH_BYTES (6u << 20)
+int cdx_iterate_noalloc(int rows, int cols, int algo, float beta, int iterations, const float* intensity,
+                        const float* support, float threshold, const void* psi0, void* rho_out, void* psi_out,
+                        void* stream);
+
 /* ---------------------------------------------------------------- helpers */
 /* AlgoParser (readConfig.cc:82-163): expand `algorithm` into step codes.
  * Writes up to `cap` codes to `out` (may be NULL) and the total to *count. */
