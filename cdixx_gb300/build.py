@@ -19,6 +19,7 @@ CSRC = PKG / "csrc"
 LIBDIR = PKG / "_lib"
 OBJDIR = LIBDIR / "obj"
 LIB = LIBDIR / "libcdx.so"
+RUN = LIBDIR / "cdi_run"
 GENCODE = "arch=compute_103a,code=sm_103a"
 
 CU_UNITS = ["cdx_api.cu", "cdx_misc.cu", "cdx_dispatch.cu", "cdx_sizes_a.cu", "cdx_sizes_b.cu",
@@ -78,6 +79,14 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
         if r.returncode != 0:
             raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
         os.replace(str(LIB) + ".tmp", LIB)
+    # the config-driven driver (the reference's cdi_run), linked against the library
+    run_src = CSRC / "cdi_run.cc"
+    if not RUN.exists() or RUN.stat().st_mtime < max(LIB.stat().st_mtime, run_src.stat().st_mtime, hdr):
+        cmd = ["g++", "-std=c++17", "-O2", *inc, "-I/usr/local/cuda/include", str(run_src), "-o", str(RUN),
+               f"-L{LIBDIR}", "-lcdx", "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("cdi_run link failed:\n" + r.stdout + r.stderr)
     if verbose:
         print(f"built {LIB}")
     return LIB
