@@ -1,0 +1,27 @@
+#!/bin/sh
+# Builds the reference's hot-path sources (src/gpu/cdi.cu, cudaConfig.cu,
+# cub_wrap.cu, src/post_gpu/cdi.cc, src/independant/readConfig.cc,
+# memManager.cc) as HOST code from where they lie in the reference checkout,
+# through the emulation headers in oracle/refshim, into oracle/_ref/ref_harness.
+# The kernels' explicit "<<<grid, block>>>" launches are rewritten on the way
+# into the compiler (a sed filter on a pipe); nothing is copied into the repo.
+# Test infrastructure (the oracle pin); needs g++ only, no GPU.
+set -e
+REF=${1:-/root/reference}
+HERE=$(cd "$(dirname "$0")" && pwd)
+OUT="$HERE/_ref"
+SHIM="$HERE/refshim"
+mkdir -p "$OUT/obj"
+CXX="g++ -std=c++17 -O2 -w -fPIC -include $SHIM/cdxref_defs.h -I$SHIM -I$REF/include -I$REF/src/gpu"
+LAUNCH='s/\([A-Za-z_][A-Za-z0-9_]*\(<[A-Za-z0-9_ ,:]*>\)\{0,1\}\)[ ]*<<<\([^>]*\)>>>/for (cdxref::Launch cdxref_l_(\3); cdxref_l_.next();) \1/g'
+for f in src/gpu/cdi.cu src/gpu/cudaConfig.cu src/gpu/cub_wrap.cu; do
+  o="$OUT/obj/$(basename "$f").o"
+  sed "$LAUNCH" "$REF/$f" | $CXX -x c++ - -I"$REF/$(dirname "$f")" -c -o "$o"
+done
+for f in src/post_gpu/cdi.cc src/independant/readConfig.cc src/independant/memManager.cc; do
+  $CXX -c "$REF/$f" -o "$OUT/obj/$(basename "$f").o"
+done
+$CXX -c "$SHIM/cdxref_stubs.cc" -o "$OUT/obj/cdxref_stubs.o"
+$CXX -c "$SHIM/ref_harness.cc" -o "$OUT/obj/ref_harness.o"
+g++ -o "$OUT/ref_harness" "$OUT"/obj/*.o
+echo "built $OUT/ref_harness"

@@ -1,0 +1,79 @@
+// Definitions the reference's hot-path sources need from subsystems outside
+// the CDI iteration (plotting, image codecs, MNIST, Fresnel propagation,
+// FISTA), as no-ops or minimal .bin restatements, plus the host-emulation
+// globals.  Test infrastructure for the oracle pin only.
+#include <map>
+
+#include "cdxref_defs.h"
+#include "cufft.h"
+#include "cuPlotter.hpp"
+#include "imgio.hpp"
+#include "memManager.hpp"
+#include "misc.hpp"
+#include "mnistData.hpp"
+#include "propagator.hpp"
+#include "tvFilter.hpp"
+
+thread_local uint3_t blockIdx, threadIdx;
+thread_local dim3 blockDim, gridDim;
+std::map<int, cdxref_plan>& cdxref_plans() { static std::map<int, cdxref_plan> m; return m; }
+float tile[1];   // the extern __shared__ tile of applyConvolution (never launched here)
+
+cuPlotter plt;
+void cuPlotter::init(int, int, const char*) {}
+int cuPlotter::initVideo(const char*, int, bool, bool) { return 0; }
+void cuPlotter::saveVideo(int) {}
+void cuPlotter::saveFloat(void*, const char*) {}
+void cuPlotter::saveComplex(void*, const char*) {}
+void cuPlotter::plotComplex(void*, const mode, bool, Real, const char*, bool, bool, bool, const char*) {}
+void cuPlotter::plotComplexColor(void*, bool, Real, const char*, bool, bool) {}
+void cuPlotter::plotFloat(void*, const mode, bool, Real, const char*, bool, bool, bool, const char*) {}
+cuPlotter::~cuPlotter() {}
+
+// .bin images: 20-byte header {char type; int rows, cols, nchann, typesize}, then data
+Real* readImage(const char* name, int& row, int& col, void* (*)(size_t)) {
+  FILE* f = fopen(name, "rb");
+  if (!f) { fprintf(stderr, "cannot open %s\n", name); abort(); }
+  imageFile h;
+  if (fread(&h, sizeof h, 1, f) != 1 || (h.type != FLOAT && h.type != FLOAT2)) abort();
+  row = h.rows;
+  col = h.cols;
+  size_t n = (size_t)row * col * (h.type == FLOAT2 ? 2 : 1);
+  Real* p = (Real*)ccmemMngr.borrowCache(n * sizeof(Real));   // released by returnCache (cdi.cc:103)
+  if (fread(p, sizeof(Real), n, f) != n) abort();
+  fclose(f);
+  return p;
+}
+extern "C" void writeComplexImage(const char* name, void* data, int row, int column) {
+  FILE* f = fopen(name, "wb");
+  imageFile h;
+  memset(&h, 0, sizeof h);
+  h.type = FLOAT2;
+  h.rows = row;
+  h.cols = column;
+  fwrite(&h, sizeof h, 1, f);
+  fwrite(data, sizeof(Real) * 2, (size_t)row * column, f);
+  fclose(f);
+}
+extern "C" void writeFloatImage(const char* name, void* data, int row, int column) {
+  FILE* f = fopen(name, "wb");
+  imageFile h;
+  memset(&h, 0, sizeof h);
+  h.type = FLOAT;
+  h.rows = row;
+  h.cols = column;
+  fwrite(&h, sizeof h, 1, f);
+  fwrite(data, sizeof(Real), (size_t)row * column, f);
+  fclose(f);
+}
+complexFormat findMiddle(Real*, int) { return 0; }
+complexFormat findMiddle(complexFormat*, int) { return 0; }
+Real* createBeamStop(int, int, int) { abort(); }
+void readComplexWaveFront(const char*, const char*, Real*&, Real*&, int&, int&) { abort(); }
+void FISTA(Real*, Real*, Real, int, void (*)(Real*, Real*)) { abort(); }
+mnistData::mnistData(const char*) {}
+mnistData::~mnistData() {}
+cuMnist::cuMnist(const char* d, int, int, int, int) : mnistData(d) {}
+void cuMnist::cuRead(void*) { abort(); }
+void propagator::multiplyFresnelPhase(complexFormat*) { abort(); }
+void propagator::removeFresnelPhase(complexFormat*) { abort(); }

@@ -1,0 +1,55 @@
+// Runs the reference's own CDI::phaseRetrieve (src/post_gpu/cdi.cc), built as
+// host code from the reference sources, on a pattern and restart iterate from
+// .bin files, and writes rho, Psi, the support field, the threshold and the
+// residual.  Test infrastructure for the oracle pin.
+//
+// ref_harness <pattern.bin (centred float)> <restart.bin (complex, FFT order)>
+//             <algorithm> <oversampling_spt> <shrinkThreshold> <exposure>
+//             <simCCDbit> <noiseLevel> <out prefix>
+#include <cstdio>
+#include <cstdlib>
+
+#include "cdi.hpp"
+#include "cudaConfig.hpp"
+#include "imgio.hpp"
+
+struct cudaVars {   // layout of __constant__ vars in src/gpu/cdi.cu:8-14
+  int rcolor;
+  Real beta_HIO;
+  Real scale;
+  Real threshold;
+};
+extern cudaVars vars;
+
+int main(int argc, char** argv) {
+  if (argc < 10) {
+    fprintf(stderr, "usage: ref_harness pattern restart algorithm spt thr exposure ccd noise prefix\n");
+    return 2;
+  }
+  CDI c("none.cfg");
+  c.common.Pattern = argv[1];
+  c.common.restart = argv[2];
+  c.algorithm = argv[3];
+  c.oversampling_spt = atof(argv[4]);
+  c.shrinkThreshold = atof(argv[5]);
+  c.exposure = atof(argv[6]);
+  c.simCCDbit = atoi(argv[7]);
+  c.noiseLevel = atoi(argv[8]);
+  c.restart = 1;
+  c.runSim = 0;
+  c.useBS = 0;
+  c.prtfIter = 1 << 30;
+  c.verbose = 0;
+  c.readFiles();
+  c.init();
+  c.prepareIter();
+  c.phaseRetrieve();
+  const std::string pre = argv[9];
+  writeComplexImage((pre + "_rho.bin").c_str(), c.objectWave, c.row, c.column);
+  writeComplexImage((pre + "_psi.bin").c_str(), c.patternWave, c.row, c.column);
+  writeFloatImage((pre + "_support.bin").c_str(), c.support, c.row, c.column);
+  FILE* f = fopen((pre + "_scalars.txt").c_str(), "w");
+  fprintf(f, "threshold %.9g\nresidual %.9g\n", (double)vars.threshold, (double)c.residual);
+  fclose(f);
+  return 0;
+}

@@ -1,0 +1,71 @@
+"""Generate the golden fixtures of the CDI path from the reference's own code.
+
+Builds the reference's hot-path sources (src/gpu/cdi.cu, cudaConfig.cu,
+cub_wrap.cu, src/post_gpu/cdi.cc, readConfig.cc, memManager.cc) as host code
+with oracle/build_ref.sh, runs CDI::phaseRetrieve from a restart iterate on
+seeded synthetic 64x64 patterns, and stores inputs and outputs in
+tests/golden/reference_cases.npz.  Needs the reference checkout (default
+/root/reference) and g++; run it in the container that has them:
+
+    python tests/golden/make_golden.py [/path/to/reference]
+
+The reference's cuFFT calls run as the exact DFT in double precision
+(oracle/refshim/cufft.h) and its CUB reductions as left folds; everything
+else is the reference's code.
+"""
+import os
+import subprocess
+import sys
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+from cdixx_gb300 import synth  # noqa: E402
+from oracle import cdi_oracle as O  # noqa: E402
+
+OUT = Path(__file__).resolve().parent / "reference_cases.npz"
+N = 64
+
+# (name, algorithm, oversampling_spt, shrinkThreshold, exposure, simCCDbit, noiseLevel)
+CASES = [(f"hio_{k}", f"{k}*HIO", 2.0, 0.1, 1.0, 0, 0) for k in range(1, 11)] + [
+    ("raar_er", "6*RAAR+3*ER", 2.0, 0.1, 1.0, 0, 0),
+    ("mixed", "2*POSHIO+2*FHIO+2*POSER+1*KKT+1*XCORRELATION", 2.0, 0.1, 1.0, 0, 0),
+    ("shrinkwrap", "3*(6*HIO+1*shrinkWrap)+4*ER", 2.0, 0.1, 1.0, 0, 0),
+    ("shrink_first", "1*shrinkWrap+4*HIO", 2.0, 0.05, 1.0, 0, 0),
+    ("ccd", "6*HIO+2*ER", 2.0, 0.1, 0.5, 1, 3),
+    ("spt4", "2*(4*RAAR+1*shrinkWrap)", 4.0, 0.2, 1.0, 0, 0),
+]
+
+
+def main(ref=None):
+    ref = ref or os.environ.get("CDX_REFERENCE", "/root/reference")
+    subprocess.run([str(ROOT / "oracle" / "build_ref.sh"), ref], check=True)
+    exe = ROOT / "oracle" / "_ref" / "ref_harness"
+    obj, sup, I = synth.config0_case(seed=5, n=N, photons=1e6)
+    psi0 = synth.random_phase_start(I, 5)
+    data = {"intensity": I, "psi0": psi0}
+    with tempfile.TemporaryDirectory() as td:
+        td = Path(td)
+        for name, alg, spt, thr, exposure, ccd, noise in CASES:
+            # readPattern centres nothing: the file holds the centred pattern times
+            # the exposure, cudaConvertFO and 1/exposure bring it back (cdi.cc:105-106)
+            O.write_bin(td / "pattern.bin", np.fft.fftshift(I) * np.float32(exposure))
+            O.write_bin(td / "restart.bin", psi0)
+            subprocess.run([str(exe), "pattern.bin", "restart.bin", alg, str(spt), str(thr), str(exposure), str(ccd),
+                            str(noise), "out"], cwd=td, check=True, capture_output=True)
+            sc = dict(line.split() for line in open(td / "out_scalars.txt"))
+            data[f"{name}/rho"] = O.read_bin(td / "out_rho.bin")
+            data[f"{name}/psi"] = O.read_bin(td / "out_psi.bin")
+            data[f"{name}/support"] = O.read_bin(td / "out_support.bin")
+            data[f"{name}/scalars"] = np.array([float(sc["threshold"]), float(sc["residual"])])
+            data[f"{name}/params"] = np.array([spt, thr, exposure, ccd, noise])
+            data[f"{name}/algorithm"] = np.array(alg)
+    np.savez_compressed(OUT, **data)
+    print(f"wrote {OUT} ({OUT.stat().st_size} bytes, {len(CASES)} cases)")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else None)
