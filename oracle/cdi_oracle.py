@@ -381,7 +381,7 @@ def shrinkwrap_step(st: CDIState, shrink_threshold: float):
 def phase_retrieve(psi0, pattern, algorithm, *, support=None, oversampling_spt=2.0,
                    beta=1.0, shrink_threshold=0.1, sim_ccd_bit=False, noise_level=0,
                    exposure=1.0, rcolor=65535, beamstop=None, dtype=np.complex128,
-                   record=None, max_steps=None):
+                   record=None, max_steps=None, step_noise=None):
     """``CDI::phaseRetrieve`` from a restart iterate (src/post_gpu/cdi.cc:297-449,
     with prepareIter cdi.cc:201-227 and initSupport 252-254).
 
@@ -390,7 +390,14 @@ def phase_retrieve(psi0, pattern, algorithm, *, support=None, oversampling_spt=2
     (prtfIter beyond the run), as are plotting and video.  Returns the state;
     ``state.rho`` is scaled back by sqrt(N) (cdi.cc:406) and ``state.residual``
     is the reference's residual (cdi.cc:413-421).
+
+    ``step_noise=(eps, seed)`` (tests only, no reference counterpart) adds
+    complex Gaussian noise of relative size eps * RMS(rho) to rho after every
+    projection step: a model of the per-step rounding of a float32 FFT (whose
+    errors are about uniform in absolute size across pixels), used to bound how
+    far two float32 implementations can drift apart along a trajectory.
     """
+    noise_rng = np.random.default_rng(step_noise[1]) if step_noise else None
     rt = np.float32 if dtype == np.complex64 else np.float64
     psi, rho = prepare_from_restart(psi0, dtype)
     rows, cols = psi.shape
@@ -414,6 +421,10 @@ def phase_retrieve(psi0, pattern, algorithm, *, support=None, oversampling_spt=2
                 st.psi = apply_mod_abs(st.psi, pattern)
             rhop = (ifft2_u(st.psi) * inv_n).astype(dtype)
             st.rho = apply_support(st.rho, rhop, st.support, st.threshold, a, beta)
+            if noise_rng is not None:
+                z = noise_rng.standard_normal(st.rho.shape) + 1j * noise_rng.standard_normal(st.rho.shape)
+                rms = np.sqrt(np.mean(np.abs(st.rho) ** 2))
+                st.rho = (st.rho + step_noise[0] * rms / np.sqrt(2) * z).astype(dtype)
             st.psi = fft2_u(st.rho).astype(dtype)
         st.iter += 1
         if record is not None and k in record:

@@ -59,10 +59,21 @@ def main(ref=None):
             sc = dict(line.split() for line in open(td / "out_scalars.txt"))
             data[f"{name}/rho"] = O.read_bin(td / "out_rho.bin")
             data[f"{name}/psi"] = O.read_bin(td / "out_psi.bin")
-            data[f"{name}/support"] = O.read_bin(td / "out_support.bin")
+            if "shrinkWrap" in alg:
+                data[f"{name}/support"] = O.read_bin(td / "out_support.bin")
             data[f"{name}/scalars"] = np.array([float(sc["threshold"]), float(sc["residual"])])
             data[f"{name}/params"] = np.array([spt, thr, exposure, ccd, noise])
             data[f"{name}/algorithm"] = np.array(alg)
+        # one step from the reference's own state after k-1 HIO steps: restart from
+        # its Psi_{k-1} (prepareIter recomputes rho_{k-1} = IFFT(Psi_{k-1})/N)
+        prev = psi0
+        for k in range(1, 11):
+            O.write_bin(td / "pattern.bin", np.fft.fftshift(I))
+            O.write_bin(td / "restart.bin", prev)
+            subprocess.run([str(exe), "pattern.bin", "restart.bin", "1*HIO", "2.0", "0.1", "1.0", "0", "0", "out"],
+                           cwd=td, check=True, capture_output=True)
+            data[f"step_{k}/rho"] = O.read_bin(td / "out_rho.bin")   # input: psi0 or hio_{k-1}/psi
+            prev = data[f"hio_{k}/psi"]
     np.savez_compressed(OUT, **data)
     print(f"wrote {OUT} ({OUT.stat().st_size} bytes, {len(CASES)} cases)")
 

@@ -11,6 +11,7 @@ import pytest
 
 from cdixx_gb300 import synth
 from oracle import cdi_oracle as O
+from tests._bounds import trajectory_bound
 
 pytestmark = pytest.mark.gpu
 
@@ -153,25 +154,20 @@ def test_each_of_first_10_iterates_within_1e5(cdx, algo, beta):
 
 
 def drift(psi0, I, alg, **kw):
-    """FP32-vs-FP64 distance of the oracle itself (the reference's float arithmetic)."""
-    a = O.phase_retrieve(psi0, I, alg, **kw)
-    b = O.phase_retrieve(psi0, I, alg, dtype=np.complex64, **kw)
-    return a, rel_l2(b.rho, a.rho)
+    """(float64 oracle state, trajectory bound): see tests/_bounds.py -- the
+    divergence a 1e-7 perturbation of Psi0 produces over the same steps."""
+    return trajectory_bound(psi0, I, alg, **kw)
 
 
-# Trajectory-level bounds.  HIO/RAAR on a Poisson pattern (83 % zero-count
-# pixels) amplify rounding: the oracle run in float32 (NumPy's float32 FFT,
-# relative error 3.6e-8) already leaves the float64 trajectory by 1e-5 .. 3e-5
-# after 10 HIO/RAAR iterations.  The GPU's FP32 FFT (relative error ~1e-7, the
-# class of cuFFT's) takes the same dynamics, so its trajectory error is bounded
-# by DRIFT_FACTOR times the float32 oracle's drift (floor 1e-5).
+# Mask agreement after long HIO runs is compared with the float32 oracle's own
+# agreement with float64 (within this factor).
 DRIFT_FACTOR = 8.0
 
 
 @pytest.mark.parametrize("algo,beta", ALGOS)
 def test_trajectory_drift_no_worse_than_reference_arithmetic(cdx, algo, beta):
-    """10 iterations straight from Psi0: the FP32 path stays within DRIFT_FACTOR of
-    the float32 oracle's distance to the FP64 trajectory (floor 1e-5)."""
+    """10 iterations straight from Psi0: the FP32 path stays within the
+    trajectory bound of the FP64 oracle."""
     I, psi0 = blob_case()
     p = cdx.default_params(256, 256, oversampling_spt=4.0, beta=beta)
     with cdx.Context(p) as ctx:
@@ -181,8 +177,8 @@ def test_trajectory_drift_no_worse_than_reference_arithmetic(cdx, algo, beta):
         got = ctx.get_object(0)
     ref, d32 = drift(psi0, I, f"10*{algo}", oversampling_spt=4.0, beta=beta)
     e = rel_l2(got, ref.rho)
-    print(f"{algo} beta={beta}: gpu drift {e:.3e}, fp32 oracle drift {d32:.3e}")
-    assert e <= max(1e-5, DRIFT_FACTOR * d32)
+    print(f"{algo} beta={beta}: gpu distance {e:.3e}, bound {d32:.3e}")
+    assert e <= d32
 
 
 def test_first_step_from_restart_iterate(cdx):
@@ -253,7 +249,7 @@ def test_shrinkwrap_first_step_and_spatial_mode(cdx):
         ref, d32 = drift(psi0, I, "1*shrinkWrap+3*HIO", oversampling_spt=2.0, shrink_threshold=0.05)
         assert abs(s["threshold"] - ref.threshold) <= 1e-5 * abs(ref.threshold)
         assert np.mean((spt > s["threshold"]) == (ref.support > ref.threshold)) >= 0.999
-        assert rel_l2(ctx.get_object(0), ref.rho) <= max(1e-5, DRIFT_FACTOR * d32)
+        assert rel_l2(ctx.get_object(0), ref.rho) <= d32
     # |rho|^2 blur (holo::iterate style): threshold = max * shrinkThreshold
     p = cdx.default_params(128, 128, oversampling_spt=2.0, shrink_threshold=0.1, shrink_mode=cdx.SHRINK_SPATIAL,
                            sigma0=3.0, sigma_min=1.5)
@@ -284,7 +280,7 @@ def test_ccd_projection_iterates(cdx):
         ctx.run("5*HIO")
         got = ctx.get_object(0)
     ref, d32 = drift(psi0, I, "5*HIO", oversampling_spt=2.0, sim_ccd_bit=True, noise_level=3, exposure=0.5)
-    assert rel_l2(got, ref.rho) <= max(1e-5, 4 * d32)
+    assert rel_l2(got, ref.rho) <= d32
 
 
 def test_residual_and_rfactor(cdx):
