@@ -216,6 +216,7 @@ int col_iter(cdx_ctx* c, bool from_psi, bool rf) {
   a.inten = c->inten_t;
   a.bs = c->bs_t;
   a.aux_stride = c->wstride;
+  a.state = c->dstate;
   a.rf_partials = rf ? c->part : nullptr;
   a.tw = c->tw_r;
   a.cols = c->cols;
@@ -241,6 +242,7 @@ int row_iter(cdx_ctx* c, int algo) {
   a.rho_stride = c->npx;
   a.mask = c->mask;
   a.mask_stride = (long long)c->rows * c->wpr;
+  a.state = c->dstate;
   a.tw = c->tw_c;
   a.rows = c->rows;
   a.mode = ROW_ITER;
@@ -302,10 +304,11 @@ int enqueue_run(cdx_ctx* c, const std::vector<int>& steps, const SwPlan& sw, boo
       ++swi;
       continue;
     }
-    const bool rf = c->p.rf_every > 0 && (it % c->p.rf_every) == 0;
+    // from iteration 1 on: the restart iterate has the measured modulus by construction
+    const bool rf = c->p.rf_every > 0 && it > 0 && (it % c->p.rf_every) == 0;
     int e = col_iter(c, from_psi, rf);
     if (e) return e;
-    if (rf) CDX_CK(rfactor_from_partials(c->part, c->col_blocks, c->batch, c->dstate, c->st));
+    if (rf) CDX_CK(rfactor_from_partials(c->part, c->col_blocks, c->batch, c->dstate, c->p.stop_rfactor, it, c->st));
     e = row_iter(c, a);
     if (e) return e;
     nl += rf ? 3 : 2;
@@ -411,6 +414,75 @@ int run_impl(cdx_ctx* c, const char* algorithm) {
   return CDX_OK;
 }
 
+}  // namespace
+
+// A set of contexts run as one CUDA graph, one parallel branch per context.
+struct cdx_group {
+  std::vector<cdx_ctx*> ctxs;
+  cudaStream_t st = nullptr;
+  cudaEvent_t fork = nullptr, ev0 = nullptr, ev1 = nullptr;
+  std::vector<cudaEvent_t> joins;
+  cudaGraphExec_t gexec = nullptr;
+  std::string gkey;
+};
+
+namespace {
+
+int group_run_impl(cdx_group* g, const char* algorithm, double* gpu_ms) {
+  const size_t n = g->ctxs.size();
+  std::vector<std::vector<int>> steps(n);
+  std::vector<SwPlan> sw(n);
+  std::string key = algorithm;
+  for (size_t i = 0; i < n; ++i) {
+    cdx_ctx* c = g->ctxs[i];
+    int e = prepare_run(c, algorithm, steps[i], sw[i]);
+    if (e) return e;
+    char k[64];
+    snprintf(k, sizeof k, "|%d|%p", (int)c->psi_in_work, (void*)c->weights);
+    key += k;
+  }
+  if (key != g->gkey || !g->gexec) {
+    if (g->gexec) { cudaGraphExecDestroy(g->gexec); g->gexec = nullptr; }
+    g->gkey.clear();
+    cudaGraph_t graph = nullptr;
+    CDX_CK(cudaStreamBeginCapture(g->st, cudaStreamCaptureModeThreadLocal));
+    int e = CDX_OK;
+    cudaError_t ce = cudaEventRecord(g->fork, g->st);
+    for (size_t i = 0; i < n && ce == cudaSuccess && !e; ++i) {
+      cdx_ctx* c = g->ctxs[i];
+      ce = cudaStreamWaitEvent(c->st, g->fork, 0);   // the context's stream joins the capture
+      if (ce == cudaSuccess) e = enqueue_run(c, steps[i], sw[i], c->psi_in_work);
+      if (ce == cudaSuccess && !e) ce = cudaEventRecord(g->joins[i], c->st);
+      if (ce == cudaSuccess && !e) ce = cudaStreamWaitEvent(g->st, g->joins[i], 0);
+    }
+    cudaError_t ce2 = cudaStreamEndCapture(g->st, &graph);
+    if (e) { if (graph) cudaGraphDestroy(graph); return e; }
+    if (ce == cudaSuccess) ce = ce2;
+    if (ce != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      return set_error(CDX_ERR_CUDA, std::string("group capture: ") + cudaGetErrorString(ce));
+    }
+    ce = cudaGraphInstantiate(&g->gexec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) return set_error(CDX_ERR_CUDA, std::string("group instantiate: ") + cudaGetErrorString(ce));
+    g->gkey = key;
+  }
+  CDX_CK(cudaEventRecord(g->ev0, g->st));
+  CDX_CK(cudaGraphLaunch(g->gexec, g->st));
+  CDX_CK(cudaEventRecord(g->ev1, g->st));
+  CDX_CK(cudaStreamSynchronize(g->st));
+  for (cdx_ctx* c : g->ctxs) {
+    if (c->last_iters > 0) c->psi_in_work = false;
+    c->fresh.assign(c->batch, 0);
+  }
+  if (gpu_ms) {
+    float ms = 0.f;
+    CDX_CK(cudaEventElapsedTime(&ms, g->ev0, g->ev1));
+    *gpu_ms = ms;
+  }
+  return CDX_OK;
+}
+
 int fill_stats(cdx_ctx* c, int idx, cdx_stats* s) {
   if (!s) return CDX_OK;
   PatState h;
@@ -425,6 +497,7 @@ int fill_stats(cdx_ctx* c, int idx, cdx_stats* s) {
   s->threshold = h.threshold;
   s->flags = h.flags;
   s->launches = c->last_launches;
+  s->converged_iter = h.conv_iter;
   float ms = 0.f;
   if (cudaEventElapsedTime(&ms, c->ev0, c->ev1) == cudaSuccess) s->gpu_ms = ms;
   else cudaGetLastError();
@@ -669,6 +742,48 @@ int cdx_set_support(cdx_ctx* c, int idx, const float* support, int where) {
 }
 
 int cdx_run_async(cdx_ctx* c, const char* algorithm) { return run_impl(c, algorithm); }
+
+int cdx_group_create(cdx_ctx* const* ctxs, int n, cdx_group** out) {
+  if (!ctxs || n < 1 || !out) return set_error(CDX_ERR_ARG, "bad group argument");
+  *out = nullptr;
+  cdx_group* g = new cdx_group();
+  for (int i = 0; i < n; ++i) {
+    if (!ctxs[i]) { delete g; return set_error(CDX_ERR_ARG, "null context in group"); }
+    for (cdx_ctx* o : g->ctxs)
+      if (o->st == ctxs[i]->st) { delete g; return set_error(CDX_ERR_ARG, "group contexts must use distinct streams"); }
+    g->ctxs.push_back(ctxs[i]);
+  }
+  bool ok = cudaStreamCreateWithFlags(&g->st, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaEventCreateWithFlags(&g->fork, cudaEventDisableTiming) == cudaSuccess &&
+            cudaEventCreate(&g->ev0) == cudaSuccess && cudaEventCreate(&g->ev1) == cudaSuccess;
+  g->joins.assign(n, nullptr);
+  for (int i = 0; ok && i < n; ++i) ok = cudaEventCreateWithFlags(&g->joins[i], cudaEventDisableTiming) == cudaSuccess;
+  if (!ok) {
+    cdx_group_destroy(g);
+    return set_error(CDX_ERR_CUDA, "group stream/event creation failed");
+  }
+  *out = g;
+  return CDX_OK;
+}
+
+int cdx_group_run(cdx_group* g, const char* algorithm, double* gpu_ms) {
+  if (!g) return set_error(CDX_ERR_ARG, "null group");
+  return group_run_impl(g, algorithm, gpu_ms);
+}
+
+int cdx_group_destroy(cdx_group* g) {
+  if (!g) return CDX_OK;
+  if (g->st) cudaStreamSynchronize(g->st);
+  if (g->gexec) cudaGraphExecDestroy(g->gexec);
+  for (cudaEvent_t e : g->joins)
+    if (e) cudaEventDestroy(e);
+  if (g->fork) cudaEventDestroy(g->fork);
+  if (g->ev0) cudaEventDestroy(g->ev0);
+  if (g->ev1) cudaEventDestroy(g->ev1);
+  if (g->st) cudaStreamDestroy(g->st);
+  delete g;
+  return CDX_OK;
+}
 
 int cdx_run(cdx_ctx* c, const char* algorithm, cdx_stats* stats) {
   int e = run_impl(c, algorithm);

@@ -169,6 +169,7 @@ __global__ void __launch_bounds__(Geom<N>::T, Geom<N>::MINB) row_pass_kernel(Row
   const long long pin = (long long)blockIdx.y * a.in_stride;
   const long long pout = (long long)blockIdx.y * a.out_stride;
 
+  if (a.state && (a.state[blockIdx.y].flags & 4)) return;   // frozen pattern
   // Every global read is an asynchronous copy issued up front: the rows (one
   // group), then in ROW_ITER the L rows of rho (a second group, which lands
   // while the inverse FFT runs).
@@ -261,6 +262,16 @@ __global__ void __launch_bounds__(Geom<N>::T, Geom<N>::MINB) col_pass_kernel(Col
   const long long C = a.cols;
   const long long tile = (long long)blockIdx.x * N * L;
 
+  // A pattern whose R-factor reached the stop value (flags bit 1, set after the
+  // previous column pass) freezes here: this pass and the row pass that follows
+  // skip it from now on, leaving rho and W consistent.
+  if (a.state) {
+    const int f = a.state[blockIdx.y].flags;
+    if (f & 6) {
+      if ((f & 4) == 0 && threadIdx.x == 0) atomicOr(&a.state[blockIdx.y].flags, 4);
+      return;
+    }
+  }
   // Asynchronous copies issued up front: the column tile (one group), then in
   // COL_ITER the tile's sqrt(I) (and I, beamstop for PROJ_CCD), a second group
   // that lands while the forward FFT runs.

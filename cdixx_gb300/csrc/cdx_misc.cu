@@ -186,7 +186,8 @@ __device__ __forceinline__ int wrap(int i, int n) {
 // the periodic halo of `rad` on both sides) are staged in shared memory.
 __global__ void __launch_bounds__(256) k_blur_x(const float2* __restrict__ rho, float2* __restrict__ tmp,
                                                 const float* __restrict__ w, int rad, int rows, int cols,
-                                                int mod2_first) {
+                                                int mod2_first, const PatState* __restrict__ stt) {
+  if (stt[blockIdx.z].flags & 6) return;   // converged patterns keep their support
   __shared__ float2 s[(kBlurTX + 2 * kBlurRadMax) * 32];
   __shared__ float ws[2 * kBlurRadMax + 1];
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
@@ -221,7 +222,8 @@ __global__ void __launch_bounds__(256) k_blur_x(const float2* __restrict__ rho, 
 __global__ void __launch_bounds__(256) k_blur_y(const float2* __restrict__ tmp, float* __restrict__ spt,
                                                 const float* __restrict__ w, int rad, int rows, int cols,
                                                 int mod2_first, float s, float* __restrict__ pmax,
-                                                double* __restrict__ psum) {
+                                                double* __restrict__ psum, const PatState* __restrict__ stt) {
+  if (stt[blockIdx.z].flags & 6) return;
   __shared__ float2 seg[256 + 2 * kBlurRadMax];
   __shared__ float ws[2 * kBlurRadMax + 1];
   const long long npx = (long long)rows * cols;
@@ -281,7 +283,7 @@ __global__ void k_shrink_finalize(const float* __restrict__ pmax, const double* 
                                   PatState* __restrict__ stt, int rows, int cols, int mod2_first,
                                   double shrink_threshold) {
   const int p = blockIdx.x;
-  if (threadIdx.x != 0) return;
+  if (threadIdx.x != 0 || (stt[p].flags & 6)) return;   // converged: no partials this time
   float m = 0.f;
   double s = 0.0;
   for (int i = 0; i < nblk; ++i) { m = fmaxf(m, pmax[p * nblk + i]); s += psum[p * nblk + i]; }
@@ -302,12 +304,12 @@ cudaError_t shrinkwrap(const float2* rho, float2* tmp, float* spt, const float* 
                        int nblk, PatState* stt, double shrink_threshold, cudaStream_t st) {
   if (radx > kBlurRadMax || rady > kBlurRadMax || radx < 0 || rady < 0) return cudaErrorInvalidValue;
   k_blur_x<<<dim3((cols + 31) / 32, (rows + kBlurTX - 1) / kBlurTX, batch), 256, 0, st>>>(rho, tmp, wx, radx, rows,
-                                                                                          cols, mod2_first);
+                                                                                          cols, mod2_first, stt);
   // y pass: gx segments per row, gy row groups; gx*gy <= nblk partials per pattern
   const int gx = (cols + 255) / 256;
   const int gy = std::max(1, std::min(rows, nblk / gx));
   if (gx * gy > nblk) return cudaErrorInvalidValue;
-  k_blur_y<<<dim3(gx, gy, batch), 256, 0, st>>>(tmp, spt, wy, rady, rows, cols, mod2_first, s, pmax, psum);
+  k_blur_y<<<dim3(gx, gy, batch), 256, 0, st>>>(tmp, spt, wy, rady, rows, cols, mod2_first, s, pmax, psum, stt);
   k_shrink_finalize<<<batch, 32, 0, st>>>(pmax, psum, gx * gy, stt, rows, cols, mod2_first, shrink_threshold);
   return cudaGetLastError();
 }
@@ -355,43 +357,55 @@ __global__ void k_rdiff(const float2* __restrict__ psi, const float* __restrict_
 }
 
 // Fixed-order final sums.  what: 0 amp_sum, 1 residual, 2 rfactor (= sum / amp_sum).
-__global__ void k_finalize_sum(const double* __restrict__ part, int nblk, PatState* __restrict__ stt, int what) {
+// For an in-loop R-factor (iter >= 0) a pattern with R <= stop (stop > 0) gets
+// flags bit 1 and conv_iter = iter + 1 (it still completes this iteration).
+__global__ void k_finalize_sum(const double* __restrict__ part, int nblk, PatState* __restrict__ stt, int what,
+                               double stop, int iter) {
   const int p = blockIdx.x;
   if (threadIdx.x != 0) return;
+  if (iter >= 0 && (stt[p].flags & 6)) return;   // already converged: partials are stale
   double s = 0.0;
   for (int i = 0; i < nblk; ++i) s += part[p * nblk + i];
   if (what == 0) stt[p].amp_sum = s;
   else if (what == 1) stt[p].residual = s;
-  else stt[p].rfactor = stt[p].amp_sum > 0.0 ? s / stt[p].amp_sum : 0.0;
+  else {
+    const double r = stt[p].amp_sum > 0.0 ? s / stt[p].amp_sum : 0.0;
+    stt[p].rfactor = r;
+    if (iter >= 0 && stop > 0.0 && r <= stop) {
+      stt[p].flags |= 2;
+      stt[p].conv_iter = iter + 1;
+    }
+  }
 }
 
 cudaError_t pattern_amp_sum(const float* amp, long long npx, int batch, double* part, int nblk, PatState* stt,
                             cudaStream_t st) {
   k_sum_real<<<dim3(nblk, batch), 256, 0, st>>>(amp, npx, part, nblk);
-  k_finalize_sum<<<batch, 32, 0, st>>>(part, nblk, stt, 0);
+  k_finalize_sum<<<batch, 32, 0, st>>>(part, nblk, stt, 0, 0.0, -1);
   return cudaGetLastError();
 }
 cudaError_t residual(const float2* psi, const float* inten, long long npx, int batch, double* part, int nblk,
                      PatState* stt, cudaStream_t st) {
   k_residual<<<dim3(nblk, batch), 256, 0, st>>>(psi, inten, npx, part, nblk);
-  k_finalize_sum<<<batch, 32, 0, st>>>(part, nblk, stt, 1);
+  k_finalize_sum<<<batch, 32, 0, st>>>(part, nblk, stt, 1, 0.0, -1);
   return cudaGetLastError();
 }
 cudaError_t rfactor(const float2* psi, const float* inten, long long npx, int batch, double* part, int nblk,
                     PatState* stt, cudaStream_t st) {
   k_rdiff<<<dim3(nblk, batch), 256, 0, st>>>(psi, inten, npx, part, nblk);
-  k_finalize_sum<<<batch, 32, 0, st>>>(part, nblk, stt, 2);
+  k_finalize_sum<<<batch, 32, 0, st>>>(part, nblk, stt, 2, 0.0, -1);
   return cudaGetLastError();
 }
-cudaError_t rfactor_from_partials(const double* part, int nblk, int batch, PatState* stt, cudaStream_t st) {
-  k_finalize_sum<<<batch, 32, 0, st>>>(part, nblk, stt, 2);
+cudaError_t rfactor_from_partials(const double* part, int nblk, int batch, PatState* stt, double stop, int iter,
+                                  cudaStream_t st) {
+  k_finalize_sum<<<batch, 32, 0, st>>>(part, nblk, stt, 2, stop, iter);
   return cudaGetLastError();
 }
 
 // Start of phaseRetrieve: avg and the flags are locals of the call (cdi.cc:315).
 __global__ void k_run_begin(PatState* stt, int batch) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p < batch) { stt[p].avg = 0.f; stt[p].flags = 0; }
+  if (p < batch) { stt[p].avg = 0.f; stt[p].flags = 0; stt[p].conv_iter = -1; }
 }
 cudaError_t run_begin(PatState* stt, int batch, cudaStream_t st) {
   k_run_begin<<<(batch + 127) / 128, 128, 0, st>>>(stt, batch);

@@ -21,6 +21,21 @@ enum : int { ROW_FFT = 0, ROW_ITER = 1 };
 enum : int { COL_FFT = 0, COL_ITER = 1 };
 enum : int { PROJ_MODABS = 0, PROJ_CCD = 1 };
 
+// Per-pattern device state of the shrinkwrap (the reference keeps it in host
+// locals of phaseRetrieve and in __constant__ vars.threshold).
+struct PatState {
+  float threshold;   // vars.threshold
+  float avg;         // avg of phaseRetrieve (0 until the first shrinkwrap)
+  float maxv;        // last max of the blurred support
+  float sum;         // last sum of the blurred support
+  double rfactor;    // last R-factor
+  double amp_sum;    // sum sqrt(I)
+  double residual;   // final residual
+  int flags;         // bit 0: NaN/zero max seen at a shrinkwrap; bit 1: R <= stop reached;
+                     // bit 2: frozen (set by the column pass after bit 1; both passes then skip)
+  int conv_iter;     // iterations run when the pattern froze (-1: never)
+};
+
 struct RowArgs {
   const float2* in;        // rows to load
   float2* out;             // rows to store (may alias in when the layouts match)
@@ -37,6 +52,7 @@ struct RowArgs {
   long long out_stride;
   long long rho_stride;
   long long mask_stride;   // mask words between patterns
+  const PatState* state;   // optional: CTAs of frozen patterns (flags bit 2) return at once
   float scale;             // factor applied on store (1 = none)
   float inv_n;             // 1/(rows*cols) (applyNorm after the inverse FFT)
   float beta;              // vars.beta_HIO
@@ -59,23 +75,10 @@ struct ColArgs {
   int noise_level;
   int in_tiled, out_tiled; // 0: row-major, 1: column-tiled with width L
   long long in_stride, out_stride, aux_stride, psi_stride;
+  PatState* state;         // optional: patterns with flags bit 1 freeze (bit 2), frozen ones return at once
   float scale;
   float ccd_scale;         // vars.scale
   float ccd_rcolor;        // vars.rcolor
-};
-
-// Per-pattern device state of the shrinkwrap (the reference keeps it in host
-// locals of phaseRetrieve and in __constant__ vars.threshold).
-struct PatState {
-  float threshold;   // vars.threshold
-  float avg;         // avg of phaseRetrieve (0 until the first shrinkwrap)
-  float maxv;        // last max of the blurred support
-  float sum;         // last sum of the blurred support
-  double rfactor;    // last R-factor
-  double amp_sum;    // sum sqrt(I)
-  double residual;   // final residual
-  int flags;         // bit 0: NaN/zero max seen at a shrinkwrap
-  int pad;
 };
 
 // Launch helpers exported by the per-size translation units.

@@ -36,6 +36,7 @@ class Params(ctypes.Structure):
         ("rcolor", ctypes.c_int), ("sim_ccd_bit", ctypes.c_int), ("noise_level", ctypes.c_int),
         ("shrink_mode", ctypes.c_int), ("sigma0", ctypes.c_float), ("sigma_min", ctypes.c_float),
         ("sigma_decay", ctypes.c_float), ("use_graph", ctypes.c_int), ("rf_every", ctypes.c_int),
+        ("stop_rfactor", ctypes.c_float),
     ]
 
 
@@ -44,6 +45,7 @@ class Stats(ctypes.Structure):
         ("steps", ctypes.c_int), ("iterations", ctypes.c_int), ("shrinkwraps", ctypes.c_int),
         ("residual", ctypes.c_double), ("rfactor", ctypes.c_double), ("threshold", ctypes.c_float),
         ("flags", ctypes.c_int), ("gpu_ms", ctypes.c_double), ("launches", ctypes.c_int),
+        ("converged_iter", ctypes.c_int),
     ]
 
     def as_dict(self):
@@ -69,6 +71,9 @@ _SIGS = {
     "cdx_run": [_P, ctypes.c_char_p, ctypes.POINTER(Stats)],
     "cdx_run_async": [_P, ctypes.c_char_p],
     "cdx_get_stats": [_P, _I, ctypes.POINTER(Stats)],
+    "cdx_group_create": [ctypes.POINTER(_P), _I, ctypes.POINTER(_P)],
+    "cdx_group_run": [_P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double)],
+    "cdx_group_destroy": [_P],
     "cdx_get_object": [_P, _I, _P, _I],
     "cdx_get_fourier": [_P, _I, _P, _I],
     "cdx_get_support": [_P, _I, _P, _I],
@@ -249,6 +254,32 @@ class Context:
         ptrs = [ctypes.c_void_p() for _ in range(4)]
         check(lib().cdx_device_arrays(self._h, *[ctypes.byref(p) for p in ptrs]))
         return [p.value for p in ptrs]
+
+
+class Group:
+    """Contexts of different pattern sizes run as one CUDA graph (cdx_group_*)."""
+
+    def __init__(self, contexts):
+        self.contexts = list(contexts)
+        arr = (ctypes.c_void_p * len(self.contexts))(*[c._h.value for c in self.contexts])
+        self._h = ctypes.c_void_p()
+        check(lib().cdx_group_create(arr, len(self.contexts), ctypes.byref(self._h)))
+
+    def run(self, algorithm: str) -> float:
+        ms = ctypes.c_double()
+        check(lib().cdx_group_run(self._h, algorithm.encode(), ctypes.byref(ms)))
+        return ms.value
+
+    def close(self):
+        if self._h:
+            lib().cdx_group_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def phase_retrieve_host(params: Params, algorithm: str, intensity, psi0=None, seed=0):

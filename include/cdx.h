@@ -64,6 +64,8 @@ typedef struct cdx_params {
   float sigma0, sigma_min, sigma_decay;  /* shrinkwrap width schedule (defaults 3, 2, 0.99) */
   int use_graph;             /* capture each cdx_run in a CUDA graph (default 1) */
   int rf_every;              /* compute the R-factor every k iterations inside the loop (0 = only at the end) */
+  float stop_rfactor;        /* with rf_every > 0: a pattern whose R-factor <= stop_rfactor finishes its
+                                iteration and then freezes (its kernels return at once); 0 = never */
 } cdx_params;
 
 typedef struct cdx_stats {
@@ -76,6 +78,7 @@ typedef struct cdx_stats {
   int flags;                 /* pattern 0: bit 0 = a shrinkwrap saw max ~ 0 or NaN (cdi.cc:334-337) */
   double gpu_ms;             /* device time of the run (CUDA events) */
   int launches;              /* kernels the run enqueued */
+  int converged_iter;        /* iterations run before the pattern froze at stop_rfactor (-1: never) */
 } cdx_stats;
 
 typedef struct cdx_ctx cdx_ctx;
@@ -121,6 +124,20 @@ int cdx_run(cdx_ctx* ctx, const char* algorithm, cdx_stats* stats);
 int cdx_run_async(cdx_ctx* ctx, const char* algorithm);
 /* Statistics of pattern idx after a run (synchronises). */
 int cdx_get_stats(cdx_ctx* ctx, int idx, cdx_stats* stats);
+
+/* ---------------------------------------------------------------- uneven batches */
+/* A group runs phaseRetrieve on several contexts (typically one per pattern
+ * size, each holding a batch of equal-size patterns) as ONE CUDA graph with a
+ * parallel branch per context, so patterns of uneven sizes share the GPU in a
+ * single launch.  No reference counterpart (the reference runs one pattern at
+ * a time).  The contexts must use distinct streams (created by cdx_create
+ * with stream NULL) and stay alive while the group exists. */
+typedef struct cdx_group cdx_group;
+int cdx_group_create(cdx_ctx* const* ctxs, int n, cdx_group** out);
+/* Runs `algorithm` on every context; synchronises; *gpu_ms gets the graph's
+ * device time (may be NULL).  Per-pattern results: cdx_get_stats / cdx_get_*. */
+int cdx_group_run(cdx_group* g, const char* algorithm, double* gpu_ms);
+int cdx_group_destroy(cdx_group* g);
 
 /* ---------------------------------------------------------------- outputs */
 int cdx_get_object(cdx_ctx* ctx, int idx, float* out, int where);   /* objectWave (complex) */

@@ -396,3 +396,74 @@ def test_large_pattern_iterates(cdx):
     e = rel_l2(got, ref.rho)
     print(f"2048^2 3*RAAR rel L2 vs FP64 oracle {e:.3e}")
     assert e <= 1e-5
+
+
+def test_group_of_uneven_sizes_equals_separate_runs(cdx):
+    """Contexts of three sizes run as one CUDA graph give the same bits as
+    separate runs."""
+    sizes = [(128, 2), (192, 1), (256, 3)]
+    alg = "6*HIO+1*shrinkWrap+4*RAAR+2*ER"
+    data = {n: [blob_case(n=n, seed=10 * n + i) for i in range(b)] for n, b in sizes}
+
+    def make(n, b):
+        ctx = cdx.Context(cdx.default_params(n, n, batch=b, oversampling_spt=3.0, shrink_threshold=0.1, beta=0.9))
+        for i, (I, psi0) in enumerate(data[n]):
+            ctx.set_pattern(i, I)
+            ctx.set_initial(i, psi0)
+        return ctx
+
+    ctxs = [make(n, b) for n, b in sizes]
+    g = cdx.Group(ctxs)
+    ms = g.run(alg)
+    assert ms > 0
+    grouped = {n: [ctx.get_object(i) for i in range(b)] for ctx, (n, b) in zip(ctxs, sizes)}
+    g.close()
+    for c in ctxs:
+        c.close()
+    # fresh contexts: a context keeps vars.threshold across restarts, as the
+    # reference does (initSupport rebuilds the rect, not the threshold)
+    for n, b in sizes:
+        ctx = make(n, b)
+        ctx.run(alg)
+        for i in range(b):
+            sep = ctx.get_object(i)
+            print(f"group vs separate, {n}x{n} pattern {i}: rel L2 {rel_l2(grouped[n][i], sep):.3e}")
+            assert np.array_equal(sep, grouped[n][i])
+        ctx.close()
+
+
+def test_patterns_freeze_at_stop_rfactor(cdx):
+    """rf_every/stop_rfactor: a pattern whose R-factor reaches the stop value
+    finishes that iteration and freezes; its state equals a plain run of the
+    same number of iterations, and other patterns keep iterating."""
+    n = 128
+    obj, sup = synth.blob_object(n, 4)
+    I = np.abs(np.fft.fft2(obj)) ** 2          # noise-free: R falls below 0.36 after ~20 HIO steps
+    I = (I / I.sum() * 1e8).astype(np.float32)
+    psi0 = synth.random_phase_start(I, 4)
+    I2, psi2 = blob_case(n=n, seed=5)           # 1e6 photons: R stays above 0.68 (float64 oracle)
+    alg = "300*HIO"
+    p = cdx.default_params(n, n, batch=2, oversampling_spt=2.0, rf_every=5, stop_rfactor=0.36)
+    with cdx.Context(p) as ctx:
+        ctx.set_pattern(0, I)
+        ctx.set_pattern(1, I2)
+        ctx.set_initial(0, psi0)
+        ctx.set_initial(1, psi2)
+        ctx.run(alg)
+        s0, s1 = ctx.stats(0), ctx.stats(1)
+        frozen = ctx.get_object(0)
+        other = ctx.get_object(1)
+    print("freeze stats", s0, s1)
+    assert 0 < s0["converged_iter"] < 300 and s1["converged_iter"] == -1
+    assert s0["converged_iter"] % 5 == 1   # checked after iteration 5j, frozen after 5j + 1
+    m = s0["converged_iter"]
+    p1 = cdx.default_params(n, n, oversampling_spt=2.0)
+    with cdx.Context(p1) as ctx:
+        ctx.set_pattern(0, I)
+        ctx.set_initial(0, psi0)
+        ctx.run(f"{m}*HIO")
+        assert np.array_equal(ctx.get_object(0), frozen)
+        ctx.set_pattern(0, I2)
+        ctx.set_initial(0, psi2)
+        ctx.run(alg)
+        assert np.array_equal(ctx.get_object(0), other)
