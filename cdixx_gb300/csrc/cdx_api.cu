@@ -217,6 +217,7 @@ int col_iter(cdx_ctx* c, bool from_psi, bool rf) {
   a.bs = c->bs_t;
   a.aux_stride = c->wstride;
   a.state = c->dstate;
+  a.tc = c->p.fft_mode == CDX_FFT_TC_BF16;
   a.rf_partials = rf ? c->part : nullptr;
   a.tw = c->tw_r;
   a.cols = c->cols;
@@ -243,6 +244,7 @@ int row_iter(cdx_ctx* c, int algo) {
   a.mask = c->mask;
   a.mask_stride = (long long)c->rows * c->wpr;
   a.state = c->dstate;
+  a.tc = c->p.fft_mode == CDX_FFT_TC_BF16;
   a.tw = c->tw_c;
   a.rows = c->rows;
   a.mode = ROW_ITER;
@@ -256,7 +258,7 @@ int row_iter(cdx_ctx* c, int algo) {
 
 // Generic 2-D transform of `batch` row-major patterns: rows then columns.
 int fft2_enqueue(const float2* in, float2* out, int rows, int cols, int batch, bool inv, float scale,
-                 const float2* tw_rows_len, const float2* tw_cols_len, cudaStream_t st) {
+                 const float2* tw_rows_len, const float2* tw_cols_len, cudaStream_t st, int tc = 0) {
   const long long n = (long long)rows * cols;
   RowArgs r{};
   r.in = in;
@@ -266,6 +268,7 @@ int fft2_enqueue(const float2* in, float2* out, int rows, int cols, int batch, b
   r.rows = rows;
   r.mode = ROW_FFT;
   r.inv = inv;
+  r.tc = tc;
   r.scale = 1.f;
   CDX_CK(row_launcher(cols)(r, batch, st));
   ColArgs c{};
@@ -276,6 +279,7 @@ int fft2_enqueue(const float2* in, float2* out, int rows, int cols, int batch, b
   c.cols = cols;
   c.mode = COL_FFT;
   c.inv = inv;
+  c.tc = tc;
   c.scale = scale;
   CDX_CK(col_launcher(rows)(c, batch, st));
   return CDX_OK;
@@ -328,6 +332,7 @@ int enqueue_run(cdx_ctx* c, const std::vector<int>& steps, const SwPlan& sw, boo
     a.cols = c->cols;
     a.mode = COL_FFT;
     a.inv = 0;
+    a.tc = c->p.fft_mode == CDX_FFT_TC_BF16;
     a.scale = 1.f;
     CDX_CK(col_launcher(c->rows)(a, c->batch, c->st));
     ++nl;
@@ -542,6 +547,7 @@ int cdx_create(const cdx_params* p, void* stream, cdx_ctx** out) {
   if (p->batch < 1 || p->batch > 65535) return set_error(CDX_ERR_ARG, "batch must be in [1, 65535]");
   if (!(p->exposure > 0)) return set_error(CDX_ERR_ARG, "exposure must be > 0");
   if (!(p->oversampling_spt > 0)) return set_error(CDX_ERR_ARG, "oversampling_spt must be > 0");
+  if (p->fft_mode != CDX_FFT_FP32 && p->fft_mode != CDX_FFT_TC_BF16) return set_error(CDX_ERR_ARG, "unknown fft_mode");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
     cudaGetLastError();
@@ -693,7 +699,8 @@ int cdx_set_beamstop(cdx_ctx* c, int idx, const float* bs, int where, int layout
 static int init_rho_from_psi(cdx_ctx* c, int idx, int count) {
   const long long off = (long long)idx * c->npx;
   const float f = (float)(1.0 / std::sqrt((double)c->rows * c->cols));
-  return fft2_enqueue(c->psi + off, c->rho + off, c->rows, c->cols, count, true, f, c->tw_r, c->tw_c, c->st);
+  return fft2_enqueue(c->psi + off, c->rho + off, c->rows, c->cols, count, true, f, c->tw_r, c->tw_c, c->st,
+                      c->p.fft_mode == CDX_FFT_TC_BF16);
 }
 
 int cdx_set_initial(cdx_ctx* c, int idx, const float* psi0, int where) {
@@ -833,7 +840,12 @@ done:
 
 // ---------------------------------------------------------------- primitives
 int cdx_fft2(const void* in, void* out, int rows, int cols, int batch, int inverse, void* stream) {
+  return cdx_fft2_ex(in, out, rows, cols, batch, inverse, CDX_FFT_FP32, stream);
+}
+
+int cdx_fft2_ex(const void* in, void* out, int rows, int cols, int batch, int inverse, int fft_mode, void* stream) {
   if (!in || !out || batch < 1) return set_error(CDX_ERR_ARG, "bad fft argument");
+  if (fft_mode != CDX_FFT_FP32 && fft_mode != CDX_FFT_TC_BF16) return set_error(CDX_ERR_ARG, "unknown fft_mode");
   int e = check_len(rows);
   if (e) return e;
   if ((e = check_len(cols))) return e;
@@ -842,7 +854,7 @@ int cdx_fft2(const void* in, void* out, int rows, int cols, int batch, int inver
   float2 *tr, *tc;
   if ((e = twiddles(rows, &tr)) || (e = twiddles(cols, &tc))) return e;
   return fft2_enqueue((const float2*)in, (float2*)out, rows, cols, batch, inverse != 0, 1.f, tr, tc,
-                      (cudaStream_t)stream);
+                      (cudaStream_t)stream, fft_mode == CDX_FFT_TC_BF16);
 }
 
 int cdx_apply_mod_abs(void* psi, const float* inten, long long n, void* stream) {

@@ -20,6 +20,7 @@
 // LD = N + N/16 + 1.  The skew keeps the strided stores of the first pass and
 // the column-tile loads free of bank conflicts for 64-bit accesses.
 #pragma once
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -255,19 +256,164 @@ __device__ __forceinline__ void fft_pass(float2* buf, const float2* tw) {
   __syncthreads();
 }
 
+// ------------------------------------------------------- tensor-core radix 16
+// The DFT-16 of eight butterflies at once as warp MMAs (mma.sync m16n8k16,
+// BF16 operands, FP32 accumulation).  In real form
+//     [Yr; Yi] = [[Fr, -Fi], [Fi, Fr]] [Xr; Xi],   F[m][r] = exp(-+2 pi i m r/16),
+// i.e. two 16-row tiles (Yr, Yi) times two 16-deep K steps (Xr, Xi), each an
+// m16n8k16 MMA with the 8 butterflies as the N dimension.  Every operand is
+// split into a BF16 head and a BF16 tail (x = hi + lo + O(2^-16 x)); the
+// three products hi*hi + hi*lo + lo*hi are accumulated in FP32 (the lo*lo term,
+// O(2^-16), is dropped), 12 MMAs per 8 butterflies.  Relative error of a pass
+// ~1e-5: a lower-precision path, reported against the float64 oracle.
+//
+// Fragment layouts of mma.m16n8k16 (PTX ISA): with g = lane/4, q = lane%4,
+//   A (16x16, row): {a0,a1} = A[g][2q..2q+1], {a2,a3} = A[g+8][2q..], {a4,a5} = A[g][2q+8..], {a6,a7} = A[g+8][2q+8..]
+//   B (16x8, col):  {b0,b1} = B[2q..2q+1][g], {b2,b3} = B[2q+8..2q+9][g]
+//   C (16x8):       {c0,c1} = C[g][2q..2q+1], {c2,c3} = C[g+8][2q..2q+1]
+struct BF2 {
+  uint32_t hi, lo;
+};
+__device__ __forceinline__ BF2 split_bf16x2(float a, float b) {
+  __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  const float2 hf = __bfloat1622float2(h);
+  __nv_bfloat162 l = __floats2bfloat162_rn(a - hf.x, b - hf.y);
+  BF2 r;
+  r.hi = *reinterpret_cast<uint32_t*>(&h);
+  r.lo = *reinterpret_cast<uint32_t*>(&l);
+  return r;
+}
+__device__ __forceinline__ void mma_bf16(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                         uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+// A fragments of Fr, Fi (head and tail) for this lane; sgn = -1 forward, +1 inverse.
+struct DftFrag {
+  uint32_t fr_hi[4], fr_lo[4], fi_hi[4], fi_lo[4], nfi_hi[4], nfi_lo[4];
+};
+template <bool INV>
+__device__ __forceinline__ void dft16_fragments(DftFrag& f) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
+  const float sgn = INV ? 1.f : -1.f;
+  // register i of the fragment holds rows (g, g+8) x cols (2q, 2q+1) / (2q+8, 2q+9)
+  const int rows[4] = {g, g + 8, g, g + 8};
+  const int cols[4] = {2 * q, 2 * q, 2 * q + 8, 2 * q + 8};
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    float cr[2], ci[2];
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      float s, c;
+      sincospif((float)((rows[i] * (cols[i] + e)) & 15) / 8.f, &s, &c);   // angle 2 pi m r / 16
+      cr[e] = c;
+      ci[e] = sgn * s;
+    }
+    BF2 r = split_bf16x2(cr[0], cr[1]);
+    BF2 m = split_bf16x2(ci[0], ci[1]);
+    BF2 n = split_bf16x2(-ci[0], -ci[1]);
+    f.fr_hi[i] = r.hi; f.fr_lo[i] = r.lo;
+    f.fi_hi[i] = m.hi; f.fi_lo[i] = m.lo;
+    f.nfi_hi[i] = n.hi; f.nfi_lo[i] = n.lo;
+  }
+}
+
+// D += A * X with A, X split into head and tail (three products).
+__device__ __forceinline__ void mma3(float (&d)[4], const uint32_t (&ah)[4], const uint32_t (&al)[4],
+                                     uint32_t bh0, uint32_t bh1, uint32_t bl0, uint32_t bl1) {
+  mma_bf16(d, ah[0], ah[1], ah[2], ah[3], bh0, bh1);
+  mma_bf16(d, ah[0], ah[1], ah[2], ah[3], bl0, bl1);
+  mma_bf16(d, al[0], al[1], al[2], al[3], bh0, bh1);
+}
+
+// One radix-16 Stockham pass (same index map as fft_pass) with the DFTs on the
+// tensor cores.  Butterflies are taken 8 at a time per warp.
 template <int N, int P, bool INV>
-__device__ __forceinline__ void fft_passes(float2* buf, const float2* tw) {
+__device__ __forceinline__ void fft_pass_tc16(float2* buf, const float2* tw, const DftFrag& F) {
+  using G = Geom<N>;
+  constexpr int L = G::L, T = G::T;
+  constexpr int R = 16;
+  static_assert(plan_radix(N, P) == 16, "tensor-core pass is radix 16");
+  constexpr int NS = plan_ns(N, P);
+  constexpr int NR = N / R;
+  constexpr int NB = L * NR;
+  static_assert(NB % 8 == 0, "butterflies come in groups of 8");
+  constexpr int CHUNKS = NB / 8;
+  constexpr int WARPS = T / 32;
+  constexpr int CPW = (CHUNKS + WARPS - 1) / WARPS;   // chunks per warp
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, g = lane >> 2, q = lane & 3;
+  // this lane loads components r = 2q, 2q+1, 2q+8, 2q+9 of butterfly g of each chunk
+  float2 x[CPW][4];
+#pragma unroll
+  for (int c = 0; c < CPW; ++c) {
+    const int ch = warp + c * WARPS;
+    if (CHUNKS % WARPS == 0 || ch < CHUNKS) {
+      const int bfly = ch * 8 + g;
+      const int l = bfly / NR, j = bfly - l * NR;
+      const int k = j % NS;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int r = 2 * q + (e & 1) + ((e >> 1) << 3);
+        float2 v = buf[G::idx(l, j + r * NR)];
+        if constexpr (NS > 1) {
+          if (r > 0) {
+            float2 w = __ldg(tw + tw_offset(N, P) + (r - 1) * NS + k);
+            if (INV) w.y = -w.y;
+            v = cmul(v, w);
+          }
+        }
+        x[c][e] = v;
+      }
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int c = 0; c < CPW; ++c) {
+    const int ch = warp + c * WARPS;
+    if (CHUNKS % WARPS == 0 || ch < CHUNKS) {
+      // B fragments: Xr rows (2q, 2q+1 | 2q+8, 2q+9) of column g, and Xi
+      const BF2 xr01 = split_bf16x2(x[c][0].x, x[c][1].x), xr89 = split_bf16x2(x[c][2].x, x[c][3].x);
+      const BF2 xi01 = split_bf16x2(x[c][0].y, x[c][1].y), xi89 = split_bf16x2(x[c][2].y, x[c][3].y);
+      float yr[4] = {0.f, 0.f, 0.f, 0.f}, yi[4] = {0.f, 0.f, 0.f, 0.f};
+      mma3(yr, F.fr_hi, F.fr_lo, xr01.hi, xr89.hi, xr01.lo, xr89.lo);     // Yr += Fr Xr
+      mma3(yr, F.nfi_hi, F.nfi_lo, xi01.hi, xi89.hi, xi01.lo, xi89.lo);   // Yr -= Fi Xi
+      mma3(yi, F.fi_hi, F.fi_lo, xr01.hi, xr89.hi, xr01.lo, xr89.lo);     // Yi += Fi Xr
+      mma3(yi, F.fr_hi, F.fr_lo, xi01.hi, xi89.hi, xi01.lo, xi89.lo);     // Yi += Fr Xi
+      // this lane holds Y[m][n] for m in {g, g+8}, butterflies n in {2q, 2q+1}
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int m = g + ((e >> 1) << 3), n = 2 * q + (e & 1);
+        const int bfly = ch * 8 + n;
+        const int l = bfly / NR, j = bfly - l * NR;
+        const int k = j % NS;
+        buf[G::idx(l, (j - k) * R + k + m * NS)] = make_float2(yr[e], yi[e]);
+      }
+    }
+  }
+  __syncthreads();
+}
+
+template <int N, int P, bool INV, bool TC>
+__device__ __forceinline__ void fft_passes(float2* buf, const float2* tw, const DftFrag& F) {
   if constexpr (plan_radix(N, P) != 0) {
-    fft_pass<N, P, INV>(buf, tw);
-    fft_passes<N, P + 1, INV>(buf, tw);
+    if constexpr (TC && plan_radix(N, P) == 16 && (Geom<N>::L * (N / 16)) % 8 == 0) fft_pass_tc16<N, P, INV>(buf, tw, F);
+    else fft_pass<N, P, INV>(buf, tw);
+    fft_passes<N, P + 1, INV, TC>(buf, tw, F);
   }
 }
 
 // Transform all L lines in place.  Callers synchronise before the call (the
-// lines must be fully written); the call ends with a barrier.
-template <int N, bool INV>
+// lines must be fully written); the call ends with a barrier.  TC selects the
+// tensor-core radix-16 passes.
+template <int N, bool INV, bool TC = false>
 __device__ __forceinline__ void fft_lines(float2* buf, const float2* tw) {
-  fft_passes<N, 0, INV>(buf, tw);
+  DftFrag F;
+  if constexpr (TC) dft16_fragments<INV>(F);
+  fft_passes<N, 0, INV, TC>(buf, tw, F);
 }
 
 }  // namespace cdx

@@ -157,8 +157,8 @@ __device__ __forceinline__ void row_elem(int e, int tiled, int tl, int& l, int& 
 
 // ------------------------------------------------------------------ row pass
 // Lines are rows of length N (= number of columns).  Grid: (ceil(rows/L), batch).
-template <int N, int MODE>
-__global__ void __launch_bounds__(Geom<N>::T, Geom<N>::MINB) row_pass_kernel(RowArgs a) {
+template <int N, int MODE, bool TC>
+__global__ void __launch_bounds__(Geom<N>::T, (TC && Geom<N>::MINB > 2) ? 2 : Geom<N>::MINB) row_pass_kernel(RowArgs a) {
   using G = Geom<N>;
   constexpr int L = G::L, T = G::T;
   extern __shared__ float2 smem[];
@@ -206,10 +206,10 @@ __global__ void __launch_bounds__(Geom<N>::T, Geom<N>::MINB) row_pass_kernel(Row
   __syncthreads();
 
   if constexpr (!iter) {
-    if (a.inv) fft_lines<N, true>(buf, tw);
-    else fft_lines<N, false>(buf, tw);
+    if (a.inv) fft_lines<N, true, TC>(buf, tw);
+    else fft_lines<N, false, TC>(buf, tw);
   } else {
-    fft_lines<N, true>(buf, tw);
+    fft_lines<N, true, TC>(buf, tw);
     cp_wait<0>();
     __syncthreads();
     // rho' = IFFT/N, update against rho and the support bits
@@ -228,7 +228,7 @@ __global__ void __launch_bounds__(Geom<N>::T, Geom<N>::MINB) row_pass_kernel(Row
       buf[G::idx(l, c)] = r;
     }
     __syncthreads();
-    fft_lines<N, false>(buf, tw);
+    fft_lines<N, false, TC>(buf, tw);
   }
   // store rows
   const float s = a.scale;
@@ -249,8 +249,8 @@ __global__ void __launch_bounds__(Geom<N>::T, Geom<N>::MINB) row_pass_kernel(Row
 // Lines are columns of length N (= number of rows).  Grid: (ceil(cols/L), batch).
 // Column-tiled arrays here have tile width L, so the CTA's tile is the
 // contiguous block [blockIdx.x * N * L, +N*L) with element t = r*L + l.
-template <int N, int MODE>
-__global__ void __launch_bounds__(Geom<N>::T, Geom<N>::MINB) col_pass_kernel(ColArgs a) {
+template <int N, int MODE, bool TC>
+__global__ void __launch_bounds__(Geom<N>::T, (TC && Geom<N>::MINB > 2) ? 2 : Geom<N>::MINB) col_pass_kernel(ColArgs a) {
   using G = Geom<N>;
   constexpr int L = G::L, T = G::T, LL = G::LOG2L;
   extern __shared__ float2 smem[];
@@ -315,10 +315,10 @@ __global__ void __launch_bounds__(Geom<N>::T, Geom<N>::MINB) col_pass_kernel(Col
   __syncthreads();
 
   if constexpr (!iter) {
-    if (a.inv) fft_lines<N, true>(buf, tw);
-    else fft_lines<N, false>(buf, tw);
+    if (a.inv) fft_lines<N, true, TC>(buf, tw);
+    else fft_lines<N, false, TC>(buf, tw);
   } else {
-    if (!a.from_psi) fft_lines<N, false>(buf, tw);
+    if (!a.from_psi) fft_lines<N, false, TC>(buf, tw);
     cp_wait<0>();
     __syncthreads();
     // Psi is complete here: optional copy-out, R-factor partial, projection
@@ -341,7 +341,7 @@ __global__ void __launch_bounds__(Geom<N>::T, Geom<N>::MINB) col_pass_kernel(Col
       if (threadIdx.x == 0) a.rf_partials[(long long)blockIdx.y * gridDim.x + blockIdx.x] = tsum;
     }
     __syncthreads();
-    fft_lines<N, true>(buf, tw);
+    fft_lines<N, true, TC>(buf, tw);
   }
   const float s = a.scale;
   float2* out = a.out + (long long)blockIdx.y * a.out_stride;

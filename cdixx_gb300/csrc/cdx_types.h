@@ -53,6 +53,7 @@ struct RowArgs {
   long long rho_stride;
   long long mask_stride;   // mask words between patterns
   const PatState* state;   // optional: CTAs of frozen patterns (flags bit 2) return at once
+  int tc;                  // 1: radix-16 passes on the tensor cores (BF16 split, FP32 accumulate)
   float scale;             // factor applied on store (1 = none)
   float inv_n;             // 1/(rows*cols) (applyNorm after the inverse FFT)
   float beta;              // vars.beta_HIO
@@ -76,6 +77,7 @@ struct ColArgs {
   int in_tiled, out_tiled; // 0: row-major, 1: column-tiled with width L
   long long in_stride, out_stride, aux_stride, psi_stride;
   PatState* state;         // optional: patterns with flags bit 1 freeze (bit 2), frozen ones return at once
+  int tc;                  // 1: radix-16 passes on the tensor cores (BF16 split, FP32 accumulate)
   float scale;
   float ccd_scale;         // vars.scale
   float ccd_rcolor;        // vars.rcolor

@@ -20,6 +20,7 @@ CDX_HOST, CDX_DEVICE = 0, 1
 CDX_FFT_ORDER, CDX_CENTERED = 0, 1
 RAAR, ER, POSER, HIO, POSHIO, FHIO, SHRINKWRAP, XCORRELATION, KKT, TV = range(10)
 SHRINK_FOURIER, SHRINK_SPATIAL = 0, 1
+FFT_FP32, FFT_TC_BF16 = 0, 1
 
 
 class CdxError(RuntimeError):
@@ -36,7 +37,7 @@ class Params(ctypes.Structure):
         ("rcolor", ctypes.c_int), ("sim_ccd_bit", ctypes.c_int), ("noise_level", ctypes.c_int),
         ("shrink_mode", ctypes.c_int), ("sigma0", ctypes.c_float), ("sigma_min", ctypes.c_float),
         ("sigma_decay", ctypes.c_float), ("use_graph", ctypes.c_int), ("rf_every", ctypes.c_int),
-        ("stop_rfactor", ctypes.c_float),
+        ("stop_rfactor", ctypes.c_float), ("fft_mode", ctypes.c_int),
     ]
 
 
@@ -80,6 +81,7 @@ _SIGS = {
     "cdx_phase_retrieve_host": [ctypes.POINTER(Params), ctypes.c_char_p, _P, _P, ctypes.c_ulonglong,
                                 _P, _P, _P, ctypes.POINTER(Stats)],
     "cdx_fft2": [_P, _P, _I, _I, _I, _I, _P],
+    "cdx_fft2_ex": [_P, _P, _I, _I, _I, _I, _I, _P],
     "cdx_apply_mod_abs": [_P, _P, _LL, _P],
     "cdx_apply_mod": [_P, _P, _P, _I, _F, _I, _LL, _P],
     "cdx_apply_support": [_P, _P, _P, _F, _F, _I, _LL, _P],
@@ -303,12 +305,16 @@ def _stream_ptr(stream):
     return ctypes.c_void_p(stream)
 
 
-def fft2(x, out, inverse=False, stream=None):
-    """myFFT / myIFFT on device tensors (complex64, shape [..., rows, cols])."""
+def fft2(x, out, inverse=False, stream=None, fft_mode=0):
+    """myFFT / myIFFT on device tensors (complex64, shape [..., rows, cols]).
+
+    fft_mode 0 (FFT_FP32) is the FP32 SIMT path; 1 (FFT_TC_BF16) runs the
+    radix-16 passes on the tensor cores with a split-BF16 operand.
+    """
     rows, cols = x.shape[-2], x.shape[-1]
     batch = int(np.prod(x.shape[:-2])) if x.dim() > 2 else 1
-    check(lib().cdx_fft2(ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(out.data_ptr()), rows, cols, batch,
-                         int(inverse), _stream_ptr(stream)))
+    check(lib().cdx_fft2_ex(ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(out.data_ptr()), rows, cols, batch,
+                            int(inverse), int(fft_mode), _stream_ptr(stream)))
     return out
 
 

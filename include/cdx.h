@@ -66,7 +66,13 @@ typedef struct cdx_params {
   int rf_every;              /* compute the R-factor every k iterations inside the loop (0 = only at the end) */
   float stop_rfactor;        /* with rf_every > 0: a pattern whose R-factor <= stop_rfactor finishes its
                                 iteration and then freezes (its kernels return at once); 0 = never */
+  int fft_mode;              /* CDX_FFT_FP32 (default) or CDX_FFT_TC_BF16 */
 } cdx_params;
+
+/* FFT arithmetic.  CDX_FFT_TC_BF16: the radix-16 passes run as tensor-core
+ * MMAs with BF16 head/tail operands and FP32 accumulation (relative error per
+ * 2-D transform ~1e-5 instead of ~1.5e-7); no reference counterpart. */
+enum { CDX_FFT_FP32 = 0, CDX_FFT_TC_BF16 = 1 };
 
 typedef struct cdx_stats {
   int steps;                 /* algorithm steps executed (iterations + shrinkwraps) */
@@ -156,6 +162,8 @@ int cdx_phase_retrieve_host(const cdx_params* p, const char* algorithm, const fl
 /* myFFT / myIFFT (cudaConfig.cu:175-180): unnormalised 2-D C2C transform of
  * `batch` patterns, in place allowed.  inverse != 0 uses exp(+2 pi i). */
 int cdx_fft2(const void* in, void* out, int rows, int cols, int batch, int inverse, void* stream);
+/* cdx_fft2 with the FFT arithmetic chosen by fft_mode (CDX_FFT_*). */
+int cdx_fft2_ex(const void* in, void* out, int rows, int cols, int batch, int inverse, int fft_mode, void* stream);
 /* applyModAbs(source, target) with state NULL (cudaConfig.cu:827-841). */
 int cdx_apply_mod_abs(void* psi, const float* intensity, long long n, void* stream);
 /* applyMod(source, target, bs, noiseLevel) (cdi.cu:438-485); scale = vars.scale. */
