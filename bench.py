@@ -229,10 +229,13 @@ def run_gpu(args):
     t_iter = float(np.median(it_ms)) / 1000.0
     peak, peak_kind = peaks()
     achieved = ALG_BYTES_PER_PX_ITER * N * N / t_iter / 1e9
+    # DRAM bytes per iteration (col + row pass) from the committed ncu summary
     traffic = None
-    tf = ROOT / "profiles" / "traffic_2048.json"
+    tf = ROOT / "profiles" / "pass_kernels_2048.md"
     if tf.exists():
-        traffic = json.loads(tf.read_text()).get("dram_bytes_per_iteration")
+        for ln in tf.read_text().splitlines():
+            if ln.startswith("traffic_bytes_per_iteration:"):
+                traffic = int(ln.split(":", 1)[1])
 
     # e2e: the whole job through the host-buffer C-ABI call
     e2e_vals = []
