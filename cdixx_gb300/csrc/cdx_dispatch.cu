@@ -37,19 +37,21 @@ int twiddle_count(int n) {
 }
 
 // Entry (r-1)*NS + k of pass p's block = W_n^(r*k*n/(NS*R)), W_n = exp(-2 pi i/n),
-// evaluated in double with the exponent reduced mod n and rounded once to float.
+// evaluated in double with the exponent reduced mod n and rounded once to float;
+// both radix plans of the length.
 void twiddle_table(int n, float2* out) {
   const double two_pi = 6.283185307179586476925286766559;
-  for (int p = 1; plan_radix(n, p) != 0; ++p) {
-    const int R = plan_radix(n, p), NS = plan_ns(n, p), step = n / (NS * R);
-    float2* blk = out + tw_offset(n, p);
-    for (int r = 1; r < R; ++r)
-      for (int k = 0; k < NS; ++k) {
-        const long long t = ((long long)r * k * step) % n;
-        const double a = two_pi * (double)t / (double)n;
-        blk[(r - 1) * NS + k] = make_float2((float)std::cos(a), (float)-std::sin(a));
-      }
-  }
+  for (int plan = 0; plan < 2; ++plan)
+    for (int p = 1; plan_radix_x(n, plan, p) != 0; ++p) {
+      const int R = plan_radix_x(n, plan, p), NS = plan_ns_x(n, plan, p), step = n / (NS * R);
+      float2* blk = out + tw_offset_x(n, plan, p);
+      for (int r = 1; r < R; ++r)
+        for (int k = 0; k < NS; ++k) {
+          const long long t = ((long long)r * k * step) % n;
+          const double a = two_pi * (double)t / (double)n;
+          blk[(r - 1) * NS + k] = make_float2((float)std::cos(a), (float)-std::sin(a));
+        }
+    }
 }
 
 }  // namespace cdx

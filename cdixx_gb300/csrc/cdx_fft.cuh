@@ -162,19 +162,40 @@ __host__ __device__ constexpr bool size_supported(int n) {
   while (m % 3 == 0) m /= 3;
   return m == 1;
 }
+__host__ __device__ constexpr int plan_len(int n) {
+  int q = 0;
+  while (plan_radix(n, q) != 0) ++q;
+  return q;
+}
+// Two schedules per length: plan 0 is the order above, plan 1 the same radices
+// reversed.  A transform with plan 0 ends with the radix plan 1 starts with,
+// and its last pass leaves a thread's values exactly where plan 1's first pass
+// reads them, so two transforms chained through an element-wise step hand the
+// data over in registers.
+__host__ __device__ constexpr int plan_radix_x(int n, int plan, int p) {
+  return plan == 0 ? plan_radix(n, p) : (p < plan_len(n) ? plan_radix(n, plan_len(n) - 1 - p) : 0);
+}
+__host__ __device__ constexpr int plan_ns_x(int n, int plan, int p) {
+  int ns = 1;
+  for (int i = 0; i < p; ++i) ns *= plan_radix_x(n, plan, i);
+  return ns;
+}
 // Twiddles of pass p live in a block of (R-1)*NS entries, entry (r-1)*NS + k
 // = W_N^(r*k*N/(NS*R)) for r = 1..R-1, k < NS, so the threads of a warp (k
 // consecutive, r fixed) read consecutive words.  Pass 0 (NS = 1) needs none.
-__host__ __device__ constexpr int tw_offset(int n, int p) {
+// The table of a length holds plan 0's blocks, then plan 1's.
+__host__ __device__ constexpr int tw_plan_count(int n, int plan) {
   int off = 0;
-  for (int q = 1; q < p; ++q) off += (plan_radix(n, q) - 1) * plan_ns(n, q);
+  for (int q = 1; q < plan_len(n); ++q) off += (plan_radix_x(n, plan, q) - 1) * plan_ns_x(n, plan, q);
   return off;
 }
-__host__ __device__ constexpr int tw_count(int n) {
-  int q = 0;
-  while (plan_radix(n, q) != 0) ++q;
-  return tw_offset(n, q);
+__host__ __device__ constexpr int tw_offset_x(int n, int plan, int p) {
+  int off = plan == 0 ? 0 : tw_plan_count(n, 0);
+  for (int q = 1; q < p; ++q) off += (plan_radix_x(n, plan, q) - 1) * plan_ns_x(n, plan, q);
+  return off;
 }
+__host__ __device__ constexpr int tw_offset(int n, int p) { return tw_offset_x(n, 0, p); }
+__host__ __device__ constexpr int tw_count(int n) { return tw_plan_count(n, 0) + tw_plan_count(n, 1); }
 
 __host__ __device__ constexpr int pow2_floor(int x) {
   int p = 1;

@@ -70,16 +70,16 @@ int scratch_address(void** out) {
 __global__ void k_fill_twiddles(float2* out, int n, int count) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= count) return;
+  const int plan = i < tw_plan_count(n, 0) ? 0 : 1;
   int p = 1;
-  while (plan_radix(n, p + 1) != 0 && tw_offset(n, p + 1) <= i) ++p;
-  const int R = plan_radix(n, p), NS = plan_ns(n, p), step = n / (NS * R);
-  const int j = i - tw_offset(n, p);
+  while (plan_radix_x(n, plan, p + 1) != 0 && tw_offset_x(n, plan, p + 1) <= i) ++p;
+  const int R = plan_radix_x(n, plan, p), NS = plan_ns_x(n, plan, p), step = n / (NS * R);
+  const int j = i - tw_offset_x(n, plan, p);
   const int r = j / NS + 1, k = j - (r - 1) * NS;
   const long long t = ((long long)r * k * step) % n;
   double s, c;
   sincospi(2.0 * (double)t / (double)n, &s, &c);
   out[i] = make_float2((float)c, (float)-s);
-  (void)R;
 }
 
 inline size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }

@@ -1,0 +1,489 @@
+// Register-handoff Stockham engine and the FP32 iteration kernels built on it.
+//
+// Same transform and pass formula as fft_pass (cdx_fft.cuh), organised so
+// that data enter and leave a CTA in registers:
+//   * pass 0 loads its butterflies straight from global memory (no staging),
+//   * the middle passes exchange through the skewed shared-memory lines,
+//   * the last pass leaves its outputs in registers.
+// A thread's last-pass outputs of plan 0 are element j + r*NS of line l for
+// its butterflies (l, j); the first pass of plan 1 (the radices reversed)
+// reads exactly those elements.  So the column pass runs
+//     FFT (plan 0) -> projection in registers -> IFFT (plan 1) -> store,
+// and the row pass
+//     IFFT (plan 0) -> 1/N and update in registers -> FFT (plan 1) -> store,
+// with two shared-memory exchanges per 2048-point transform and no staging of
+// the lines in or out.
+//
+// Butterfly g of a pass (g = threadIdx.x + b*T) belongs to line
+// l = (g >> cb) & (L-1) and index j = (g >> (cb + log2 L)) << cb | (g & (2^cb - 1)):
+// with cb = 0 consecutive threads take consecutive lines (a column tile of
+// width L is then read as one contiguous run); the row pass uses cb = log2 of
+// the column tile width on tiled data, so 2^cb x L threads cover one piece of
+// a tile, and the largest valid cb on row-major data.
+// The map is the same for every pass of a kernel, which is what makes the
+// register handoff valid.
+#pragma once
+#include "cdx_kernels.cuh"
+
+namespace cdx {
+
+template <int N, int PLAN, int P>
+struct RPass {
+  using G = Geom<N>;
+  static constexpr int R = plan_radix_x(N, PLAN, P);
+  static constexpr int NS = plan_ns_x(N, PLAN, P);
+  static constexpr int NR = N / R;
+  static constexpr int NB = G::L * NR;
+  static constexpr int B = (NB + G::T - 1) / G::T;
+  static constexpr int TWO = tw_offset_x(N, PLAN, P);
+};
+
+// largest chunk bits valid for every pass: NR is a multiple of 2^cb
+template <int N>
+__host__ __device__ constexpr int rfft_cb_max() {
+  if ((N & (N - 1)) != 0) return 0;
+  int rmax = 1;
+  for (int p = 0; plan_radix(N, p) != 0; ++p) rmax = plan_radix(N, p) > rmax ? plan_radix(N, p) : rmax;
+  int nr = N / rmax, c = 0;
+  while ((2 << c) <= nr) ++c;
+  return c;
+}
+
+// (l, j) of butterfly b of this thread in a radix-R pass; false past the end
+template <int N, int R>
+__device__ __forceinline__ bool bfly_of(int b, int cb, int& l, int& j) {
+  using G = Geom<N>;
+  constexpr int NB = G::L * (N / R);
+  const int g = threadIdx.x + b * G::T;
+  if ((NB % G::T) != 0 && g >= NB) return false;
+  l = (g >> cb) & (G::L - 1);
+  j = ((g >> (cb + G::LOG2L)) << cb) | (g & ((1 << cb) - 1));
+  return true;
+}
+
+// shared-memory word of element j + r*NR of line l (linear in r when NR % 16 == 0)
+template <int N, int NR>
+__device__ __forceinline__ int sidx_in(int l, int j, int r) {
+  using G = Geom<N>;
+  if constexpr (NR % 16 == 0) return G::idx(l, j) + r * (NR + NR / 16);
+  else return G::idx(l, j + r * NR);
+}
+// shared-memory word of element base + r*NS of line l
+template <int N, int R, int NS>
+__device__ __forceinline__ int sidx_out(int l, int base, int r) {
+  using G = Geom<N>;
+  if constexpr (NS % 16 == 0) return G::idx(l, base) + r * (NS + NS / 16);
+  else if constexpr (NS == 1 && R == 16) return G::idx(l, base) + r;   // base = 16 j
+  else return G::idx(l, base + r * NS);
+}
+
+// twiddles and the radix-R DFT of one butterfly of pass P
+template <int N, int PLAN, int P, bool INV>
+__device__ __forceinline__ void rpass_compute(float2 (&v)[RPass<N, PLAN, P>::R], int j, const float2* tw) {
+  using S = RPass<N, PLAN, P>;
+  if constexpr (S::NS > 1) {
+    const int k = j % S::NS;
+#pragma unroll
+    for (int r = 1; r < S::R; ++r) {
+      float2 w = __ldg(tw + S::TWO + (r - 1) * S::NS + k);
+      if (INV) w.y = -w.y;
+      v[r] = cmul(v[r], w);
+    }
+  }
+  dftR<S::R, INV>(v);
+}
+
+template <int N, int PLAN, int P>
+__device__ __forceinline__ void rpass_store(float2* buf, float2 (&v)[RPass<N, PLAN, P>::B][RPass<N, PLAN, P>::R],
+                                            int cb) {
+  using S = RPass<N, PLAN, P>;
+#pragma unroll
+  for (int b = 0; b < S::B; ++b) {
+    int l, j;
+    if (!bfly_of<N, S::R>(b, cb, l, j)) continue;
+    const int k = j % S::NS;
+    const int base = (j - k) * S::R + k;
+#pragma unroll
+    for (int r = 0; r < S::R; ++r) buf[sidx_out<N, S::R, S::NS>(l, base, r)] = v[b][r];
+  }
+}
+
+template <int N, int PLAN, int P>
+__device__ __forceinline__ void rpass_load(const float2* buf, float2 (&v)[RPass<N, PLAN, P>::B][RPass<N, PLAN, P>::R],
+                                           int cb) {
+  using S = RPass<N, PLAN, P>;
+#pragma unroll
+  for (int b = 0; b < S::B; ++b) {
+    int l, j;
+    if (!bfly_of<N, S::R>(b, cb, l, j)) continue;
+#pragma unroll
+    for (int r = 0; r < S::R; ++r) v[b][r] = buf[sidx_in<N, S::NR>(l, j, r)];
+  }
+}
+
+template <int N, int PLAN, int P, bool INV>
+__device__ __forceinline__ void rpass_compute_all(float2 (&v)[RPass<N, PLAN, P>::B][RPass<N, PLAN, P>::R], int cb,
+                                                  const float2* tw) {
+  using S = RPass<N, PLAN, P>;
+#pragma unroll
+  for (int b = 0; b < S::B; ++b) {
+    int l, j;
+    if (!bfly_of<N, S::R>(b, cb, l, j)) continue;
+    rpass_compute<N, PLAN, P, INV>(v[b], j, tw);
+  }
+}
+
+// middle passes P .. M-2 through shared memory (each ends with a barrier)
+template <int N, int PLAN, int P, bool INV>
+__device__ __forceinline__ void rfft_middle(float2* buf, const float2* tw, int cb) {
+  if constexpr (P < plan_len(N) - 1) {
+    using S = RPass<N, PLAN, P>;
+    float2 v[S::B][S::R];
+    rpass_load<N, PLAN, P>(buf, v, cb);
+    __syncthreads();
+    rpass_compute_all<N, PLAN, P, INV>(v, cb, tw);
+    rpass_store<N, PLAN, P>(buf, v, cb);
+    __syncthreads();
+    rfft_middle<N, PLAN, P + 1, INV>(buf, tw, cb);
+  }
+}
+
+template <int N, int PLAN>
+using RFirst = RPass<N, PLAN, 0>;
+template <int N, int PLAN>
+using RLast = RPass<N, PLAN, plan_len(N) - 1>;
+
+// The whole transform of the CTA's L lines: `in` holds pass 0's inputs
+// (element j + r*N/R0 of line l for butterfly (l, j)), `out` receives the
+// last pass's outputs (element j + r*NS_last).  The shared lines must be free
+// on entry (callers synchronise); on return other threads may still be
+// reading them, so callers synchronise before the next write.
+template <int N, int PLAN, bool INV>
+__device__ __forceinline__ void rfft(float2 (&in)[RFirst<N, PLAN>::B][RFirst<N, PLAN>::R],
+                                     float2 (&out)[RLast<N, PLAN>::B][RLast<N, PLAN>::R], float2* buf,
+                                     const float2* tw, int cb) {
+  constexpr int M = plan_len(N);
+  rpass_compute_all<N, PLAN, 0, INV>(in, cb, tw);
+  if constexpr (M == 1) {
+#pragma unroll
+    for (int b = 0; b < RFirst<N, PLAN>::B; ++b)
+#pragma unroll
+      for (int r = 0; r < RFirst<N, PLAN>::R; ++r) out[b][r] = in[b][r];
+  } else {
+    rpass_store<N, PLAN, 0>(buf, in, cb);
+    __syncthreads();
+    rfft_middle<N, PLAN, 1, INV>(buf, tw, cb);
+    rpass_load<N, PLAN, M - 1>(buf, out, cb);
+    rpass_compute_all<N, PLAN, M - 1, INV>(out, cb, tw);
+  }
+}
+
+// Shared memory and resident CTAs per SM (register budget) of the
+// register-handoff kernels.
+#ifndef CDX_RK_MINB_COL
+#define CDX_RK_MINB_COL 0
+#endif
+#ifndef CDX_RK_MINB_ROW
+#define CDX_RK_MINB_ROW 0
+#endif
+template <int N>
+struct RGeom {
+  using G = Geom<N>;
+  static constexpr int SMEM_ROW_ITER = G::SMEM_LINES + G::L * G::LD * (int)sizeof(float2) + G::L * ((N + 31) >> 5) * 4;
+  static constexpr int MINB_COL = (CDX_RK_MINB_COL > 0 && G::T == 256) ? CDX_RK_MINB_COL : G::MINB;
+  static constexpr int MINB_ROW = (CDX_RK_MINB_ROW > 0 && G::T == 256) ? CDX_RK_MINB_ROW : G::MINB;
+};
+
+// ------------------------------------------------------------- real-space updates
+template <int ALGO>
+__device__ __forceinline__ float2 update_t(bool inside, float2 x, float2 p, float beta) {
+  return apply_update(ALGO, inside, x, p, beta);
+}
+
+// ---------------------------------------------------------------- column pass
+// Lines are columns (length N = rows).  Column-tiled arrays have tile width L.
+template <int N, int MODE>
+__global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_COL) col_pass_rk(ColArgs a) {
+  using G = Geom<N>;
+  constexpr int L = G::L, T = G::T;
+  using F0 = RFirst<N, 0>;
+  using FL = RLast<N, 0>;   // == RFirst<N, 1> in shape
+  using IL = RLast<N, 1>;
+  static_assert(FL::R == RFirst<N, 1>::R && FL::B == RFirst<N, 1>::B, "plan 1 starts where plan 0 ends");
+  extern __shared__ float2 smem[];
+  __shared__ double red[T / 32];
+  const float2* __restrict__ tw = a.tw;
+  float2* buf = smem;
+  const int c0 = blockIdx.x * L;
+  const int ncols = min(L, a.cols - c0);
+  const long long C = a.cols;
+  const long long tile = (long long)blockIdx.x * N * L;
+
+  if (a.state) {
+    const int f = a.state[blockIdx.y].flags;
+    if (f & 6) {
+      if ((f & 4) == 0 && threadIdx.x == 0) atomicOr(&a.state[blockIdx.y].flags, 4);
+      return;
+    }
+  }
+  constexpr bool iter = MODE == COL_ITER;
+  float* amp_s = reinterpret_cast<float*>(smem + L * G::LD);
+  float* int_s = amp_s + L * N;
+  float* bs_s = int_s + L * N;
+  const long long aux = (long long)blockIdx.y * a.aux_stride + tile;
+  if constexpr (iter) {
+    const bool ccd = a.proj == PROJ_CCD;
+#pragma unroll 4
+    for (int q = threadIdx.x; q < L * N / 4; q += T) {
+      cp_async16(amp_s + 4 * q, a.amp + aux + 4 * q, true);
+      if (ccd) {
+        cp_async16(int_s + 4 * q, a.inten + aux + 4 * q, true);
+        if (a.bs) cp_async16(bs_s + 4 * q, a.bs + aux + 4 * q, true);
+      }
+    }
+    cp_commit();
+  }
+  const float2* in = a.in + (long long)blockIdx.y * a.in_stride;
+  const bool in_t = a.in_tiled != 0;
+  auto gload = [&](int l, int m) -> float2 {
+    if (in_t) return __ldcg(in + tile + (long long)m * L + l);
+    return l < ncols ? __ldcg(in + m * C + c0 + l) : make_float2(0.f, 0.f);
+  };
+  float2 v[FL::B][FL::R];
+  const bool fwd_fft = !iter || !a.from_psi;
+  if (fwd_fft) {
+    float2 v0[F0::B][F0::R];
+#pragma unroll
+    for (int b = 0; b < F0::B; ++b) {
+      int l, j;
+      if (!bfly_of<N, F0::R>(b, 0, l, j)) continue;
+#pragma unroll
+      for (int r = 0; r < F0::R; ++r) v0[b][r] = gload(l, j + r * F0::NR);
+    }
+    if (!iter && a.inv) rfft<N, 0, true>(v0, v, buf, tw, 0);
+    else rfft<N, 0, false>(v0, v, buf, tw, 0);
+  } else {
+    // Psi given: load it where the forward transform would have left it
+#pragma unroll
+    for (int b = 0; b < FL::B; ++b) {
+      int l, j;
+      if (!bfly_of<N, FL::R>(b, 0, l, j)) continue;
+#pragma unroll
+      for (int r = 0; r < FL::R; ++r) v[b][r] = gload(l, j + r * FL::NS);
+    }
+  }
+  float2* out = a.out + (long long)blockIdx.y * a.out_stride;
+  const bool out_t = a.out_tiled != 0;
+  const float s = a.scale;
+  if constexpr (!iter) {
+#pragma unroll
+    for (int b = 0; b < FL::B; ++b) {
+      int l, j;
+      if (!bfly_of<N, FL::R>(b, 0, l, j)) continue;
+#pragma unroll
+      for (int r = 0; r < FL::R; ++r) {
+        const int m = j + r * FL::NS;
+        float2 y = v[b][r];
+        if (s != 1.f) { y.x *= s; y.y *= s; }
+        if (out_t) __stcg(out + tile + (long long)m * L + l, y);
+        else if (l < ncols) __stcg(out + m * C + c0 + l, y);
+      }
+    }
+    return;
+  } else {
+    cp_wait<0>();
+    __syncthreads();
+    // Psi complete in registers: optional copy-out, R-factor partial, projection
+    double rsum = 0.0;
+    float2* psi_out = a.psi_out ? a.psi_out + (long long)blockIdx.y * a.psi_stride : nullptr;
+#pragma unroll
+    for (int b = 0; b < FL::B; ++b) {
+      int l, j;
+      if (!bfly_of<N, FL::R>(b, 0, l, j)) continue;
+#pragma unroll
+      for (int r = 0; r < FL::R; ++r) {
+        const int m = j + r * FL::NS;
+        float2 z = v[b][r];
+        if (l < ncols) {
+          if (psi_out) psi_out[m * C + c0 + l] = z;
+          const int t = m * L + l;
+          const float amp = amp_s[t];
+          if (a.rf_partials) rsum += fabsf(hypotf(z.x, z.y) - amp);
+          if (a.proj == PROJ_MODABS) z = proj_modabs_fast(z, amp);
+          else z = proj_ccd(z, int_s[t], a.bs ? bs_s[t] : 0.f, a.bs != nullptr, a.noise_level, a.ccd_scale,
+                            a.ccd_rcolor);
+        } else {
+          z = make_float2(0.f, 0.f);
+        }
+        v[b][r] = z;
+      }
+    }
+    if (a.rf_partials) {
+      const double tsum = block_sum_d<T>(rsum, red);
+      if (threadIdx.x == 0) a.rf_partials[(long long)blockIdx.y * gridDim.x + blockIdx.x] = tsum;
+    }
+    float2 o[IL::B][IL::R];
+    rfft<N, 1, true>(v, o, buf, tw, 0);
+#pragma unroll
+    for (int b = 0; b < IL::B; ++b) {
+      int l, j;
+      if (!bfly_of<N, IL::R>(b, 0, l, j)) continue;
+#pragma unroll
+      for (int r = 0; r < IL::R; ++r) {
+        const int m = j + r * IL::NS;
+        float2 y = o[b][r];
+        if (s != 1.f) { y.x *= s; y.y *= s; }
+        if (out_t) __stcg(out + tile + (long long)m * L + l, y);
+        else if (l < ncols) __stcg(out + m * C + c0 + l, y);
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------- row pass
+// Lines are rows (length N = cols).  Column-tiled arrays have tile width
+// 2^tile_log2 (the column pass's L for the row count).
+template <int N, int MODE, int ALGO>
+__device__ __forceinline__ void row_pass_body(const RowArgs& a) {
+  using G = Geom<N>;
+  constexpr int L = G::L, T = G::T;
+  using F0 = RFirst<N, 0>;
+  using FL = RLast<N, 0>;
+  using IL = RLast<N, 1>;
+  static_assert(FL::R == RFirst<N, 1>::R && FL::B == RFirst<N, 1>::B, "plan 1 starts where plan 0 ends");
+  extern __shared__ float2 smem[];
+  const float2* __restrict__ tw = a.tw;
+  float2* buf = smem;
+  const int row0 = blockIdx.x * L;
+  const int nrows = min(L, a.rows - row0);
+  constexpr bool iter = MODE == ROW_ITER;
+  const int tl = a.tile_log2;
+  // tiled: four (or 2^tl) threads per tile row piece; row-major: consecutive
+  // threads take consecutive columns
+  const bool tiled = a.in_tiled || a.out_tiled;
+  const int cb = tiled ? min(tl, rfft_cb_max<N>()) : rfft_cb_max<N>();
+
+  // rho rows and support words of the CTA (ROW_ITER), landing during the inverse FFT
+  constexpr int RS = G::LD;                 // rho line stride in shared memory
+  constexpr int WPR = (N + 31) >> 5;
+  float2* rho_s = smem + L * G::LD;
+  uint32_t* mask_s = reinterpret_cast<uint32_t*>(rho_s + L * RS);
+  float2* rho = a.rho + (long long)blockIdx.y * a.rho_stride + (long long)row0 * N;
+  if constexpr (iter) {
+    if constexpr (RS % 2 == 0) {
+#pragma unroll 4
+      for (int e = threadIdx.x; e < L * N / 2; e += T) {
+        const int l = (2 * e) / N, c = 2 * e - l * N;
+        const bool ok = l < nrows;
+        cp_async16(rho_s + l * RS + c, ok ? rho + 2 * e : rho, ok);
+      }
+    } else {
+#pragma unroll 4
+      for (int e = threadIdx.x; e < L * N; e += T) {
+        const int l = e / N, c = e - l * N;
+        const bool ok = l < nrows;
+        cp_async8(rho_s + l * RS + c, ok ? rho + e : rho, ok);
+      }
+    }
+    const uint32_t* mask = a.mask + (long long)blockIdx.y * a.mask_stride + (long long)row0 * WPR;
+    for (int w = threadIdx.x; w < L * WPR; w += T) {
+      const bool ok = w / WPR < nrows;
+      cp_async4(mask_s + w, ok ? mask + w : mask, ok);
+    }
+    cp_commit();
+  }
+  const float2* in = a.in + (long long)blockIdx.y * a.in_stride;
+  const long long R = a.rows;
+  auto goff = [&](bool t, int l, int c) -> long long {
+    const int row = row0 + l;
+    return t ? ((((long long)(c >> tl)) * R + row) << tl) + (c & ((1 << tl) - 1)) : (long long)row * N + c;
+  };
+  float2 v[FL::B][FL::R];
+  {
+    float2 v0[F0::B][F0::R];
+#pragma unroll
+    for (int b = 0; b < F0::B; ++b) {
+      int l, j;
+      if (!bfly_of<N, F0::R>(b, cb, l, j)) continue;
+#pragma unroll
+      for (int r = 0; r < F0::R; ++r)
+        v0[b][r] = l < nrows ? __ldcg(in + goff(a.in_tiled, l, j + r * F0::NR)) : make_float2(0.f, 0.f);
+    }
+    if (iter || a.inv) rfft<N, 0, true>(v0, v, buf, tw, cb);
+    else rfft<N, 0, false>(v0, v, buf, tw, cb);
+  }
+  float2* out = a.out + (long long)blockIdx.y * a.out_stride;
+  const float s = a.scale;
+  if constexpr (!iter) {
+#pragma unroll
+    for (int b = 0; b < FL::B; ++b) {
+      int l, j;
+      if (!bfly_of<N, FL::R>(b, cb, l, j)) continue;
+      if (l >= nrows) continue;
+#pragma unroll
+      for (int r = 0; r < FL::R; ++r) {
+        float2 y = v[b][r];
+        if (s != 1.f) { y.x *= s; y.y *= s; }
+        __stcg(out + goff(a.out_tiled, l, j + r * FL::NS), y);
+      }
+    }
+  } else {
+    cp_wait<0>();
+    __syncthreads();
+    // rho' = IFFT/N; update against rho and the support bits
+#pragma unroll
+    for (int b = 0; b < FL::B; ++b) {
+      int l, j;
+      if (!bfly_of<N, FL::R>(b, cb, l, j)) continue;
+#pragma unroll
+      for (int r = 0; r < FL::R; ++r) {
+        const int c = j + r * FL::NS;
+        float2 y = make_float2(0.f, 0.f);
+        if (l < nrows) {
+          float2 p = v[b][r];
+          p.x *= a.inv_n;
+          p.y *= a.inv_n;
+          const float2 x = rho_s[l * RS + c];
+          const bool inside = (mask_s[l * WPR + (c >> 5)] >> (c & 31)) & 1u;
+          y = update_t<ALGO>(inside, x, p, a.beta);
+          rho[l * N + c] = y;
+        }
+        v[b][r] = y;
+      }
+    }
+    float2 o[IL::B][IL::R];
+    rfft<N, 1, false>(v, o, buf, tw, cb);
+#pragma unroll
+    for (int b = 0; b < IL::B; ++b) {
+      int l, j;
+      if (!bfly_of<N, IL::R>(b, cb, l, j)) continue;
+      if (l >= nrows) continue;
+#pragma unroll
+      for (int r = 0; r < IL::R; ++r) {
+        float2 y = o[b][r];
+        if (s != 1.f) { y.x *= s; y.y *= s; }
+        __stcg(out + goff(a.out_tiled, l, j + r * IL::NS), y);
+      }
+    }
+  }
+}
+
+template <int N, int MODE>
+__global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_ROW) row_pass_rk(RowArgs a) {
+  if (a.state && (a.state[blockIdx.y].flags & 4)) return;   // frozen pattern
+  if constexpr (MODE == ROW_FFT) {
+    row_pass_body<N, ROW_FFT, ALGO_ER>(a);
+  } else {
+    switch (a.algo) {
+      case ALGO_HIO: row_pass_body<N, ROW_ITER, ALGO_HIO>(a); break;
+      case ALGO_RAAR: row_pass_body<N, ROW_ITER, ALGO_RAAR>(a); break;
+      case ALGO_ER: row_pass_body<N, ROW_ITER, ALGO_ER>(a); break;
+      case ALGO_POSER: row_pass_body<N, ROW_ITER, ALGO_POSER>(a); break;
+      case ALGO_POSHIO: row_pass_body<N, ROW_ITER, ALGO_POSHIO>(a); break;
+      default: row_pass_body<N, ROW_ITER, ALGO_FHIO>(a); break;
+    }
+  }
+}
+
+
+}  // namespace cdx

@@ -1,23 +1,42 @@
 // Per-length instantiation of the row/column pass kernels and their launchers.
+// FP32 (tc == 0): the register-handoff kernels of cdx_rfft.cuh.  Tensor-core
+// radix-16 passes (tc == 1): the staged kernels of cdx_kernels.cuh.
 #pragma once
-#include "cdx_kernels.cuh"
+#include "cdx_rfft.cuh"
 
 namespace cdx {
 
-template <int N, bool TC>
-cudaError_t prepare_variant() {
+template <int N>
+cudaError_t prepare_tc() {
   using G = Geom<N>;
   cudaError_t e;
-  if ((e = cudaFuncSetAttribute(row_pass_kernel<N, ROW_FFT, TC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  if ((e = cudaFuncSetAttribute(row_pass_kernel<N, ROW_FFT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 G::SMEM_LINES)) != cudaSuccess)
     return e;
-  if ((e = cudaFuncSetAttribute(row_pass_kernel<N, ROW_ITER, TC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  if ((e = cudaFuncSetAttribute(row_pass_kernel<N, ROW_ITER, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 G::SMEM_ROW_ITER)) != cudaSuccess)
     return e;
-  if ((e = cudaFuncSetAttribute(col_pass_kernel<N, COL_FFT, TC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  if ((e = cudaFuncSetAttribute(col_pass_kernel<N, COL_FFT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 G::SMEM_LINES)) != cudaSuccess)
     return e;
-  return cudaFuncSetAttribute(col_pass_kernel<N, COL_ITER, TC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  return cudaFuncSetAttribute(col_pass_kernel<N, COL_ITER, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              G::SMEM_COL_CCD);
+}
+
+template <int N>
+cudaError_t prepare_rk() {
+  using G = Geom<N>;
+  cudaError_t e;
+  if ((e = cudaFuncSetAttribute(row_pass_rk<N, ROW_FFT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                G::SMEM_LINES)) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(row_pass_rk<N, ROW_ITER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                RGeom<N>::SMEM_ROW_ITER)) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(col_pass_rk<N, COL_FFT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                G::SMEM_LINES)) != cudaSuccess)
+    return e;
+  return cudaFuncSetAttribute(col_pass_rk<N, COL_ITER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               G::SMEM_COL_CCD);
 }
 
@@ -25,31 +44,21 @@ cudaError_t prepare_variant() {
 // current device (outside any stream capture).
 template <int N>
 cudaError_t prepare_len() {
-  cudaError_t e = prepare_variant<N, false>();
-  return e != cudaSuccess ? e : prepare_variant<N, true>();
-}
-
-template <int N, bool TC>
-void launch_row_variant(const RowArgs& a, dim3 grid, cudaStream_t st) {
-  using G = Geom<N>;
-  if (a.mode == ROW_ITER) row_pass_kernel<N, ROW_ITER, TC><<<grid, G::T, G::SMEM_ROW_ITER, st>>>(a);
-  else row_pass_kernel<N, ROW_FFT, TC><<<grid, G::T, G::SMEM_LINES, st>>>(a);
-}
-
-template <int N, bool TC>
-void launch_col_variant(const ColArgs& a, dim3 grid, cudaStream_t st) {
-  using G = Geom<N>;
-  if (a.mode == COL_ITER)
-    col_pass_kernel<N, COL_ITER, TC><<<grid, G::T, a.proj == PROJ_CCD ? G::SMEM_COL_CCD : G::SMEM_COL_ITER, st>>>(a);
-  else col_pass_kernel<N, COL_FFT, TC><<<grid, G::T, G::SMEM_LINES, st>>>(a);
+  cudaError_t e = prepare_rk<N>();
+  return e != cudaSuccess ? e : prepare_tc<N>();
 }
 
 template <int N>
 cudaError_t launch_row(const RowArgs& a, int batch, cudaStream_t st) {
   using G = Geom<N>;
   dim3 grid((a.rows + G::L - 1) / G::L, batch);
-  if (a.tc) launch_row_variant<N, true>(a, grid, st);
-  else launch_row_variant<N, false>(a, grid, st);
+  if (a.tc) {
+    if (a.mode == ROW_ITER) row_pass_kernel<N, ROW_ITER, true><<<grid, G::T, G::SMEM_ROW_ITER, st>>>(a);
+    else row_pass_kernel<N, ROW_FFT, true><<<grid, G::T, G::SMEM_LINES, st>>>(a);
+  } else {
+    if (a.mode == ROW_ITER) row_pass_rk<N, ROW_ITER><<<grid, G::T, RGeom<N>::SMEM_ROW_ITER, st>>>(a);
+    else row_pass_rk<N, ROW_FFT><<<grid, G::T, G::SMEM_LINES, st>>>(a);
+  }
   return cudaGetLastError();
 }
 
@@ -57,8 +66,14 @@ template <int N>
 cudaError_t launch_col(const ColArgs& a, int batch, cudaStream_t st) {
   using G = Geom<N>;
   dim3 grid((a.cols + G::L - 1) / G::L, batch);
-  if (a.tc) launch_col_variant<N, true>(a, grid, st);
-  else launch_col_variant<N, false>(a, grid, st);
+  const int smem_iter = a.proj == PROJ_CCD ? G::SMEM_COL_CCD : G::SMEM_COL_ITER;
+  if (a.tc) {
+    if (a.mode == COL_ITER) col_pass_kernel<N, COL_ITER, true><<<grid, G::T, smem_iter, st>>>(a);
+    else col_pass_kernel<N, COL_FFT, true><<<grid, G::T, G::SMEM_LINES, st>>>(a);
+  } else {
+    if (a.mode == COL_ITER) col_pass_rk<N, COL_ITER><<<grid, G::T, smem_iter, st>>>(a);
+    else col_pass_rk<N, COL_FFT><<<grid, G::T, G::SMEM_LINES, st>>>(a);
+  }
   return cudaGetLastError();
 }
 
