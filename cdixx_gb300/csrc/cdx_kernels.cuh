@@ -69,15 +69,6 @@ __device__ __forceinline__ float2 proj_modabs(float2 s, float amp) {
   float rat = amp / mod;
   return make_float2(s.x * rat, s.y * rat);
 }
-// The same projection with amp/|s| as one reciprocal square root of |s|^2
-// (a few ulp from the division above); |s|^2 outside [2^-100, 2^100] takes
-// the exact form, so no intermediate under- or overflows.
-__device__ __forceinline__ float2 proj_modabs_fast(float2 s, float amp) {
-  const float m2 = fmaf(s.x, s.x, s.y * s.y);
-  if (!(m2 > 7.8886e-31f && m2 < 1.2676e30f)) return proj_modabs(s, amp);
-  const float rat = amp * rsqrtf(m2);
-  return make_float2(s.x * rat, s.y * rat);
-}
 // Noise-tolerant projection, 5-argument applyMod with bsnorm == 1
 // (src/gpu/cdi.cu:438-485).  scale = vars.scale, rcolor = vars.rcolor.
 __device__ __forceinline__ float2 proj_ccd(float2 s, float inten, float bs, bool has_bs,

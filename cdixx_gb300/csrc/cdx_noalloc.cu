@@ -65,22 +65,12 @@ int scratch_address(void** out) {
   return CDX_OK;
 }
 
-// Per-pass twiddle table of length n (same entries as the host table of
-// cdx_dispatch.cu), evaluated on the device in double precision.
-__global__ void k_fill_twiddles(float2* out, int n, int count) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= count) return;
-  const int plan = i < tw_plan_count(n, 0) ? 0 : 1;
-  int p = 1;
-  while (plan_radix_x(n, plan, p + 1) != 0 && tw_offset_x(n, plan, p + 1) <= i) ++p;
-  const int R = plan_radix_x(n, plan, p), NS = plan_ns_x(n, plan, p), step = n / (NS * R);
-  const int j = i - tw_offset_x(n, plan, p);
-  const int r = j / NS + 1, k = j - (r - 1) * NS;
-  const long long t = ((long long)r * k * step) % n;
-  double s, c;
-  sincospi(2.0 * (double)t / (double)n, &s, &c);
-  out[i] = make_float2((float)c, (float)-s);
-}
+// Per-pass twiddle tables, filled on the host by the same routine as the
+// context path's (cdx_dispatch.cu), so both entry points use identical
+// values.  Static host storage (the largest table, length 4096, has 8160
+// entries); a call copies its tables from there into the device scratch.
+constexpr int kMaxTw = 8192;
+static float2 g_tw_host[2][kMaxTw];
 
 inline size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
 
@@ -114,6 +104,7 @@ extern "C" int cdx_iterate_noalloc(int rows, int cols, int algo, float beta, int
   const long long wst = (long long)rows * cp;
   const int wpr = (cols + 31) >> 5;
   const int ntr = twiddle_count(rows), ntc = twiddle_count(cols);
+  if (ntr > kMaxTw || ntc > kMaxTw) return set_error_cstr(CDX_ERR_SIZE, "cdx_iterate_noalloc: twiddle table too long");
   const size_t o_work = 0;
   const size_t o_amp = o_work + al256(sizeof(float2) * wst);
   const size_t o_mask = o_amp + al256(sizeof(float) * wst);
@@ -139,9 +130,20 @@ extern "C" int cdx_iterate_noalloc(int rows, int cols, int algo, float beta, int
 
   // the array keeps the previous call's contents: clear what this call uses
   NA_CK(cudaMemsetAsync(s, 0, need, st));
-  if (ntr > 0) k_fill_twiddles<<<(ntr + 255) / 256, 256, 0, st>>>(tw_r, rows, ntr);
-  if (ntc > 0) k_fill_twiddles<<<(ntc + 255) / 256, 256, 0, st>>>(tw_c, cols, ntc);
-  NA_CK(cudaGetLastError());
+  {
+    // the host tables are shared by all calls: fill and copy under the lock
+    static std::mutex tw_lock;
+    std::lock_guard<std::mutex> g(tw_lock);
+    if (ntr > 0) {
+      twiddle_table(rows, g_tw_host[0]);
+      NA_CK(cudaMemcpyAsync(tw_r, g_tw_host[0], sizeof(float2) * ntr, cudaMemcpyHostToDevice, st));
+    }
+    if (ntc > 0) {
+      twiddle_table(cols, g_tw_host[1]);
+      NA_CK(cudaMemcpyAsync(tw_c, g_tw_host[1], sizeof(float2) * ntc, cudaMemcpyHostToDevice, st));
+    }
+    NA_CK(cudaStreamSynchronize(st));   // the host tables may be refilled by the next call
+  }
   // sqrt(I), column-tiled (applyModAbs's sqrtf of I > 0, else 0)
   NA_CK(to_tiled(intensity, amp_t, rows, cols, tl, wst, 1, st));
   NA_CK(amp_from_pattern(amp_t, amp_t, wst, st));

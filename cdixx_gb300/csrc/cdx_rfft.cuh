@@ -309,7 +309,7 @@ __global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_COL) col_pass_rk(Co
           const int t = m * L + l;
           const float amp = amp_s[t];
           if (a.rf_partials) rsum += fabsf(hypotf(z.x, z.y) - amp);
-          if (a.proj == PROJ_MODABS) z = proj_modabs_fast(z, amp);
+          if (a.proj == PROJ_MODABS) z = proj_modabs(z, amp);
           else z = proj_ccd(z, int_s[t], a.bs ? bs_s[t] : 0.f, a.bs != nullptr, a.noise_level, a.ccd_scale,
                             a.ccd_rcolor);
         } else {

@@ -94,8 +94,22 @@ _SIGS = {
     "cdx_size_supported": [_I],
     "cdx_last_error": [],
     "cdx_version": [],
+    # include/cdx_unet.h
+    "cdx_unet_config_default": [ctypes.c_void_p],
+    "cdx_unet_create": [ctypes.c_void_p, _P, ctypes.POINTER(_P)],
+    "cdx_unet_destroy": [_P],
+    "cdx_unet_param_count": [_P],
+    "cdx_unet_get_params": [_P, _P, _LL],
+    "cdx_unet_set_params": [_P, _P, _LL],
+    "cdx_unet_get_grads": [_P, _P, _LL],
+    "cdx_unet_forward": [_P, _P, _P, _I],
+    "cdx_unet_loss_backward": [_P, _P, _P, _P, _P, _I, ctypes.POINTER(ctypes.c_double)],
+    "cdx_unet_adam_step": [_P, _F],
+    "cdx_unet_warm_start": [_P, _P, _P, _I, _I, _P, _P],
+    "cdx_forward_model": [_I, _I, ctypes.c_ulonglong, _LL, ctypes.c_double, _P, _P, _P, _P, _P],
 }
-_RESTYPE = {"cdx_last_error": ctypes.c_char_p, "cdx_version": ctypes.c_char_p}
+_RESTYPE = {"cdx_last_error": ctypes.c_char_p, "cdx_version": ctypes.c_char_p, "cdx_unet_destroy": None,
+            "cdx_unet_param_count": ctypes.c_longlong}
 
 _lib = None
 
