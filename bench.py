@@ -17,6 +17,12 @@ pattern; the full job (2000 iterations) is 40 steps.
            support 1, write rho 8) / the measured duration of one iteration (its
            column + row pass), against the measured HBM copy bandwidth.
 
+  warm_start  the learned warm start: a U-Net trained here (one pass over 50k
+           forward-model seeds, batch 64) against the plain random-phase path on
+           1024 held-out 256^2 patterns, patterns/s reaching R <= 0.02
+  batched  512 patterns of uneven sizes {128..512}^2, HIO/ER 500 each, one
+           CUDA graph: patterns/s
+
 `--impl reference` times the CPU restatement of the reference path (the
 oracle, float32, multi-threaded scipy FFT) on a bounded sample of the same
 workload.
@@ -161,6 +167,123 @@ def run_reference(args):
     return 0
 
 
+WARM_N, WARM_BATCH, WARM_TRAIN_SEEDS, WARM_EVAL = 256, 64, 50_000, 1024
+WARM_TARGET = 0.02
+# the reference's path for this object family: HIO beta 0.9 x180 then ER x20 with a
+# shrinkwrap every 20 iterations, from a random-phase start and the rect support
+PLAIN_ALGO = "10*(" + "+".join(["20*HIO+1*shrinkWrap"] * 9) + "+20*ER+1*shrinkWrap)"
+# from the network's warm start: the same HIO/ER schedule on its (fixed) support
+WARM_ALGO = "10*(180*HIO+20*ER)"
+
+
+def warm_start_section():
+    """Learned warm start (U-Net trained here by the library's own kernels) vs the
+    plain random-phase path on held-out noise-free 256^2 blob patterns: patterns/s
+    that reach R <= WARM_TARGET within 2000 iterations (per-pattern stop)."""
+    import torch
+    from cdixx_gb300 import metrics, unet
+    from cdixx_gb300 import native as cdx
+    n, B = WARM_N, WARM_BATCH
+    net = unet.UNet(n=n, levels=4, base=32, batch=B, seed=SEED)
+    steps = WARM_TRAIN_SEEDS // B
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    losses = unet.train(net, steps, seed=SEED, photons=1e6, lr=1e-3)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    res = {"plain": [0, 0.0, [], []], "learned": [0, 0.0, [], []]}   # reached, seconds, iters, errors
+    ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+    for k in range(WARM_EVAL // B):
+        I, a, _, _ = unet.forward_model(n, B, SEED + 1, k * B, -1e6)
+        truth = a.cpu().numpy() if k < 2 else None
+        ev[0].record()
+        out = net.forward(I)
+        psi_w, sup_w = net.warm_start(I, out, 3)
+        ev[1].record()
+        torch.cuda.synchronize()
+        net_s = ev[0].elapsed_time(ev[1]) / 1000.0
+        for mode in ("plain", "learned"):
+            prm = cdx.default_params(n, n, batch=B, beta=0.9, shrink_threshold=0.1, oversampling_spt=2.0,
+                                     rf_every=10, stop_rfactor=WARM_TARGET)
+            with cdx.Context(prm) as ctx:
+                for i in range(B):
+                    ctx.set_pattern(i, I[i])
+                if mode == "plain":
+                    ctx.random_start(SEED + k)
+                else:
+                    for i in range(B):
+                        ctx.set_initial(i, psi_w[i])
+                        ctx.set_support(i, sup_w[i])
+                st = ctx.run(PLAIN_ALGO if mode == "plain" else WARM_ALGO)
+                conv = [ctx.stats(i)["converged_iter"] for i in range(B)]
+                r = res[mode]
+                r[0] += sum(c >= 0 for c in conv)
+                r[1] += st["gpu_ms"] / 1000.0 + (net_s if mode == "learned" else 0.0)
+                r[2] += [c for c in conv if c >= 0]
+                if truth is not None:
+                    r[3] += [metrics.error_vs_truth(ctx.get_object(i), truth[i]) for i in range(B)]
+    out = {"metric": f"patterns/s reaching R<={WARM_TARGET} within 2000 iterations",
+           "patterns": WARM_EVAL, "n": n, "data": "noise-free synthetic blob objects (held-out seeds)",
+           "train": {"seeds": steps * B, "batch": B, "lr": 1e-3, "seconds": train_s,
+                     "loss_first": losses[0], "loss_last": float(np.mean(losses[-20:]))}}
+    for mode, (reached, secs, its, errs) in res.items():
+        out[mode] = {"patterns_per_s": reached / secs, "reached": reached / WARM_EVAL,
+                     "median_iterations": float(np.median(its)) if its else None,
+                     "gpu_s": secs, "median_error_vs_truth": float(np.median(errs)) if errs else None,
+                     "algorithm": PLAIN_ALGO if mode == "plain" else WARM_ALGO + " (+ U-Net forward)"}
+    pp = out["plain"]["patterns_per_s"]
+    out["speedup"] = out["learned"]["patterns_per_s"] / pp if pp > 0 else None
+    net.close()
+    return out
+
+
+BATCH_SIZES = (128, 192, 256, 384, 512)
+BATCH_PATTERNS = 512
+BATCH_ALGO = "500*HIO+500*ER"
+
+
+def batched_section():
+    """512 patterns of uneven sizes (uniform over BATCH_SIZES squared, photons
+    log-uniform 1e5..1e8, blob objects in a support of 1/4 linear size), HIO and
+    ER 500 iterations each, every size one context, all run as one CUDA graph."""
+    import torch
+    from cdixx_gb300 import native as cdx
+    from cdixx_gb300 import unet
+    rng = np.random.default_rng(SEED)
+    sizes = rng.choice(BATCH_SIZES, BATCH_PATTERNS)
+    photons = 10 ** rng.uniform(5, 8, BATCH_PATTERNS)
+    ctxs = []
+    px = 0
+    for n in BATCH_SIZES:
+        idx = np.nonzero(sizes == n)[0]
+        if len(idx) == 0:
+            continue
+        ctx = cdx.Context(cdx.default_params(int(n), int(n), batch=len(idx), beta=0.9, oversampling_spt=2.0))
+        for j, p in enumerate(idx):
+            I, _, _, _ = unet.forward_model(int(n), 1, SEED + 2, int(p), float(photons[p]))
+            ctx.set_pattern(j, I[0])
+        ctx.random_start(SEED + int(n))
+        ctxs.append(ctx)
+        px += len(idx) * int(n) * int(n)
+    g = cdx.Group(ctxs)
+    g.run("2*HIO")   # warm-up; the timed algorithm's graph is built inside the timed call,
+    # but gpu_ms covers only its launch (events on the group's stream)
+    for c in ctxs:
+        c.random_start(SEED)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ms = g.run(BATCH_ALGO)
+    wall = time.perf_counter() - t0
+    g.close()
+    for c in ctxs:
+        c.close()
+    iters = 1000
+    return {"metric": "patterns/s", "patterns": BATCH_PATTERNS, "sizes": list(BATCH_SIZES),
+            "algorithm": BATCH_ALGO, "patterns_per_s": BATCH_PATTERNS / (ms / 1000.0),
+            "pixel_iterations_per_s": px * iters / (ms / 1000.0), "gpu_ms": ms, "wall_ms_incl_graph_build": wall * 1000,
+            "contexts": len(ctxs), "launch": "one CUDA graph (cdx_group) with one branch per size"}
+
+
 def run_gpu(args):
     import torch
     from cdixx_gb300 import native as cdx
@@ -259,6 +382,11 @@ def run_gpu(args):
         cpu = {"value": v, "unit": "iter/s", "cores": threads, "kind": "port",
                "sample": "2 RAAR iterations of the 2048^2 pattern, float32 oracle, "
                          f"scipy.fft with {threads} workers ({dt:.2f} s)"}
+    warm = batched = None
+    if rank == 0 and not args.no_warm:
+        warm = warm_start_section()
+    if rank == 0 and not args.no_batched:
+        batched = batched_section()
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "iter/s", "n_gpus": world, "steps": args.steps,
@@ -276,6 +404,8 @@ def run_gpu(args):
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": launches_per_step * args.steps,
+            "warm_start": warm,
+            "batched": batched,
         }
         print(json.dumps(line))
     ctx.close()
@@ -291,6 +421,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-warm", action="store_true", help="skip the learned warm-start section")
+    ap.add_argument("--no-batched", action="store_true", help="skip the uneven-size batch section")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
