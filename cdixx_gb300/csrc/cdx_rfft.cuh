@@ -468,22 +468,12 @@ __device__ __forceinline__ void row_pass_body(const RowArgs& a) {
   }
 }
 
-template <int N, int MODE>
+// One kernel per update (ALGO is ignored in ROW_FFT mode): the executed code
+// holds a single update and no switch.
+template <int N, int MODE, int ALGO>
 __global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_ROW) row_pass_rk(RowArgs a) {
   if (a.state && (a.state[blockIdx.y].flags & 4)) return;   // frozen pattern
-  if constexpr (MODE == ROW_FFT) {
-    row_pass_body<N, ROW_FFT, ALGO_ER>(a);
-  } else {
-    switch (a.algo) {
-      case ALGO_HIO: row_pass_body<N, ROW_ITER, ALGO_HIO>(a); break;
-      case ALGO_RAAR: row_pass_body<N, ROW_ITER, ALGO_RAAR>(a); break;
-      case ALGO_ER: row_pass_body<N, ROW_ITER, ALGO_ER>(a); break;
-      case ALGO_POSER: row_pass_body<N, ROW_ITER, ALGO_POSER>(a); break;
-      case ALGO_POSHIO: row_pass_body<N, ROW_ITER, ALGO_POSHIO>(a); break;
-      default: row_pass_body<N, ROW_ITER, ALGO_FHIO>(a); break;
-    }
-  }
+  row_pass_body<N, MODE, ALGO>(a);
 }
-
 
 }  // namespace cdx

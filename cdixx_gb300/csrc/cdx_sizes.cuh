@@ -27,12 +27,17 @@ template <int N>
 cudaError_t prepare_rk() {
   using G = Geom<N>;
   cudaError_t e;
-  if ((e = cudaFuncSetAttribute(row_pass_rk<N, ROW_FFT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  if ((e = cudaFuncSetAttribute(row_pass_rk<N, ROW_FFT, ALGO_ER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 G::SMEM_LINES)) != cudaSuccess)
     return e;
-  if ((e = cudaFuncSetAttribute(row_pass_rk<N, ROW_ITER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                RGeom<N>::SMEM_ROW_ITER)) != cudaSuccess)
-    return e;
+  const void* iter_kernels[] = {
+      (const void*)row_pass_rk<N, ROW_ITER, ALGO_HIO>, (const void*)row_pass_rk<N, ROW_ITER, ALGO_RAAR>,
+      (const void*)row_pass_rk<N, ROW_ITER, ALGO_ER>, (const void*)row_pass_rk<N, ROW_ITER, ALGO_POSER>,
+      (const void*)row_pass_rk<N, ROW_ITER, ALGO_POSHIO>, (const void*)row_pass_rk<N, ROW_ITER, ALGO_FHIO>};
+  for (const void* k : iter_kernels)
+    if ((e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, RGeom<N>::SMEM_ROW_ITER)) !=
+        cudaSuccess)
+      return e;
   if ((e = cudaFuncSetAttribute(col_pass_rk<N, COL_FFT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 G::SMEM_LINES)) != cudaSuccess)
     return e;
@@ -56,8 +61,16 @@ cudaError_t launch_row(const RowArgs& a, int batch, cudaStream_t st) {
     if (a.mode == ROW_ITER) row_pass_kernel<N, ROW_ITER, true><<<grid, G::T, G::SMEM_ROW_ITER, st>>>(a);
     else row_pass_kernel<N, ROW_FFT, true><<<grid, G::T, G::SMEM_LINES, st>>>(a);
   } else {
-    if (a.mode == ROW_ITER) row_pass_rk<N, ROW_ITER><<<grid, G::T, RGeom<N>::SMEM_ROW_ITER, st>>>(a);
-    else row_pass_rk<N, ROW_FFT><<<grid, G::T, G::SMEM_LINES, st>>>(a);
+    constexpr int SM = RGeom<N>::SMEM_ROW_ITER;
+    if (a.mode != ROW_ITER) row_pass_rk<N, ROW_FFT, ALGO_ER><<<grid, G::T, G::SMEM_LINES, st>>>(a);
+    else switch (a.algo) {   // unknown codes take the FHIO branch, as applySupport does (cdi.cc:25-36)
+      case ALGO_HIO: row_pass_rk<N, ROW_ITER, ALGO_HIO><<<grid, G::T, SM, st>>>(a); break;
+      case ALGO_RAAR: row_pass_rk<N, ROW_ITER, ALGO_RAAR><<<grid, G::T, SM, st>>>(a); break;
+      case ALGO_ER: row_pass_rk<N, ROW_ITER, ALGO_ER><<<grid, G::T, SM, st>>>(a); break;
+      case ALGO_POSER: row_pass_rk<N, ROW_ITER, ALGO_POSER><<<grid, G::T, SM, st>>>(a); break;
+      case ALGO_POSHIO: row_pass_rk<N, ROW_ITER, ALGO_POSHIO><<<grid, G::T, SM, st>>>(a); break;
+      default: row_pass_rk<N, ROW_ITER, ALGO_FHIO><<<grid, G::T, SM, st>>>(a); break;
+    }
   }
   return cudaGetLastError();
 }
