@@ -179,10 +179,14 @@ __device__ __forceinline__ void rfft(float2 (&in)[RFirst<N, PLAN>::B][RFirst<N, 
 }
 
 // Shared memory and resident CTAs per SM (register budget) of the
-// register-handoff kernels.
+// register-handoff kernels.  The column pass at 256 threads is budgeted for 4
+// CTAs per SM (64 registers, no spills; 2-4 % faster than 3); the row pass is
+// held to 3 by its shared memory (the staged rho rows: loading rho straight
+// from global memory instead was 4-30 % slower, its latency exposed).
 #ifndef CDX_RK_MINB_COL
-#define CDX_RK_MINB_COL 0
+#define CDX_RK_MINB_COL 4
 #endif
+
 #ifndef CDX_RK_MINB_ROW
 #define CDX_RK_MINB_ROW 0
 #endif
@@ -202,7 +206,8 @@ __device__ __forceinline__ float2 update_t(bool inside, float2 x, float2 p, floa
 
 // ---------------------------------------------------------------- column pass
 // Lines are columns (length N = rows).  Column-tiled arrays have tile width L.
-template <int N, int MODE>
+// PROJ (COL_ITER): the modulus projection, PROJ_MODABS or PROJ_CCD.
+template <int N, int MODE, int PROJ>
 __global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_COL) col_pass_rk(ColArgs a) {
   using G = Geom<N>;
   constexpr int L = G::L, T = G::T;
@@ -232,11 +237,10 @@ __global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_COL) col_pass_rk(Co
   float* bs_s = int_s + L * N;
   const long long aux = (long long)blockIdx.y * a.aux_stride + tile;
   if constexpr (iter) {
-    const bool ccd = a.proj == PROJ_CCD;
 #pragma unroll 4
     for (int q = threadIdx.x; q < L * N / 4; q += T) {
       cp_async16(amp_s + 4 * q, a.amp + aux + 4 * q, true);
-      if (ccd) {
+      if constexpr (PROJ == PROJ_CCD) {
         cp_async16(int_s + 4 * q, a.inten + aux + 4 * q, true);
         if (a.bs) cp_async16(bs_s + 4 * q, a.bs + aux + 4 * q, true);
       }
@@ -293,34 +297,47 @@ __global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_COL) col_pass_rk(Co
   } else {
     cp_wait<0>();
     __syncthreads();
-    // Psi complete in registers: optional copy-out, R-factor partial, projection
-    double rsum = 0.0;
-    float2* psi_out = a.psi_out ? a.psi_out + (long long)blockIdx.y * a.psi_stride : nullptr;
+    // Psi complete in registers: optional copy-out and R-factor partial (each
+    // one loop behind one uniform branch), then the projection (branch-free
+    // per element, so the compiler interleaves the elements)
+    if (a.psi_out) {
+      float2* psi_out = a.psi_out + (long long)blockIdx.y * a.psi_stride;
+#pragma unroll
+      for (int b = 0; b < FL::B; ++b) {
+        int l, j;
+        if (!bfly_of<N, FL::R>(b, 0, l, j) || l >= ncols) continue;
+#pragma unroll
+        for (int r = 0; r < FL::R; ++r) psi_out[(j + r * FL::NS) * C + c0 + l] = v[b][r];
+      }
+    }
+    if (a.rf_partials) {
+      double rsum = 0.0;
+#pragma unroll
+      for (int b = 0; b < FL::B; ++b) {
+        int l, j;
+        if (!bfly_of<N, FL::R>(b, 0, l, j) || l >= ncols) continue;
+#pragma unroll
+        for (int r = 0; r < FL::R; ++r) {
+          const float2 z = v[b][r];
+          rsum += fabsf(hypotf(z.x, z.y) - amp_s[(j + r * FL::NS) * L + l]);
+        }
+      }
+      const double tsum = block_sum_d<T>(rsum, red);
+      if (threadIdx.x == 0) a.rf_partials[(long long)blockIdx.y * gridDim.x + blockIdx.x] = tsum;
+    }
 #pragma unroll
     for (int b = 0; b < FL::B; ++b) {
       int l, j;
       if (!bfly_of<N, FL::R>(b, 0, l, j)) continue;
 #pragma unroll
       for (int r = 0; r < FL::R; ++r) {
-        const int m = j + r * FL::NS;
+        const int t = (j + r * FL::NS) * L + l;
         float2 z = v[b][r];
-        if (l < ncols) {
-          if (psi_out) psi_out[m * C + c0 + l] = z;
-          const int t = m * L + l;
-          const float amp = amp_s[t];
-          if (a.rf_partials) rsum += fabsf(hypotf(z.x, z.y) - amp);
-          if (a.proj == PROJ_MODABS) z = proj_modabs(z, amp);
-          else z = proj_ccd(z, int_s[t], a.bs ? bs_s[t] : 0.f, a.bs != nullptr, a.noise_level, a.ccd_scale,
-                            a.ccd_rcolor);
-        } else {
-          z = make_float2(0.f, 0.f);
-        }
-        v[b][r] = z;
+        if constexpr (PROJ == PROJ_MODABS) z = proj_modabs(z, amp_s[t]);
+        else z = proj_ccd(z, int_s[t], a.bs ? bs_s[t] : 0.f, a.bs != nullptr, a.noise_level, a.ccd_scale,
+                          a.ccd_rcolor);
+        v[b][r] = l < ncols ? z : make_float2(0.f, 0.f);
       }
-    }
-    if (a.rf_partials) {
-      const double tsum = block_sum_d<T>(rsum, red);
-      if (threadIdx.x == 0) a.rf_partials[(long long)blockIdx.y * gridDim.x + blockIdx.x] = tsum;
     }
     float2 o[IL::B][IL::R];
     rfft<N, 1, true>(v, o, buf, tw, 0);

@@ -38,10 +38,13 @@ cudaError_t prepare_rk() {
     if ((e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, RGeom<N>::SMEM_ROW_ITER)) !=
         cudaSuccess)
       return e;
-  if ((e = cudaFuncSetAttribute(col_pass_rk<N, COL_FFT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  if ((e = cudaFuncSetAttribute(col_pass_rk<N, COL_FFT, PROJ_MODABS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 G::SMEM_LINES)) != cudaSuccess)
     return e;
-  return cudaFuncSetAttribute(col_pass_rk<N, COL_ITER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  if ((e = cudaFuncSetAttribute(col_pass_rk<N, COL_ITER, PROJ_MODABS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                G::SMEM_COL_ITER)) != cudaSuccess)
+    return e;
+  return cudaFuncSetAttribute(col_pass_rk<N, COL_ITER, PROJ_CCD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               G::SMEM_COL_CCD);
 }
 
@@ -84,8 +87,9 @@ cudaError_t launch_col(const ColArgs& a, int batch, cudaStream_t st) {
     if (a.mode == COL_ITER) col_pass_kernel<N, COL_ITER, true><<<grid, G::T, smem_iter, st>>>(a);
     else col_pass_kernel<N, COL_FFT, true><<<grid, G::T, G::SMEM_LINES, st>>>(a);
   } else {
-    if (a.mode == COL_ITER) col_pass_rk<N, COL_ITER><<<grid, G::T, smem_iter, st>>>(a);
-    else col_pass_rk<N, COL_FFT><<<grid, G::T, G::SMEM_LINES, st>>>(a);
+    if (a.mode != COL_ITER) col_pass_rk<N, COL_FFT, PROJ_MODABS><<<grid, G::T, G::SMEM_LINES, st>>>(a);
+    else if (a.proj == PROJ_CCD) col_pass_rk<N, COL_ITER, PROJ_CCD><<<grid, G::T, smem_iter, st>>>(a);
+    else col_pass_rk<N, COL_ITER, PROJ_MODABS><<<grid, G::T, smem_iter, st>>>(a);
   }
   return cudaGetLastError();
 }
