@@ -34,6 +34,7 @@ using namespace cdx;
 namespace {
 
 constexpr int kRedBlocks = 152;   // reduction CTAs per pattern (one per SM)
+constexpr int kSwBlocks = 608;    // shrinkwrap y-pass CTAs per pattern (four per SM)
 
 // ---------------------------------------------------------------- twiddles
 // Per-pass twiddle table of length n (cdx_dispatch.cu), one per (device, n),
@@ -86,7 +87,7 @@ struct cdx_ctx {
   uint32_t* mask = nullptr;
   float2 *tw_r = nullptr, *tw_c = nullptr;   // lengths rows (column pass) and cols (row pass)
   double* part = nullptr;                    // [batch][part_per_pat]
-  float* pmax = nullptr;                     // [batch][kRedBlocks]
+  float* pmax = nullptr;                     // [batch][kSwBlocks]
   int part_per_pat = 0;
   int col_blocks = 0;
   PatState* dstate = nullptr;
@@ -302,7 +303,7 @@ int enqueue_run(cdx_ctx* c, const std::vector<int>& steps, const SwPlan& sw, boo
       const bool m2 = c->p.shrink_mode == CDX_SHRINK_SPATIAL;
       CDX_CK(shrinkwrap(c->rho, c->tmp, c->spt, c->weights + sw.offx[swi], sw.radx[swi], c->weights + sw.offy[swi],
                         sw.rady[swi], c->rows, c->cols, c->batch, m2, (float)((double)c->rows * c->cols), c->pmax,
-                        c->part, kRedBlocks, c->dstate, c->p.shrink_threshold, c->st));
+                        c->part, kSwBlocks, c->dstate, c->p.shrink_threshold, c->st));
       CDX_CK(support_bits(c->spt, c->dstate, 0.f, c->mask, c->rows, c->cols, c->batch, c->st));
       nl += 4;
       ++swi;
@@ -571,7 +572,7 @@ int cdx_create(const cdx_params* p, void* stream, cdx_ctx** out) {
       return fail(set_error(CDX_ERR_CUDA, "stream create failed"));
     c->own_stream = true;
   }
-  if (prep_launcher(c->rows)() != cudaSuccess || prep_launcher(c->cols)() != cudaSuccess)
+  if (prep_launcher(c->rows)() != cudaSuccess || prep_launcher(c->cols)() != cudaSuccess || misc_prepare() != cudaSuccess)
     return fail(set_error(CDX_ERR_CUDA, std::string("kernel attributes: ") + cudaGetErrorString(cudaGetLastError())));
   if ((e = twiddles(c->rows, &c->tw_r)) || (e = twiddles(c->cols, &c->tw_c))) return fail(e);
   const int lc = lines_per_cta(c->rows);
@@ -580,7 +581,7 @@ int cdx_create(const cdx_params* p, void* stream, cdx_ctx** out) {
   c->cp = (c->cols + lc - 1) / lc * lc;
   c->wstride = (long long)c->rows * c->cp;
   c->col_blocks = c->cp / lc;
-  c->part_per_pat = std::max(kRedBlocks, c->col_blocks);
+  c->part_per_pat = std::max(std::max(kRedBlocks, kSwBlocks), c->col_blocks);
   // one arena: row-major rho, psi, tmp, I, support; tiled W, sqrt(I), I;
   // bits, partials, state
   const size_t B = (size_t)c->batch, N = (size_t)c->npx, W = (size_t)c->wstride;
@@ -596,7 +597,7 @@ int cdx_create(const cdx_params* p, void* stream, cdx_ctx** out) {
   const size_t o_spt = off; off += al(sizeof(float) * B * N);
   const size_t o_mask = off; off += al(sizeof(uint32_t) * B * c->rows * c->wpr);
   const size_t o_part = off; off += al(sizeof(double) * B * c->part_per_pat);
-  const size_t o_pmax = off; off += al(sizeof(float) * B * kRedBlocks);
+  const size_t o_pmax = off; off += al(sizeof(float) * B * kSwBlocks);
   const size_t o_state = off; off += al(sizeof(PatState) * B);
   if (cudaMalloc(&c->arena, off) != cudaSuccess) {
     cudaGetLastError();

@@ -183,13 +183,14 @@ __device__ __forceinline__ int wrap(int i, int n) {
 }
 
 // x pass: CTA = 32 columns x kBlurTX rows of outputs; the rows it needs (with
-// the periodic halo of `rad` on both sides) are staged in shared memory.
+// the periodic halo of `rad` on both sides) are staged in shared memory sized
+// for this radius (dynamic), so small radii keep more CTAs per SM.
 __global__ void __launch_bounds__(256) k_blur_x(const float2* __restrict__ rho, float2* __restrict__ tmp,
                                                 const float* __restrict__ w, int rad, int rows, int cols,
                                                 int mod2_first, const PatState* __restrict__ stt) {
   if (stt[blockIdx.z].flags & 6) return;   // converged patterns keep their support
-  __shared__ float2 s[(kBlurTX + 2 * kBlurRadMax) * 32];
-  __shared__ float ws[2 * kBlurRadMax + 1];
+  extern __shared__ float2 s[];            // (kBlurTX + 2 rad) x 32, then the 2 rad + 1 weights
+  float* ws = reinterpret_cast<float*>(s + (kBlurTX + 2 * rad) * 32);
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   const int y = blockIdx.x * 32 + tx;
   const int x0 = blockIdx.y * kBlurTX;
@@ -205,66 +206,88 @@ __global__ void __launch_bounds__(256) k_blur_x(const float2* __restrict__ rho, 
   }
   __syncthreads();
   if (y >= cols) return;
-  for (int k = ty; k < kBlurTX && x0 + k < rows; k += 8) {
-    float sx = 0.f, sy = 0.f;
-    for (int d = 0; d <= 2 * rad; ++d) {
-      const float2 v = s[(k + d) * 32 + tx];
-      sx = fmaf(ws[d], v.x, sx);
-      sy = fmaf(ws[d], v.y, sy);
+  // 8 outputs per thread (rows ty, ty+8, ..., ty+56) accumulated together
+  float ax[8], ay[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) ax[q] = ay[q] = 0.f;
+  for (int d = 0; d <= 2 * rad; ++d) {
+    const float wd = ws[d];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const float2 v = s[(ty + 8 * q + d) * 32 + tx];
+      ax[q] = fmaf(wd, v.x, ax[q]);
+      ay[q] = fmaf(wd, v.y, ay[q]);
     }
-    tmp[blockIdx.z * npx + (long long)(x0 + k) * cols + y] = make_float2(sx, sy);
+  }
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const int k = ty + 8 * q;
+    if (x0 + k < rows) tmp[blockIdx.z * npx + (long long)(x0 + k) * cols + y] = make_float2(ax[q], ay[q]);
   }
 }
 
-// y pass: CTA = 256-column segments of rows blockIdx.y, +gridDim.y, ...; the
-// segment with its periodic halo is staged in shared memory.  Writes the
-// support field and per-CTA max / sum partials.
+// y pass: each warp filters whole 256-column row segments on its own (rows
+// blockIdx.y*8 + warp, stepping by gridDim.y*8), the segment and its periodic
+// halo staged in the warp's slice of shared memory; no block barrier in the
+// row loop.  Writes the support field and per-CTA max / sum partials.
 __global__ void __launch_bounds__(256) k_blur_y(const float2* __restrict__ tmp, float* __restrict__ spt,
                                                 const float* __restrict__ w, int rad, int rows, int cols,
                                                 int mod2_first, float s, float* __restrict__ pmax,
                                                 double* __restrict__ psum, const PatState* __restrict__ stt) {
   if (stt[blockIdx.z].flags & 6) return;
-  __shared__ float2 seg[256 + 2 * kBlurRadMax];
-  __shared__ float ws[2 * kBlurRadMax + 1];
+  extern __shared__ float2 seg_all[];      // 8 x (256 + 2 rad), then the weights
+  const int seglen = 256 + 2 * rad;
+  float* ws = reinterpret_cast<float*>(seg_all + 8 * seglen);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  float2* seg = seg_all + wid * seglen;
   const long long npx = (long long)rows * cols;
   const long long p = blockIdx.z;
   const float2* src = tmp + p * npx;
   float* out = spt + p * npx;
   for (int i = threadIdx.x; i <= 2 * rad; i += 256) ws[i] = w[i];
-  const int y0 = blockIdx.x * 256, y = y0 + threadIdx.x;
+  __syncthreads();
+  const int y0 = blockIdx.x * 256;
   float m = 0.f;   // findMax initialises with 0 (src/gpu/cub_wrap.cu:88-92)
   double acc = 0.0;
-  for (int r = blockIdx.y; r < rows; r += gridDim.y) {
-    __syncthreads();
-    for (int j = threadIdx.x; j < 256 + 2 * rad; j += 256)
-      seg[j] = src[(long long)r * cols + wrap(y0 - rad + j, cols)];
-    __syncthreads();
-    if (y < cols) {
-      float sx = 0.f, sy = 0.f;
-      for (int d = 0; d <= 2 * rad; ++d) {
-        const float2 v = seg[threadIdx.x + d];
-        sx = fmaf(ws[d], v.x, sx);
-        sy = fmaf(ws[d], v.y, sy);
+  for (int r = blockIdx.y * 8 + wid; r < rows; r += gridDim.y * 8) {
+    __syncwarp();
+    for (int j = lane; j < seglen; j += 32) seg[j] = src[(long long)r * cols + wrap(y0 - rad + j, cols)];
+    __syncwarp();
+    float ax[8], ay[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) ax[q] = ay[q] = 0.f;
+    for (int d = 0; d <= 2 * rad; ++d) {
+      const float wd = ws[d];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const float2 v = seg[lane + 32 * q + d];
+        ax[q] = fmaf(wd, v.x, ax[q]);
+        ay[q] = fmaf(wd, v.y, ay[q]);
       }
+    }
+    float racc = 0.f;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int y = y0 + lane + 32 * q;
+      if (y >= cols) continue;
       float o;
       if (mod2_first) {
-        o = sx;
+        o = ax[q];
       } else {
-        sx *= s;
-        sy *= s;
+        const float sx = ax[q] * s, sy = ay[q] * s;
         o = sx * sx + sy * sy;
       }
       out[(long long)r * cols + y] = o;
       m = fmaxf(m, o);   // a NaN input is dropped by fmaxf; the finaliser checks the sum
-      acc += (double)o;
+      racc += o;
     }
+    acc += (double)racc;
   }
   __shared__ float sm[32];
   __shared__ double sd[32];
   m = warp_max_f(m);
   acc = warp_sum_d(acc);
-  const int wid = threadIdx.x >> 5, ln = threadIdx.x & 31;
-  if (ln == 0) { sm[wid] = m; sd[wid] = acc; }
+  if (lane == 0) { sm[wid] = m; sd[wid] = acc; }
   __syncthreads();
   if (threadIdx.x == 0) {
     float mm = 0.f;
@@ -303,13 +326,15 @@ cudaError_t shrinkwrap(const float2* rho, float2* tmp, float* spt, const float* 
                        int rady, int rows, int cols, int batch, int mod2_first, float s, float* pmax, double* psum,
                        int nblk, PatState* stt, double shrink_threshold, cudaStream_t st) {
   if (radx > kBlurRadMax || rady > kBlurRadMax || radx < 0 || rady < 0) return cudaErrorInvalidValue;
-  k_blur_x<<<dim3((cols + 31) / 32, (rows + kBlurTX - 1) / kBlurTX, batch), 256, 0, st>>>(rho, tmp, wx, radx, rows,
-                                                                                          cols, mod2_first, stt);
-  // y pass: gx segments per row, gy row groups; gx*gy <= nblk partials per pattern
+  const size_t smx = sizeof(float2) * (kBlurTX + 2 * radx) * 32 + sizeof(float) * (2 * radx + 1);
+  k_blur_x<<<dim3((cols + 31) / 32, (rows + kBlurTX - 1) / kBlurTX, batch), 256, smx, st>>>(rho, tmp, wx, radx, rows,
+                                                                                            cols, mod2_first, stt);
+  // y pass: gx segments per row, gy groups of 8 rows; gx*gy <= nblk partials per pattern
   const int gx = (cols + 255) / 256;
-  const int gy = std::max(1, std::min(rows, nblk / gx));
+  const int gy = std::max(1, std::min((rows + 7) / 8, nblk / gx));
   if (gx * gy > nblk) return cudaErrorInvalidValue;
-  k_blur_y<<<dim3(gx, gy, batch), 256, 0, st>>>(tmp, spt, wy, rady, rows, cols, mod2_first, s, pmax, psum, stt);
+  const size_t smy = sizeof(float2) * 8 * (256 + 2 * rady) + sizeof(float) * (2 * rady + 1);
+  k_blur_y<<<dim3(gx, gy, batch), 256, smy, st>>>(tmp, spt, wy, rady, rows, cols, mod2_first, s, pmax, psum, stt);
   k_shrink_finalize<<<batch, 32, 0, st>>>(pmax, psum, gx * gy, stt, rows, cols, mod2_first, shrink_threshold);
   return cudaGetLastError();
 }
@@ -452,6 +477,12 @@ cudaError_t random_start(const float* inten, const float* bs, float bs_thr, floa
                          unsigned long long seed, cudaStream_t st) {
   k_random_start<<<grid1d(npx * batch, 256), 256, 0, st>>>(inten, bs, bs_thr, psi, npx, batch, seed);
   return cudaGetLastError();
+}
+
+cudaError_t misc_prepare() {
+  // the x pass of the largest radius needs more than the default 48 KB
+  const int smx = (int)(sizeof(float2) * (kBlurTX + 2 * kBlurRadMax) * 32 + sizeof(float) * (2 * kBlurRadMax + 1));
+  return cudaFuncSetAttribute(k_blur_x, cudaFuncAttributeMaxDynamicSharedMemorySize, smx);
 }
 
 }  // namespace cdx

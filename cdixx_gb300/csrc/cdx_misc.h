@@ -19,6 +19,8 @@ cudaError_t apply_support(float2* rho, const float2* rhop, const float* spt, flo
 cudaError_t rect_support(float* spt, int rows, int cols, int batch, int sx, int sy, int ex, int ey, cudaStream_t st);
 cudaError_t support_bits(const float* spt, const PatState* st_or_null, float fixed_thr, uint32_t* bits, int rows,
                          int cols, int batch, cudaStream_t st);
+// Kernel attributes of the stencil kernels (once per device, outside capture).
+cudaError_t misc_prepare();
 cudaError_t shrinkwrap(const float2* rho, float2* tmp, float* spt, const float* wx, int radx, const float* wy,
                        int rady, int rows, int cols, int batch, int mod2_first, float s, float* pmax, double* psum,
                        int nblk, PatState* stt, double shrink_threshold, cudaStream_t st);
