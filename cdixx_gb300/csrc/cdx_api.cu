@@ -147,29 +147,52 @@ struct SwPlan {
 
 // Periodic kernel equal to the inverse DFT of the sampled frequency Gaussian
 // exp(-f^2/(2 sf^2)) (f in FFT order) that applyGaussMult multiplies Psi by
-// (src/gpu/cudaConfig.cu:380-395); truncated where it falls below 1e-10 of
-// its peak.
+// (src/gpu/cudaConfig.cu:380-395); truncated at the smallest radius whose
+// dropped tail holds at most 2e-8 of the kernel's absolute mass (below float32
+// resolution of the blurred field), at most 64.  The Gaussian is cut at the
+// Nyquist frequency, so the kernel rings: a pointwise 1e-10 cut would need
+// r = 50 at sigma = 3 where this one needs 12.
 void fourier_kernel(int n, double sf, std::vector<float>& w, int& off, int& rad) {
-  const int mmax = std::min(n - 1, 64);   // the kernel is far below 1e-10 of its peak by then
-  std::vector<double> k(mmax + 1), ct(n), g(n);
-  const double two_pi = 6.283185307179586476925286766559;
-  for (int t = 0; t < n; ++t) ct[t] = std::cos(two_pi * (double)t / n);
-  for (int f = 0; f < n; ++f) {
-    const int fr = f >= n / 2 ? f - n : f;
-    g[f] = std::exp(-(double)fr * fr / (2.0 * sf * sf));
+  // the sigma schedule repeats every run: cache the truncated kernel per (n, sf)
+  static std::mutex mu;
+  static std::map<std::pair<int, double>, std::vector<float>> cache;
+  std::vector<float> taps;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find({n, sf});
+    if (it != cache.end()) taps = it->second;
   }
-  for (int m = 0; m <= mmax; ++m) {
-    double s = 0.0;
-    for (int f = 0; f < n; ++f) s += g[f] * ct[(int)(((long long)f * m) % n)];
-    k[m] = s / n;
+  if (taps.empty()) {
+    const int half = n / 2;
+    std::vector<double> k(half + 1), ct(n), g(n);
+    const double two_pi = 6.283185307179586476925286766559;
+    for (int t = 0; t < n; ++t) ct[t] = std::cos(two_pi * (double)t / n);
+    for (int f = 0; f < n; ++f) {
+      const int fr = f >= n / 2 ? f - n : f;
+      g[f] = std::exp(-(double)fr * fr / (2.0 * sf * sf));
+    }
+    for (int m = 0; m <= half; ++m) {
+      double s = 0.0;
+      for (int f = 0; f < n; ++f) s += g[f] * ct[(int)(((long long)f * m) % n)];
+      k[m] = s / n;
+    }
+    // absolute mass of the whole periodic kernel (k is even: k[m] = k[n - m])
+    double total = 0.0;
+    for (int m = 0; m < n; ++m) total += std::fabs(k[m <= half ? m : n - m]);
+    const int rmax = std::min((n - 1) / 2, 64);
+    double kept = std::fabs(k[0]);
+    int r = 0;
+    while (r < rmax && total - kept > 2e-8 * total) {
+      ++r;
+      kept += 2.0 * std::fabs(k[r]);
+    }
+    for (int d = -r; d <= r; ++d) taps.push_back((float)k[d < 0 ? -d : d]);
+    std::lock_guard<std::mutex> lk(mu);
+    cache[{n, sf}] = taps;
   }
-  int r = 0;
-  const int rmax = std::min((n - 1) / 2, mmax);
-  while (r < rmax && std::fabs(k[r + 1]) > 1e-10 * std::fabs(k[0])) ++r;
   off = (int)w.size();
-  rad = r;
-  // the kernel is even in m (G is even up to its f = -n/2 sample)
-  for (int d = -r; d <= r; ++d) w.push_back((float)k[d < 0 ? -d : d]);
+  rad = ((int)taps.size() - 1) / 2;
+  w.insert(w.end(), taps.begin(), taps.end());
 }
 
 // Normalised sampled Gaussian of width sigma px, radius floor(6 sigma)/2 as
