@@ -74,6 +74,7 @@ void CDI::allocateMem() {   // cdi.cc:42-61
   p.sigma0 = (float)sigma0;
   p.sigma_min = (float)sigmaMin;
   p.sigma_decay = (float)sigmaDecay;
+  p.prtf_iter = prtfIter;   // readConfig default 1000, as the reference
   check(cdx_create(&p, nullptr, &ctx_), "allocateMem");
   float* pd = nullptr;
   void* pw = nullptr;
@@ -135,6 +136,18 @@ void CDI::readObjectWave() {
   const double n = (double)row * column;
   for (size_t i = 0; i < pat.size(); ++i)
     pat[i] = (float)(((double)obj[2 * i] * obj[2 * i] + (double)obj[2 * i + 1] * obj[2 * i + 1]) / n);
+  if (simCCDbit) {
+    // detector quantisation and dark noise (applyPoissonNoise_WO, cdi.cc:191-193)
+    void* dp = nullptr;
+    if (cudaMalloc(&dp, pat.size() * sizeof(float)) != cudaSuccess) check(CDX_ERR_NOMEM, "readObjectWave");
+    cudaMemcpy(dp, pat.data(), pat.size() * sizeof(float), cudaMemcpyHostToDevice);
+    const float ex = exposure > 0 ? (float)exposure : 1.f;
+    check(cdx_ccd_noise((float*)dp, (long long)pat.size(), (float)noiseLevel, ex, 65535 /* rcolor, format.hpp:20 */,
+                        seed_, nullptr),
+          "readObjectWave");
+    cudaMemcpy(pat.data(), dp, pat.size() * sizeof(float), cudaMemcpyDeviceToHost);
+    cudaFree(dp);
+  }
   check(cdx_set_pattern(ctx_, 0, pat.data(), CDX_HOST, CDX_FFT_ORDER, 1.f), "readObjectWave");
 }
 
@@ -276,6 +289,14 @@ complexFormat* CDI::phaseRetrieve() {   // cdi.cc:297-449
   residual = (Real)stats_.residual;
   printf("residual= %f\n", residual);
   if (stats_.flags & 1) printf("max is ~0 or NaN at a shrinkwrap\n");
+  // prtf.txt (cdi.cc:436-440) when the run reached prtfIter
+  std::vector<float> prtf(row / 2);
+  if (cdx_get_prtf(ctx_, 0, prtf.data(), CDX_HOST) == CDX_OK) {
+    if (FILE* f = fopen("prtf.txt", "w")) {
+      for (int i = 0; i < row / 2; ++i) fprintf(f, "%d, %f\n", i, prtf[i]);
+      fclose(f);
+    }
+  }
   return patternWave;
 }
 

@@ -102,6 +102,16 @@ struct cdx_ctx {
   bool psi_in_work = false;   // psi holds Psi0 and W nothing yet: the next iteration starts from psi
   int sx = 0, sy = 0, ex = 0, ey = 0;
 
+  // PRTF (prtf_iter >= 0): projected Psi, rho' = IFFT(P_M Psi)/N, the ER cache,
+  // gamma0, the phasor sum, the prtfIter mask; polar sums [batch][2][rows/2]
+  float2 *pr_psi = nullptr, *pr_rhop = nullptr, *pr_cache = nullptr, *pr_gamma0 = nullptr, *pr_map = nullptr;
+  float* pr_mask = nullptr;
+  float* pr_polar = nullptr;
+  double* pr_part = nullptr;
+  PrtfState* pr_state = nullptr;
+  bool pr_valid = false;       // the last run reached prtf_iter
+  bool pr_reached = false;     // set while enqueueing
+
   // graph cache
   std::string gkey;
   cudaGraphExec_t gexec = nullptr;
@@ -226,7 +236,7 @@ void plan_shrinkwrap(const cdx_ctx* c, int count, SwPlan& P) {
   }
 }
 
-int col_iter(cdx_ctx* c, bool from_psi, bool rf) {
+int col_iter(cdx_ctx* c, bool from_psi, bool rf, float2* psi_proj = nullptr) {
   ColArgs a{};
   // the first iteration after a restart reads Psi0 (row-major) from psi
   a.in = from_psi ? c->psi : c->work;
@@ -235,7 +245,8 @@ int col_iter(cdx_ctx* c, bool from_psi, bool rf) {
   a.out = c->work;
   a.out_tiled = 1;
   a.out_stride = c->wstride;
-  a.psi_out = nullptr;
+  a.psi_out = psi_proj;
+  a.psi_stride = c->npx;
   a.amp = c->amp_t;
   a.inten = c->inten_t;
   a.bs = c->bs_t;
@@ -320,8 +331,12 @@ int enqueue_run(cdx_ctx* c, const std::vector<int>& steps, const SwPlan& sw, boo
   CDX_CK(scale_complex(c->rho, (float)(1.0 / std::sqrt((double)c->rows * c->cols)), n_all, c->st));
   ++nl;
   bool from_psi = psi_in_work;
-  int it = 0, swi = 0;
+  int it = 0, swi = 0, step = -1;
+  const bool prtf = c->pr_map && c->p.prtf_iter >= 0;
+  c->pr_reached = false;
+  if (prtf) CDX_CK(cudaMemsetAsync(c->pr_map, 0, sizeof(float2) * n_all, c->st));
   for (int a : steps) {
+    ++step;   // phaseRetrieve's iter: every step, shrinkwraps included
     if (a == ALGO_SHRINKWRAP) {
       const bool m2 = c->p.shrink_mode == CDX_SHRINK_SPATIAL;
       CDX_CK(shrinkwrap(c->rho, c->tmp, c->spt, c->weights + sw.offx[swi], sw.radx[swi], c->weights + sw.offy[swi],
@@ -334,14 +349,39 @@ int enqueue_run(cdx_ctx* c, const std::vector<int>& steps, const SwPlan& sw, boo
     }
     // from iteration 1 on: the restart iterate has the measured modulus by construction
     const bool rf = c->p.rf_every > 0 && it > 0 && (it % c->p.rf_every) == 0;
-    int e = col_iter(c, from_psi, rf);
+    const bool pstep = prtf && step >= c->p.prtf_iter;
+    int e = col_iter(c, from_psi, rf, pstep ? c->pr_psi : nullptr);
     if (e) return e;
     if (rf) CDX_CK(rfactor_from_partials(c->part, c->col_blocks, c->batch, c->dstate, c->p.stop_rfactor, it, c->st));
     e = row_iter(c, a);
     if (e) return e;
     nl += rf ? 3 : 2;
+    if (pstep) {
+      // cdi.cc:355-380: rho' = IFFT(P_M Psi)/N, the ER correlation with gamma0, its
+      // phase, and the phasor accumulation of P_M Psi
+      const bool first = step == c->p.prtf_iter;
+      e = fft2_enqueue(c->pr_psi, c->pr_rhop, c->rows, c->cols, c->batch, true,
+                       (float)(1.0 / ((double)c->rows * c->cols)), c->tw_r, c->tw_c, c->st);
+      if (e) return e;
+      CDX_CK(prtf_step(c->pr_rhop, c->mask, c->rows, c->cols, c->batch, c->pr_cache, c->pr_gamma0, first, c->pr_part,
+                       kRedBlocks, c->pr_state, c->dstate, c->st));
+      CDX_CK(prtf_accum(c->pr_psi, c->pr_map, first ? c->pr_mask : nullptr, c->npx, c->batch, c->pr_state, c->dstate,
+                        c->st));
+      if (first) {
+        CDX_CK(prtf_polar(c->pr_mask, nullptr, 1.f, c->rows, c->cols, c->batch, c->pr_polar, c->st));
+        c->pr_reached = true;
+      }
+      nl += first ? 6 : 5;
+    }
     from_psi = false;
     ++it;
+  }
+  if (prtf && c->pr_reached) {
+    // |prtf_map| / (iter - prtfIter), polar sums (cdi.cc:424-433)
+    const float inv = (float)(1.0 / ((double)(step + 1) - c->p.prtf_iter));
+    CDX_CK(prtf_polar(nullptr, c->pr_map, inv, c->rows, c->cols, c->batch, c->pr_polar + c->batch * (c->rows / 2),
+                      c->st));
+    ++nl;
   }
   // final Psi = FFT(rho): W holds rowFFT(rho); with no iteration psi still holds Psi0
   if (!(it == 0 && psi_in_work)) {
@@ -439,6 +479,7 @@ int run_impl(cdx_ctx* c, const char* algorithm) {
     CDX_CK(cudaEventRecord(c->ev1, c->st));
   }
   if (c->last_iters > 0) c->psi_in_work = false;
+  c->pr_valid = c->pr_reached;
   c->fresh.assign(c->batch, 0);
   return CDX_OK;
 }
@@ -502,6 +543,7 @@ int group_run_impl(cdx_group* g, const char* algorithm, double* gpu_ms) {
   CDX_CK(cudaStreamSynchronize(g->st));
   for (cdx_ctx* c : g->ctxs) {
     if (c->last_iters > 0) c->psi_in_work = false;
+    c->pr_valid = c->pr_reached;
     c->fresh.assign(c->batch, 0);
   }
   if (gpu_ms) {
@@ -553,6 +595,7 @@ int cdx_params_default(cdx_params* p) {
   p->sigma_decay = 0.99f;      // cdi.cc:339
   p->use_graph = 1;
   p->rf_every = 0;
+  p->prtf_iter = -1;
   return CDX_OK;
 }
 
@@ -646,6 +689,24 @@ int cdx_create(const cdx_params* p, void* stream, cdx_ctx** out) {
     return fail(set_error(CDX_ERR_CUDA, "state init failed"));
   rect_of(c);
   if ((e = reset_support(c, 0, c->batch))) return fail(e);
+  if (p->prtf_iter >= 0) {
+    const size_t nb = (size_t)c->batch * c->npx;
+    bool ok = cudaMalloc(&c->pr_psi, sizeof(float2) * nb) == cudaSuccess &&
+              cudaMalloc(&c->pr_rhop, sizeof(float2) * nb) == cudaSuccess &&
+              cudaMalloc(&c->pr_cache, sizeof(float2) * nb) == cudaSuccess &&
+              cudaMalloc(&c->pr_gamma0, sizeof(float2) * nb) == cudaSuccess &&
+              cudaMalloc(&c->pr_map, sizeof(float2) * nb) == cudaSuccess &&
+              cudaMalloc(&c->pr_mask, sizeof(float) * nb) == cudaSuccess &&
+              cudaMalloc(&c->pr_polar, sizeof(float) * 2 * c->batch * (c->rows / 2 + 1)) == cudaSuccess &&
+              cudaMalloc(&c->pr_part, sizeof(double) * 2 * c->batch * kRedBlocks) == cudaSuccess &&
+              cudaMalloc(&c->pr_state, sizeof(PrtfState) * c->batch) == cudaSuccess;
+    if (!ok) return fail(set_error(CDX_ERR_NOMEM, "PRTF buffers"));
+    // the reference's cache and gamma0 come from its pool uncleared; here they start at zero
+    ok = cudaMemsetAsync(c->pr_cache, 0, sizeof(float2) * nb, c->st) == cudaSuccess &&
+         cudaMemsetAsync(c->pr_gamma0, 0, sizeof(float2) * nb, c->st) == cudaSuccess &&
+         cudaMemsetAsync(c->pr_state, 0, sizeof(PrtfState) * c->batch, c->st) == cudaSuccess;
+    if (!ok) return fail(set_error(CDX_ERR_CUDA, "PRTF buffer clear"));
+  }
   if (cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess)
     return fail(set_error(CDX_ERR_CUDA, "event create failed"));
   if (cudaStreamSynchronize(c->st) != cudaSuccess)
@@ -662,10 +723,28 @@ int cdx_destroy(cdx_ctx* c) {
   if (c->bs) cudaFree(c->bs);
   if (c->bs_t) cudaFree(c->bs_t);
   if (c->arena) cudaFree(c->arena);
+  for (void* q : {(void*)c->pr_psi, (void*)c->pr_rhop, (void*)c->pr_cache, (void*)c->pr_gamma0, (void*)c->pr_map,
+                  (void*)c->pr_mask, (void*)c->pr_polar, (void*)c->pr_part, (void*)c->pr_state})
+    if (q) cudaFree(q);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->own_stream && c->st) cudaStreamDestroy(c->st);
   delete c;
+  return CDX_OK;
+}
+
+int cdx_get_prtf(cdx_ctx* c, int idx, float* out, int where) {
+  if (!c || !out || idx < 0 || idx >= c->batch) return set_error(CDX_ERR_ARG, "bad PRTF argument");
+  if (!c->pr_polar || !c->pr_valid) return set_error(CDX_ERR_STATE, "no PRTF: prtf_iter off or not reached");
+  const int h = c->rows / 2;
+  std::vector<float> w(h), v(h);
+  CDX_CK(cudaMemcpyAsync(w.data(), c->pr_polar + (size_t)idx * h, sizeof(float) * h, cudaMemcpyDeviceToHost, c->st));
+  CDX_CK(cudaMemcpyAsync(v.data(), c->pr_polar + (size_t)(c->batch + idx) * h, sizeof(float) * h,
+                         cudaMemcpyDeviceToHost, c->st));
+  CDX_CK(cudaStreamSynchronize(c->st));
+  for (int i = 0; i < h; ++i) v[i] = v[i] / w[i];   // prtf[i]/weights[i] (cdi.cc:437-439)
+  if (where == CDX_DEVICE) CDX_CK(cudaMemcpy(out, v.data(), sizeof(float) * h, cudaMemcpyHostToDevice));
+  else memcpy(out, v.data(), sizeof(float) * h);
   return CDX_OK;
 }
 

@@ -153,6 +153,17 @@ __global__ void k_intensity(const float2* __restrict__ F, const double* __restri
   }
 }
 
+// applyPoissonNoise_WO (src/gpu/cdi.cu:291-296) with scale = vars.scale =
+// 1/exposure (init_cuda_image, cdi.cc:52): the pattern quantised to detector
+// counts, plus zero-mean Poisson(noise_level) dark noise per pixel.
+__global__ void k_ccd_noise(float* __restrict__ I, long long n, double noise_level, float scale, float rcolor,
+                            unsigned long long seed) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double k = poisson_sample(noise_level, seed, 0x43434431ull, (unsigned long long)i);
+    I[i] = scale * ((float)(int)(I[i] * rcolor / scale) + (float)k - (float)noise_level) / rcolor;
+  }
+}
+
 }  // namespace fm
 }  // namespace cdx
 
@@ -196,5 +207,18 @@ extern "C" int cdx_forward_model(int n, int count, unsigned long long seed, long
   cudaFree(prm);
   cudaFree(sum);
   cudaFree(rho);
+  return CDX_OK;
+}
+
+extern "C" int cdx_ccd_noise(float* pattern, long long count, float noise_level, float exposure, int rcolor,
+                             unsigned long long seed, void* stream) {
+  if (!pattern || count < 0 || !(noise_level >= 0.f) || !(exposure > 0.f) || rcolor <= 0)
+    return set_error(CDX_ERR_ARG, "bad CCD-noise argument");
+  if (count == 0) return CDX_OK;
+  const int g = (int)std::min<long long>((count + 255) / 256, 152 * 32);
+  k_ccd_noise<<<g, 256, 0, (cudaStream_t)stream>>>(pattern, count, (double)noise_level, 1.f / exposure, (float)rcolor,
+                                                    seed);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return set_error(CDX_ERR_CUDA, std::string("ccd noise: ") + cudaGetErrorString(e));
   return CDX_OK;
 }

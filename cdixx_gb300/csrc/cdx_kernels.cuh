@@ -327,12 +327,12 @@ __global__ void __launch_bounds__(Geom<N>::T, (TC && Geom<N>::MINB > 2) ? 2 : Ge
       const int r = t >> LL, l = t & (L - 1);
       if (l < ncols) {
         float2 s = buf[G::idx(l, r)];
-        if (a.psi_out) a.psi_out[(long long)blockIdx.y * a.psi_stride + r * C + c0 + l] = s;
         const float amp = amp_s[t];
         if (a.rf_partials) rsum += fabsf(hypotf(s.x, s.y) - amp);
         if (a.proj == PROJ_MODABS) s = proj_modabs(s, amp);
         else s = proj_ccd(s, int_s[t], a.bs ? bs_s[t] : 0.f, a.bs != nullptr,
                           a.noise_level, a.ccd_scale, a.ccd_rcolor);
+        if (a.psi_out) a.psi_out[(long long)blockIdx.y * a.psi_stride + r * C + c0 + l] = s;
         buf[G::idx(l, r)] = s;
       }
     }

@@ -485,4 +485,154 @@ cudaError_t misc_prepare() {
   return cudaFuncSetAttribute(k_blur_x, cudaFuncAttributeMaxDynamicSharedMemorySize, smx);
 }
 
+// ---------------------------------------------------------------------- PRTF
+// One PRTF step per pattern (cdi.cc:355-380): with the ER update of
+// applySupport (inside: x + 1.9 (rho' - x), outside: 0),
+//   first step:  gamma0 = ER(0, rho'), cache = gamma0 * gamma0
+//   later steps: cache = ER(cache, rho') * conj(gamma0)
+// and the complex sum of cache (fixed-order partials per CTA, then per pattern):
+// phi0 = -arg(sum)/2 at the first step, theta = phi0 + arg(sum) afterwards.
+__global__ void k_prtf_step(const float2* __restrict__ rhop, const uint32_t* __restrict__ bits, int rows, int cols,
+                            float2* __restrict__ cache, float2* __restrict__ gamma0, int first,
+                            double* __restrict__ part, int nblk, const PatState* __restrict__ stt) {
+  const long long p = blockIdx.y;
+  const long long npx = (long long)rows * cols;
+  const int wpr = (cols + 31) >> 5;
+  double sr = 0.0, si = 0.0;
+  if (!(stt[p].flags & 4)) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npx; i += (long long)nblk * blockDim.x) {
+      const long long g = p * npx + i;
+      const int r = (int)(i / cols), c = (int)(i - (long long)r * cols);
+      const bool inside = (bits[p * rows * wpr + (long long)r * wpr + (c >> 5)] >> (c & 31)) & 1u;
+      const float2 q = rhop[g];
+      float2 v;
+      if (first) {
+        const float2 g0 = inside ? make_float2(relax19(0.f, q.x), relax19(0.f, q.y)) : make_float2(0.f, 0.f);
+        gamma0[g] = g0;
+        v = cmul(g0, g0);
+      } else {
+        const float2 x = cache[g];
+        const float2 e = inside ? make_float2(relax19(x.x, q.x), relax19(x.y, q.y)) : make_float2(0.f, 0.f);
+        const float2 g0 = gamma0[g];
+        v = cmul(e, make_float2(g0.x, -g0.y));
+      }
+      cache[g] = v;
+      sr += v.x;
+      si += v.y;
+    }
+  }
+  __shared__ double rr[8], ri[8];
+  sr = warp_sum_d(sr);
+  si = warp_sum_d(si);
+  if ((threadIdx.x & 31) == 0) { rr[threadIdx.x >> 5] = sr; ri[threadIdx.x >> 5] = si; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { a += rr[w]; b += ri[w]; }
+    part[(p * nblk + blockIdx.x) * 2] = a;
+    part[(p * nblk + blockIdx.x) * 2 + 1] = b;
+  }
+}
+
+__global__ void k_prtf_phase(const double* __restrict__ part, int nblk, PrtfState* __restrict__ ps, int first) {
+  const int p = blockIdx.x;
+  if (threadIdx.x != 0) return;
+  double a = 0.0, b = 0.0;
+  for (int i = 0; i < nblk; ++i) { a += part[(p * nblk + i) * 2]; b += part[(p * nblk + i) * 2 + 1]; }
+  // findSum returns a float complex; phi0 and phi are Real (float) in phaseRetrieve
+  const float ang = atan2f((float)b, (float)a);
+  if (first) {
+    ps[p].phi0 = -ang / 2;
+    ps[p].theta = ps[p].phi0;
+  } else {
+    ps[p].theta = ps[p].phi0 + ang;
+  }
+}
+
+cudaError_t prtf_step(const float2* rhop, const uint32_t* bits, int rows, int cols, int batch, float2* cache,
+                      float2* gamma0, int first, double* part, int nblk, PrtfState* ps, const PatState* stt,
+                      cudaStream_t st) {
+  k_prtf_step<<<dim3(nblk, batch), 256, 0, st>>>(rhop, bits, rows, cols, cache, gamma0, first, part, nblk, stt);
+  k_prtf_phase<<<batch, 32, 0, st>>>(part, nblk, ps, first);
+  return cudaGetLastError();
+}
+
+// addPhase (src/gpu/cudaConfig.cu:876-887): map += (b/|b|) e^{i theta} where
+// |b| > 1e-6; on the first step also the |b| > 1e-6 mask (bitMap, cdi.cc:363).
+__global__ void k_prtf_accum(const float2* __restrict__ b, float2* __restrict__ map, float* __restrict__ mask,
+                             long long npx, int batch, const PrtfState* __restrict__ ps,
+                             const PatState* __restrict__ stt) {
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < npx * batch;
+       g += (long long)gridDim.x * blockDim.x) {
+    const long long p = g / npx;
+    if (stt[p].flags & 4) continue;
+    const float2 v = b[g];
+    const float mod = hypotf(v.x, v.y);
+    if (mask) mask[g] = mod > 1e-6f ? 1.f : 0.f;
+    if (mod > 1e-6f) {
+      const float r = v.x / mod, i = v.y / mod;
+      float s, c;
+      sincosf(ps[p].theta, &s, &c);
+      float2 m = map[g];
+      m.x += r * c - i * s;
+      m.y += r * s + i * c;
+      map[g] = m;
+    }
+  }
+}
+
+cudaError_t prtf_accum(const float2* psi_proj, float2* map, float* mask_or_null, long long npx, int batch,
+                       const PrtfState* ps, const PatState* stt, cudaStream_t st) {
+  k_prtf_accum<<<grid1d(npx * batch, 256), 256, 0, st>>>(psi_proj, map, mask_or_null, npx, batch, ps, stt);
+  return cudaGetLastError();
+}
+
+// cart2polar_kernel + edgeReduce on the centred image (cudaConvertFO of the
+// FFT-order field): for radius r < rows/2, the sum over 2*cols angles, in
+// angle order and in float like edgeReduce, of the bilinear sample at
+// (r cos t, r sin t) about the centre (rows/2, cols/2).  The image is the
+// mask (float) or |map| * inv_count.
+__device__ __forceinline__ float prtf_pixel(const float* mask, const float2* map, float inv_count, int rows, int cols,
+                                            int x, int y) {
+  const int fx = (x + (rows >> 1)) % rows, fy = (y + (cols >> 1)) % cols;   // centred -> FFT order
+  const long long i = (long long)fx * cols + fy;
+  if (mask) return mask[i];
+  const float2 m = map[i];
+  return hypotf(m.x, m.y) * inv_count;
+}
+__global__ void k_prtf_polar(const float* __restrict__ mask, const float2* __restrict__ map, float inv_count,
+                             int rows, int cols, float* __restrict__ out) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const long long p = blockIdx.y;
+  if (r >= (rows >> 1)) return;
+  const long long npx = (long long)rows * cols;
+  const float* mk = mask ? mask + p * npx : nullptr;
+  const float2* mp = map ? map + p * npx : nullptr;
+  const int nang = cols << 1;
+  float acc = 0.f;
+  for (int a = 0; a < nang; ++a) {
+    float s, c;
+    sincosf((float)(a * (2.0 * 3.14159265358979323846 / nang)), &s, &c);   // x * (2.0f*M_PI/cuda_row): double
+    float x = r * c + (rows >> 1), y = r * s + (cols >> 1);
+    const int x0 = (int)floorf(x), y0 = (int)floorf(y);
+    const float fx = x - x0, fy = y - y0;
+    float v = 0.f;
+    if (!(x0 < 0 || x0 + 1 >= rows || y0 < 0 || y0 + 1 >= cols)) {
+      const float v00 = prtf_pixel(mk, mp, inv_count, rows, cols, x0, y0);
+      const float v01 = prtf_pixel(mk, mp, inv_count, rows, cols, x0, y0 + 1);
+      const float v10 = prtf_pixel(mk, mp, inv_count, rows, cols, x0 + 1, y0);
+      const float v11 = prtf_pixel(mk, mp, inv_count, rows, cols, x0 + 1, y0 + 1);
+      v = (1 - fx) * (1 - fy) * v00 + (1 - fx) * fy * v01 + fx * (1 - fy) * v10 + fx * fy * v11;
+    }
+    acc += v;
+  }
+  out[p * (rows >> 1) + r] = acc;
+}
+
+cudaError_t prtf_polar(const float* mask, const float2* map, float inv_count, int rows, int cols, int batch,
+                       float* out, cudaStream_t st) {
+  k_prtf_polar<<<dim3(((rows >> 1) + 127) / 128, batch), 128, 0, st>>>(mask, map, inv_count, rows, cols, out);
+  return cudaGetLastError();
+}
+
 }  // namespace cdx

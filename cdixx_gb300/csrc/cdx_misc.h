@@ -37,4 +37,14 @@ cudaError_t state_init(PatState* stt, int batch, float thr, cudaStream_t st);
 cudaError_t random_start(const float* inten, const float* bs, float bs_thr, float2* psi, long long npx, int batch,
                          unsigned long long seed, cudaStream_t st);
 
+// PRTF (src/post_gpu/cdi.cc:355-380, 424-440): one step's ER-correlation and
+// phase, the phasor accumulation, and the polar sums of cart2polar_kernel +
+// edgeReduce (src/gpu/cudaConfig.cu:1027-1063).
+cudaError_t prtf_step(const float2* rhop, const uint32_t* bits, int rows, int cols, int batch, float2* cache,
+                      float2* gamma0, int first, double* part, int nblk, PrtfState* ps, const PatState* stt,
+                      cudaStream_t st);
+cudaError_t prtf_accum(const float2* psi_proj, float2* map, float* mask_or_null, long long npx, int batch,
+                       const PrtfState* ps, const PatState* stt, cudaStream_t st);
+cudaError_t prtf_polar(const float* mask, const float2* map, float inv_count, int rows, int cols, int batch,
+                       float* out, cudaStream_t st);
 }  // namespace cdx

@@ -297,19 +297,9 @@ __global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_COL) col_pass_rk(Co
   } else {
     cp_wait<0>();
     __syncthreads();
-    // Psi complete in registers: optional copy-out and R-factor partial (each
-    // one loop behind one uniform branch), then the projection (branch-free
-    // per element, so the compiler interleaves the elements)
-    if (a.psi_out) {
-      float2* psi_out = a.psi_out + (long long)blockIdx.y * a.psi_stride;
-#pragma unroll
-      for (int b = 0; b < FL::B; ++b) {
-        int l, j;
-        if (!bfly_of<N, FL::R>(b, 0, l, j) || l >= ncols) continue;
-#pragma unroll
-        for (int r = 0; r < FL::R; ++r) psi_out[(j + r * FL::NS) * C + c0 + l] = v[b][r];
-      }
-    }
+    // Psi complete in registers: optional R-factor partial (one loop behind
+    // one uniform branch), then the projection (branch-free per element, so
+    // the compiler interleaves the elements), then the optional copy-out of P_M Psi
     if (a.rf_partials) {
       double rsum = 0.0;
 #pragma unroll
@@ -337,6 +327,16 @@ __global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_COL) col_pass_rk(Co
         else z = proj_ccd(z, int_s[t], a.bs ? bs_s[t] : 0.f, a.bs != nullptr, a.noise_level, a.ccd_scale,
                           a.ccd_rcolor);
         v[b][r] = l < ncols ? z : make_float2(0.f, 0.f);
+      }
+    }
+    if (a.psi_out) {
+      float2* psi_out = a.psi_out + (long long)blockIdx.y * a.psi_stride;
+#pragma unroll
+      for (int b = 0; b < FL::B; ++b) {
+        int l, j;
+        if (!bfly_of<N, FL::R>(b, 0, l, j) || l >= ncols) continue;
+#pragma unroll
+        for (int r = 0; r < FL::R; ++r) psi_out[(j + r * FL::NS) * C + c0 + l] = v[b][r];
       }
     }
     float2 o[IL::B][IL::R];

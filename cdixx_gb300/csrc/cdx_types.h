@@ -36,6 +36,12 @@ struct PatState {
   int conv_iter;     // iterations run when the pattern froze (-1: never)
 };
 
+// Per-pattern PRTF state (phaseRetrieve's phi0 and the phase of the current step).
+struct PrtfState {
+  float phi0;        // -arg(sum gamma0^2)/2 at prtfIter
+  float theta;       // phase added to this step's P_M Psi
+};
+
 struct RowArgs {
   const float2* in;        // rows to load
   float2* out;             // rows to store (may alias in when the layouts match)
@@ -62,7 +68,7 @@ struct RowArgs {
 struct ColArgs {
   const float2* in;        // columns to load
   float2* out;             // columns to store (may alias in when the layouts match)
-  float2* psi_out;         // COL_ITER: optional row-major copy of Psi before the projection
+  float2* psi_out;         // COL_ITER: optional row-major copy of P_M(Psi), the projected Psi
   const float* amp;        // sqrt(max(I,0)), column-tiled (width = the kernel's L)
   const float* inten;      // I, column-tiled (PROJ_CCD)
   const float* bs;         // beamstop, column-tiled (PROJ_CCD), may be null

@@ -37,7 +37,7 @@ class Params(ctypes.Structure):
         ("rcolor", ctypes.c_int), ("sim_ccd_bit", ctypes.c_int), ("noise_level", ctypes.c_int),
         ("shrink_mode", ctypes.c_int), ("sigma0", ctypes.c_float), ("sigma_min", ctypes.c_float),
         ("sigma_decay", ctypes.c_float), ("use_graph", ctypes.c_int), ("rf_every", ctypes.c_int),
-        ("stop_rfactor", ctypes.c_float), ("fft_mode", ctypes.c_int),
+        ("stop_rfactor", ctypes.c_float), ("fft_mode", ctypes.c_int), ("prtf_iter", ctypes.c_int),
     ]
 
 
@@ -78,10 +78,12 @@ _SIGS = {
     "cdx_get_object": [_P, _I, _P, _I],
     "cdx_get_fourier": [_P, _I, _P, _I],
     "cdx_get_support": [_P, _I, _P, _I],
+    "cdx_get_prtf": [_P, _I, _P, _I],
     "cdx_phase_retrieve_host": [ctypes.POINTER(Params), ctypes.c_char_p, _P, _P, ctypes.c_ulonglong,
                                 _P, _P, _P, ctypes.POINTER(Stats)],
     "cdx_fft2": [_P, _P, _I, _I, _I, _I, _P],
     "cdx_fft2_ex": [_P, _P, _I, _I, _I, _I, _I, _P],
+    "cdx_ccd_noise": [_P, _LL, _F, _F, _I, ctypes.c_ulonglong, _P],
     "cdx_apply_mod_abs": [_P, _P, _LL, _P],
     "cdx_apply_mod": [_P, _P, _P, _I, _F, _I, _LL, _P],
     "cdx_apply_support": [_P, _P, _P, _F, _F, _I, _LL, _P],
@@ -266,6 +268,12 @@ class Context:
     def get_support(self, idx=0, out=None):
         return self._get(lib().cdx_get_support, idx, False, out)
 
+    def get_prtf(self, idx=0):
+        """PRTF of the last run: rows/2 floats (the prtf.txt column)."""
+        a = np.empty(self.rows // 2, np.float32)
+        check(lib().cdx_get_prtf(self._h, idx, a.ctypes.data_as(ctypes.c_void_p), CDX_HOST))
+        return a
+
     def device_arrays(self):
         ptrs = [ctypes.c_void_p() for _ in range(4)]
         check(lib().cdx_device_arrays(self._h, *[ctypes.byref(p) for p in ptrs]))
@@ -330,6 +338,13 @@ def fft2(x, out, inverse=False, stream=None, fft_mode=0):
     check(lib().cdx_fft2_ex(ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(out.data_ptr()), rows, cols, batch,
                             int(inverse), int(fft_mode), _stream_ptr(stream)))
     return out
+
+
+def ccd_noise(pattern, noise_level, exposure=1.0, rcolor=65535, seed=0, stream=None):
+    """applyPoissonNoise_WO on a device float tensor, in place."""
+    check(lib().cdx_ccd_noise(ctypes.c_void_p(pattern.data_ptr()), pattern.numel(), noise_level, exposure, rcolor,
+                              ctypes.c_ulonglong(seed), _stream_ptr(stream)))
+    return pattern
 
 
 def apply_mod_abs(psi, intensity, stream=None):

@@ -67,6 +67,8 @@ typedef struct cdx_params {
   float stop_rfactor;        /* with rf_every > 0: a pattern whose R-factor <= stop_rfactor finishes its
                                 iteration and then freezes (its kernels return at once); 0 = never */
   int fft_mode;              /* CDX_FFT_FP32 (default) or CDX_FFT_TC_BF16 */
+  int prtf_iter;             /* prtfIter: from this step on (the step counter of phaseRetrieve, shrinkwraps
+                                included) accumulate the phase-retrieval transfer function; -1 = off (default) */
 } cdx_params;
 
 /* FFT arithmetic.  CDX_FFT_TC_BF16: the radix-16 passes run as tensor-core
@@ -149,6 +151,11 @@ int cdx_group_destroy(cdx_group* g);
 int cdx_get_object(cdx_ctx* ctx, int idx, float* out, int where);   /* objectWave (complex) */
 int cdx_get_fourier(cdx_ctx* ctx, int idx, float* out, int where);  /* patternWave (complex) */
 int cdx_get_support(cdx_ctx* ctx, int idx, float* out, int where);  /* support (float field) */
+/* PRTF of the last run (cdi.cc:355-380, 424-440): rows/2 floats, radius r =
+ * the angular sum of |<P_M Psi e^{i phi}>| over the steps from prtf_iter on,
+ * divided by the angular sum of the |P_M Psi| > 1e-6 mask at prtf_iter (the
+ * prtf.txt column).  CDX_ERR_STATE when the run did not reach prtf_iter. */
+int cdx_get_prtf(cdx_ctx* ctx, int idx, float* out, int where);
 
 /* ---------------------------------------------------------------- one call, host buffers */
 /* Whole path for one pattern with HOST buffers: create, set pattern, set
@@ -162,6 +169,13 @@ int cdx_phase_retrieve_host(const cdx_params* p, const char* algorithm, const fl
 /* myFFT / myIFFT (cudaConfig.cu:175-180): unnormalised 2-D C2C transform of
  * `batch` patterns, in place allowed.  inverse != 0 uses exp(+2 pi i). */
 int cdx_fft2(const void* in, void* out, int rows, int cols, int batch, int inverse, void* stream);
+/* applyPoissonNoise_WO (src/gpu/cdi.cu:291-296), the simulation's detector
+ * model (simCCDbit, cdi.cc:191-193): on `count` floats of a DEVICE pattern,
+ * I <- s (trunc(I rcolor / s) + Poisson(noise_level) - noise_level) / rcolor
+ * with s = 1/exposure (vars.scale).  Random numbers are counter based (seed,
+ * pixel index), not the reference's curand MRG32k3a states. */
+int cdx_ccd_noise(float* pattern, long long count, float noise_level, float exposure, int rcolor,
+                  unsigned long long seed, void* stream);
 /* cdx_fft2 with the FFT arithmetic chosen by fft_mode (CDX_FFT_*). */
 int cdx_fft2_ex(const void* in, void* out, int rows, int cols, int batch, int inverse, int fft_mode, void* stream);
 /* applyModAbs(source, target) with state NULL (cudaConfig.cu:827-841). */

@@ -343,6 +343,36 @@ class CDIState:
     iter: int = 0
     residual: float = 0.0
     history: list = field(default_factory=list)
+    prtf: np.ndarray = None  # prtf.txt column when the run reached prtf_iter
+
+
+def prtf_polar(img):
+    """``cart2polar_kernel`` + ``edgeReduce`` (src/gpu/cudaConfig.cu:1027-1063) on
+    the centred image (``cudaConvertFO`` of an FFT-order field): for radius r <
+    rows/2 the float32 sum over 2*cols angles, in angle order, of the bilinear
+    sample at (r cos t, r sin t) about (rows/2, cols/2)."""
+    img = np.fft.fftshift(np.asarray(img, np.float32))
+    rows, cols = img.shape
+    nang = 2 * cols
+    out = np.zeros(rows // 2, np.float32)
+    a = np.arange(nang)
+    ang = (a * (2.0 * np.pi / nang)).astype(np.float32)   # x * (2.0f*M_PI/cuda_row), double then float
+    c, s = np.cos(ang).astype(np.float32), np.sin(ang).astype(np.float32)
+    for r in range(rows // 2):
+        x = np.float32(r) * c + np.float32(rows >> 1)
+        y = np.float32(r) * s + np.float32(cols >> 1)
+        x0, y0 = np.floor(x).astype(int), np.floor(y).astype(int)
+        fx, fy = (x - x0).astype(np.float32), (y - y0).astype(np.float32)
+        ok = (x0 >= 0) & (x0 + 1 < rows) & (y0 >= 0) & (y0 + 1 < cols)
+        xa, ya = np.where(ok, x0, 0), np.where(ok, y0, 0)
+        v = ((1 - fx) * (1 - fy) * img[xa, ya] + (1 - fx) * fy * img[xa, ya + ok] +
+             fx * (1 - fy) * img[xa + ok, ya] + fx * fy * img[xa + ok, ya + ok])
+        v = np.where(ok, v, np.float32(0)).astype(np.float32)
+        acc = np.float32(0)
+        for t in v:   # edgeReduce adds the angles one by one in float
+            acc = np.float32(acc + t)
+        out[r] = acc
+    return out
 
 
 def prepare_from_restart(psi0, dtype=np.complex128):
@@ -381,7 +411,7 @@ def shrinkwrap_step(st: CDIState, shrink_threshold: float):
 def phase_retrieve(psi0, pattern, algorithm, *, support=None, oversampling_spt=2.0,
                    beta=1.0, shrink_threshold=0.1, sim_ccd_bit=False, noise_level=0,
                    exposure=1.0, rcolor=65535, beamstop=None, dtype=np.complex128,
-                   record=None, max_steps=None, step_noise=None):
+                   record=None, max_steps=None, step_noise=None, prtf_iter=-1):
     """``CDI::phaseRetrieve`` from a restart iterate (src/post_gpu/cdi.cc:297-449,
     with prepareIter cdi.cc:201-227 and initSupport 252-254).
 
@@ -409,6 +439,8 @@ def phase_retrieve(psi0, pattern, algorithm, *, support=None, oversampling_spt=2
     if max_steps is not None:
         steps = steps[:max_steps]
     inv_n = rt(1.0 / (rows * cols))
+    prtf_map = cache = gamma0 = weights = None
+    phi0 = 0.0
     for k, a in enumerate(steps):
         if a == SHRINKWRAP:
             shrinkwrap_step(st, shrink_threshold)
@@ -421,6 +453,26 @@ def phase_retrieve(psi0, pattern, algorithm, *, support=None, oversampling_spt=2
                 st.psi = apply_mod_abs(st.psi, pattern)
             rhop = (ifft2_u(st.psi) * inv_n).astype(dtype)
             st.rho = apply_support(st.rho, rhop, st.support, st.threshold, a, beta)
+            if prtf_iter >= 0 and k >= prtf_iter:
+                # PRTF block of phaseRetrieve (cdi.cc:355-380); cache and gamma0 start at 0
+                if prtf_map is None:
+                    prtf_map = np.zeros_like(st.psi)
+                    cache = np.zeros_like(st.psi)
+                    gamma0 = np.zeros_like(st.psi)
+                mod = np.abs(st.psi)
+                if k == prtf_iter:
+                    gamma0 = apply_support(np.zeros_like(rhop), rhop, st.support, st.threshold, ER)
+                    cache = gamma0 * gamma0
+                    sm = cache.sum()
+                    phi0 = float(np.float32(-np.arctan2(np.float32(sm.imag), np.float32(sm.real)) / 2))
+                    theta = phi0
+                    weights = prtf_polar((mod > 1e-6).astype(np.float32))
+                else:
+                    cache = apply_support(cache, rhop, st.support, st.threshold, ER) * np.conj(gamma0)
+                    sm = cache.sum()
+                    theta = float(np.float32(phi0 + np.arctan2(np.float32(sm.imag), np.float32(sm.real))))
+                ph = np.where(mod > 1e-6, st.psi / np.where(mod > 1e-6, mod, 1), 0)
+                prtf_map = prtf_map + ph * np.exp(1j * theta)
             if noise_rng is not None:
                 z = noise_rng.standard_normal(st.rho.shape) + 1j * noise_rng.standard_normal(st.rho.shape)
                 rms = np.sqrt(np.mean(np.abs(st.rho) ** 2))
@@ -431,6 +483,9 @@ def phase_retrieve(psi0, pattern, algorithm, *, support=None, oversampling_spt=2
             st.history.append((st.rho.copy(), st.psi.copy(), st.support.copy(), st.threshold))
     st.rho = (st.rho * rt(math.sqrt(rows * cols))).astype(dtype)
     st.residual = residual(st.psi, pattern)
+    if weights is not None:
+        # |prtf_map| / (iter - prtfIter), polar sums, prtf[i]/weights[i] (cdi.cc:424-439)
+        st.prtf = prtf_polar(np.abs(prtf_map) / (len(steps) - prtf_iter)) / weights
     return st
 
 

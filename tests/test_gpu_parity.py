@@ -479,3 +479,51 @@ def test_patterns_freeze_at_stop_rfactor(cdx):
         ctx.set_initial(0, psi2)
         ctx.run(alg)
         assert np.array_equal(ctx.get_object(0), other)
+
+
+def test_ccd_noise_model(cdx, torch_cuda):
+    """applyPoissonNoise_WO (cdi.cu:291-296): I -> s (trunc(I rcolor/s) + P - noise)/rcolor,
+    s = 1/exposure, P ~ Poisson(noise): the result minus the quantised pattern is
+    (P - noise) s / rcolor, mean 0 and variance noise (s/rcolor)^2."""
+    torch = torch_cuda
+    rng = np.random.default_rng(3)
+    n, noise, exposure, rcolor = 512, 25.0, 2.0, 65535
+    I = (rng.random((n, n)) * 3.0).astype(np.float32)
+    d = torch.from_numpy(I.copy()).cuda()
+    cdx.ccd_noise(d, noise, exposure, rcolor, seed=9)
+    got = d.cpu().numpy().astype(np.float64)
+    s = 1.0 / exposure
+    quant = s * np.trunc(I.astype(np.float32) * np.float32(rcolor) / np.float32(s)).astype(np.float64) / rcolor
+    k = (got - quant) * rcolor / s + noise           # the Poisson draws
+    assert np.allclose(k, np.round(k), atol=2e-2)
+    k = np.round(k)
+    assert k.min() >= 0
+    assert abs(k.mean() - noise) < 0.05 and abs(k.var() - noise) < 0.5
+    d2 = torch.from_numpy(I.copy()).cuda()
+    cdx.ccd_noise(d2, noise, exposure, rcolor, seed=9)
+    assert torch.equal(d, d2)   # counter based: same seed, same draws
+
+
+@pytest.mark.parametrize("alg,prtf_iter,tol", [("30*ER", 10, 1e-4),
+                                               ("10*HIO+1*shrinkWrap+10*ER+1*shrinkWrap+10*ER", 12, 1e-3)])
+def test_prtf_matches_oracle(cdx, alg, prtf_iter, tol):
+    """PRTF (cdi.cc:355-380, 424-440): the prtf.txt column against the oracle's
+    restatement from the same start; relative max difference <= tol (ER is
+    contractive; the run with HIO and shrinkwraps inherits its trajectory drift)."""
+    I, psi0 = blob_case(n=64, seed=5)
+    ref = O.phase_retrieve(psi0, I, alg, oversampling_spt=2.0, beta=0.9, shrink_threshold=0.1, prtf_iter=prtf_iter)
+    p = cdx.default_params(64, 64, oversampling_spt=2.0, beta=0.9, shrink_threshold=0.1, prtf_iter=prtf_iter)
+    with cdx.Context(p) as ctx:
+        ctx.set_pattern(0, I)
+        ctx.set_initial(0, psi0)
+        ctx.run(alg)
+        got = ctx.get_prtf(0)
+        assert got.shape == (32,)
+        e = np.max(np.abs(got - ref.prtf)) / np.max(np.abs(ref.prtf))
+        print(f"PRTF {alg[:20]}: max rel diff {e:.2e}, prtf[0:4] {got[:4]}")
+        assert e <= tol
+        # a run that stops before prtf_iter has no PRTF
+        ctx.set_initial(0, psi0)
+        ctx.run(f"{prtf_iter - 1}*ER")
+        with pytest.raises(cdx.CdxError):
+            ctx.get_prtf(0)
