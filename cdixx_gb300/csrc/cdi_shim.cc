@@ -310,4 +310,47 @@ void CDI::saveState() {   // cdi.cc:255-294: restart file of Psi plus .bin dumps
   cdx_write_bin(out_path(outputDir, "recon_object" + save_suffix + ".bin").c_str(), rho.data(), row, column, 1);
   for (float& v : spt) v = v > stats_.threshold ? 1.f : 0.f;   // bitMap(support, support)
   cdx_write_bin(out_path(outputDir, "support" + save_suffix + ".bin").c_str(), spt.data(), row, column, 0);
+
+  // findMiddle (misc.cc:27-42): centroid of the support bitmap in units of the
+  // field, coordinates (x + 0.5)/row - 0.5 (multiplyx/multiplyy, cudaConfig.cu:1427-1437)
+  double s0 = 0, sx = 0, sy = 0;
+  for (int x = 0; x < row; ++x)
+    for (int y = 0; y < column; ++y) {
+      const double m = spt[(size_t)x * column + y];
+      s0 += m;
+      sx += m * (float)((x + 0.5f) / row - 0.5f);
+      sy += m * (float)((y + 0.5f) / column - 0.5f);
+    }
+  const float midx = s0 > 0 ? (float)(sx / s0) : 0.f, midy = s0 > 0 ? (float)(sy / s0) : 0.f;
+  printf("mid= %f,%f\n", midx, midy);
+  // crop (cudaConfig.cu:348-358) of the object to the support size around the centroid
+  const double os = oversampling_spt > 0 ? oversampling_spt : 2.;
+  const int row_spt = (int)(row / os), col_spt = (int)(column / os);
+  int shiftx = (int)(row * midx);
+  if (shiftx + row_spt / 2 > row / 2) shiftx = (row - row_spt) / 2;
+  else if (shiftx - row_spt / 2 < -row / 2) shiftx = (row_spt - row) / 2;
+  int shifty = (int)(column * midy);
+  if (shifty + col_spt / 2 > column / 2) shifty = (row - col_spt) / 2;   // row, as the reference has it
+  else if (shifty - col_spt / 2 < -column / 2) shifty = (col_spt - column) / 2;
+  std::vector<float> crop((size_t)row_spt * col_spt * 2);
+  for (int x = 0; x < row_spt; ++x)
+    for (int y = 0; y < col_spt; ++y) {
+      const long long t = (long long)(x + (row - row_spt) / 2 + shiftx) * column + y + (column - col_spt) / 2 + shifty;
+      const size_t o = ((size_t)x * col_spt + y) * 2;
+      if (t >= 0 && t < (long long)n) {
+        crop[o] = rho[2 * t];
+        crop[o + 1] = rho[2 * t + 1];
+      }
+    }
+  cdx_write_bin(out_path(outputDir, "recon_wave" + save_suffix + ".bin").c_str(), crop.data(), row_spt, col_spt, 1);
+  // autocorrelation of the reconstruction: FFT(|Psi|^2) (cdi.cc:289-292)
+  std::vector<float> ac(2 * n, 0.f);
+  for (size_t i = 0; i < n; ++i) ac[2 * i] = psi[2 * i] * psi[2 * i] + psi[2 * i + 1] * psi[2 * i + 1];
+  void* d = nullptr;
+  if (cudaMalloc(&d, ac.size() * sizeof(float)) != cudaSuccess) check(CDX_ERR_NOMEM, "saveState");
+  cudaMemcpy(d, ac.data(), ac.size() * sizeof(float), cudaMemcpyHostToDevice);
+  check(cdx_fft2(d, d, row, column, 1, 0, nullptr), "saveState");
+  cudaMemcpy(ac.data(), d, ac.size() * sizeof(float), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  cdx_write_bin(out_path(outputDir, "autocorrelation_recon.bin").c_str(), ac.data(), row, column, 1);
 }

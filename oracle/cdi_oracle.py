@@ -534,3 +534,35 @@ def read_bin(path):
         if t == FLOAT2:
             return np.frombuffer(f.read(rows * cols * 8), np.complex64).reshape(rows, cols)
         raise ValueError(f"FILETYPE unrecognized: {t}")
+
+
+def find_middle(mask):
+    """``findMiddle`` (src/post_gpu/misc.cc:27-42) with ``multiplyx``/``multiplyy``
+    (src/gpu/cudaConfig.cu:1427-1437): the centroid of a field in units of its
+    size, coordinate (x + 0.5)/rows - 0.5."""
+    rows, cols = mask.shape
+    m = np.asarray(mask, np.float64)
+    s = m.sum()
+    cx = ((np.arange(rows) + 0.5) / rows - 0.5)[:, None]
+    cy = ((np.arange(cols) + 0.5) / cols - 0.5)[None, :]
+    return float(np.float32((m * cx).sum() / s)), float(np.float32((m * cy).sum() / s))
+
+
+def crop_about(src, out_rows, out_cols, midx, midy):
+    """``crop`` (src/gpu/cudaConfig.cu:348-358) of a rows x cols field to
+    out_rows x out_cols about (midx, midy), with the reference's clamping (its
+    y clamp uses rows)."""
+    rows, cols = src.shape
+    shiftx = int(rows * np.float32(midx))
+    if shiftx + out_rows // 2 > rows // 2:
+        shiftx = (rows - out_rows) // 2
+    elif shiftx - out_rows // 2 < -(rows // 2):
+        shiftx = (out_rows - rows) // 2
+    shifty = int(cols * np.float32(midy))
+    if shifty + out_cols // 2 > cols // 2:
+        shifty = (rows - out_cols) // 2
+    elif shifty - out_cols // 2 < -(cols // 2):
+        shifty = (out_cols - cols) // 2
+    x = np.arange(out_rows)[:, None] + (rows - out_rows) // 2 + shiftx
+    y = np.arange(out_cols)[None, :] + (cols - out_cols) // 2 + shifty
+    return src.reshape(-1)[(x * cols + y)]

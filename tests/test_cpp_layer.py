@@ -101,3 +101,13 @@ Job = {{
     res = float(r.stdout.split("residual=")[1].split()[0])
     assert abs(res - ref.residual) <= max(1e-3, 2 * tol) * ref.residual
     assert (tmp_path / "support.bin").exists() and (tmp_path / "autocorrelation.bin").exists()
+    # saveState post-processing (cdi.cc:266-292): centroid, crop, autocorrelation
+    spt = O.read_bin(tmp_path / "support.bin")
+    midx, midy = O.find_middle(spt)
+    got_mid = [float(v) for v in r.stdout.split("mid=")[1].split()[0].split(",")]
+    assert abs(got_mid[0] - midx) < 2e-6 and abs(got_mid[1] - midy) < 2e-6   # printed with 6 decimals
+    wave = O.read_bin(tmp_path / "recon_wave.bin")
+    assert wave.shape == (n // 2, n // 2)
+    assert np.array_equal(wave, O.crop_about(rho, n // 2, n // 2, got_mid[0], got_mid[1]))
+    ac = O.read_bin(tmp_path / "autocorrelation_recon.bin")
+    assert rel_l2(ac, np.fft.fft2(np.abs(psi.astype(np.complex128)) ** 2)) < 1e-5
