@@ -108,6 +108,7 @@ _SIGS = {
     "cdx_unet_loss_backward": [_P, _P, _P, _P, _P, _I, ctypes.POINTER(ctypes.c_double)],
     "cdx_unet_adam_step": [_P, _F],
     "cdx_unet_warm_start": [_P, _P, _P, _I, _I, _P, _P],
+    "cdx_gemm_bf16_tc": [_P, _P, _P, _I, _I, _I, _P, _P],
     "cdx_forward_model": [_I, _I, ctypes.c_ulonglong, _LL, ctypes.c_double, _P, _P, _P, _P, _P],
 }
 _RESTYPE = {"cdx_last_error": ctypes.c_char_p, "cdx_version": ctypes.c_char_p, "cdx_unet_destroy": None,

@@ -76,6 +76,11 @@ int cdx_unet_warm_start(cdx_unet* u, const float* intensity, const float* out, i
 int cdx_forward_model(int n, int count, unsigned long long seed, long long first, double photons,
                       float* intensity, float* amp_t, float* phase_t, float* support_t, void* stream);
 
+/* D[m][n] = sum_k A[m][k] B[n][k] on the tcgen05 tensor cores (A, B K-major
+ * BF16 device arrays, D FP32 row-major; K a multiple of 8).  *err_flag (device
+ * int, set by the caller to 0) becomes 1 if a tile's pipeline wait timed out. */
+int cdx_gemm_bf16_tc(const void* A, const void* B, float* D, int M, int N, int K, int* err_flag, void* stream);
+
 #pragma GCC visibility pop
 
 #ifdef __cplusplus
