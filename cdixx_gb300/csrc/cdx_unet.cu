@@ -12,6 +12,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -495,6 +496,7 @@ struct Net {
   float* dout = nullptr;
   int* twin = nullptr;
   float2* wrk = nullptr;   // warm start scratch
+  int* umma_err = nullptr; // set by a tcgen05 tile whose pipeline wait timed out
   int adam_t = 0;
   bool weights_dirty = true;
 };
@@ -587,7 +589,8 @@ int build(Net* u) {
   if ((e = dalloc(u, &u->gpart, gp)) || (e = dalloc(u, &u->cpart, cp)) || (e = dalloc(u, &u->wpart, wp)) ||
       (e = dalloc(u, &u->gsum, (size_t)B * c.groups * 2)) || (e = dalloc(u, &u->lpart, (size_t)B * 64 * 2)) ||
       (e = dalloc(u, &u->loss, 1)) || (e = dalloc(u, &u->dout, (size_t)B * c.n * c.n * 4)) ||
-      (e = dalloc(u, &u->twin, (size_t)B)) || (e = dalloc(u, &u->wrk, (size_t)B * c.n * c.n)))
+      (e = dalloc(u, &u->twin, (size_t)B)) || (e = dalloc(u, &u->wrk, (size_t)B * c.n * c.n)) ||
+      (e = dalloc(u, &u->umma_err, 1)))
     return e;
   u->gpart_cap = gp;
   u->cpart_cap = cp;
@@ -654,11 +657,35 @@ ConvShape conv_shape(const Net* u, const Layer& l, int count) {
   return s;
 }
 
+template <int BN, class Op>
+int launch_umma(const Op& op, long long M, int NC, int K, int* err, cudaStream_t st) {
+  static bool attr = false;   // per process; the attribute is per device function, cheap to repeat
+  if (!attr) {
+    U_CK(cudaFuncSetAttribute(umma::k_umma<BN, Op>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              umma::smem_bytes(BN)));
+    attr = true;
+  }
+  const dim3 grid((unsigned)((M + 127) / 128), (unsigned)((NC + BN - 1) / BN));
+  umma::k_umma<BN, Op><<<grid, 128, umma::smem_bytes(BN), st>>>(op, (int)M, NC, K, err);
+  U_CK(cudaGetLastError());
+  return CDX_OK;
+}
+
+// forward (DGRAD false) or data-gradient GEMM: tcgen05 tiles when the net is
+// configured for them, else the mma.sync kernel
 template <bool DGRAD>
-int launch_gemm(const GemmArgs& a, cudaStream_t st) {
+int launch_gemm(const Net* u, const GemmArgs& a, cudaStream_t st) {
   const ConvShape& s = a.s;
   const long long M = DGRAD ? (long long)s.N * s.H * s.W : (long long)s.N * s.Ho * s.Wo;
   const int NC = DGRAD ? s.Cin : s.Cout;
+  const int K = DGRAD ? s.KH * s.KW * s.Cout : s.KH * s.KW * s.Cin;
+  if (u->cfg.umma) {
+    using Op = typename std::conditional<DGRAD, ConvDgradOp, ConvFwdOp>::type;
+    const Op op{a};
+    if (NC <= 32) return launch_umma<32>(op, M, NC, K, u->umma_err, st);
+    if (NC <= 64) return launch_umma<64>(op, M, NC, K, u->umma_err, st);
+    return launch_umma<128>(op, M, NC, K, u->umma_err, st);
+  }
   const dim3 grid((unsigned)((M + 127) / 128), (unsigned)((NC + (NC <= 32 ? 31 : 63)) / (NC <= 32 ? 32 : 64)));
   if (NC <= 32) k_conv_gemm<DGRAD, 32><<<grid, 128, 0, st>>>(a);
   else k_conv_gemm<DGRAD, 64><<<grid, 128, 0, st>>>(a);
@@ -707,13 +734,13 @@ int forward(Net* u, const float* inten, int count) {
       a.w = l.wt;
       a.out0 = l.pre;
       a.out1 = l.pre;
-      if ((e = launch_gemm<true>(a, u->st))) return e;
+      if ((e = launch_gemm<true>(u, a, u->st))) return e;
     } else {
       a.x0 = act_of(u, l.in0);
       a.x1 = l.in1 >= 0 ? act_of(u, l.in1) : a.x0;
       a.w = l.wb;
       a.out0 = l.pre;
-      if ((e = launch_gemm<false>(a, u->st))) return e;
+      if ((e = launch_gemm<false>(u, a, u->st))) return e;
     }
     const long long px = (long long)count * l.out_h * l.out_h;
     if (l.kind == L_HEAD) {
@@ -779,7 +806,7 @@ int backward(Net* u, const float* amp_t, const float* ph_t, const float* sup_t, 
         f.w = l.wb;
         f.out0 = u->L[l.in0].dact;
         f.accumulate = 1;
-        if ((e = launch_gemm<false>(f, u->st))) return e;
+        if ((e = launch_gemm<false>(u, f, u->st))) return e;
       }
     } else {
       a.x0 = act_of(u, l.in0);
@@ -794,7 +821,7 @@ int backward(Net* u, const float* amp_t, const float* ph_t, const float* sup_t, 
         d.out0 = u->L[l.in0].dact;
         d.out1 = l.in1 >= 0 ? u->L[l.in1].dact : d.out0;
         d.accumulate = 1;
-        if ((e = launch_gemm<true>(d, u->st))) return e;
+        if ((e = launch_gemm<true>(u, d, u->st))) return e;
       }
     }
   }
@@ -824,6 +851,7 @@ int cdx_unet_config_default(cdx_unet_config* c) {
   c->slope = 0.01f;
   c->support_weight = 0.1f;
   c->seed = 20260101ull;
+  c->umma = 0;
   return CDX_OK;
 }
 
@@ -862,7 +890,8 @@ int cdx_unet_create(const cdx_unet_config* c, void* stream, cdx_unet** out) {
     if (cudaMemcpy(n->params, h.data(), sizeof(float) * h.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemset(n->m, 0, sizeof(float) * n->np) != cudaSuccess ||
         cudaMemset(n->v, 0, sizeof(float) * n->np) != cudaSuccess ||
-        cudaMemset(n->grads, 0, sizeof(float) * n->np) != cudaSuccess)
+        cudaMemset(n->grads, 0, sizeof(float) * n->np) != cudaSuccess ||
+        cudaMemset(n->umma_err, 0, sizeof(int)) != cudaSuccess)
       e = set_error(CDX_ERR_CUDA, "parameter upload failed");
   }
   if (e) {
@@ -906,6 +935,14 @@ int cdx_unet_get_grads(const cdx_unet* u, float* host, long long count) {
   return CDX_OK;
 }
 
+static int check_umma(Net* n) {
+  int flag = 0;
+  U_CK(cudaMemcpyAsync(&flag, n->umma_err, sizeof(int), cudaMemcpyDeviceToHost, n->st));
+  U_CK(cudaStreamSynchronize(n->st));
+  if (flag) return set_error(CDX_ERR_CUDA, "tensor-core GEMM pipeline wait timed out");
+  return CDX_OK;
+}
+
 int cdx_unet_forward(cdx_unet* u, const float* intensity, float* out, int count) {
   if (!u || !intensity || !out) return set_error(CDX_ERR_ARG, "null argument");
   if (count < 1 || count > u->net.cfg.batch) return set_error(CDX_ERR_ARG, "count must be in [1, batch]");
@@ -915,8 +952,7 @@ int cdx_unet_forward(cdx_unet* u, const float* intensity, float* out, int count)
   const int P = n->cfg.n * n->cfg.n;
   k_head_out<<<grid_for((long long)count * P), kThreads, 0, n->st>>>(n->L.back().pre, P, (long long)count * P, out);
   U_CK(cudaGetLastError());
-  U_CK(cudaStreamSynchronize(n->st));
-  return CDX_OK;
+  return check_umma(n);
 }
 
 int cdx_unet_loss_backward(cdx_unet* u, const float* intensity, const float* amp_t, const float* phase_t,
@@ -930,8 +966,7 @@ int cdx_unet_loss_backward(cdx_unet* u, const float* intensity, const float* amp
   if (loss) {
     U_CK(cudaMemcpyAsync(loss, n->loss, sizeof(double), cudaMemcpyDeviceToHost, n->st));
   }
-  U_CK(cudaStreamSynchronize(n->st));
-  return CDX_OK;
+  return check_umma(n);
 }
 
 int cdx_unet_adam_step(cdx_unet* u, float lr) {

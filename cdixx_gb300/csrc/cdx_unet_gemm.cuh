@@ -22,6 +22,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "cdx_umma.cuh"
+
 namespace cdx {
 namespace unet {
 
@@ -313,6 +315,90 @@ __global__ void __launch_bounds__(128) k_conv_wgrad(GemmArgs a) {
         }
     }
 }
+
+// ------------------------------------------------ tcgen05 operand policies
+// The forward and data-gradient GEMMs on the 5th-generation tensor cores
+// (cdx_umma.cuh): the same gathers as above, staged into the UMMA tiles.
+struct ConvFwdOp {
+  GemmArgs a;
+  struct Row { int n, oy, ox; bool ok; };
+  struct Kc { int ky, kx, ci; bool ok; };
+  __device__ Row row(int m, int M) const {
+    Row r{0, 0, 0, m < M};
+    if (r.ok) {
+      const int hw = a.s.Ho * a.s.Wo;
+      r.n = m / hw;
+      const int t = m - r.n * hw;
+      r.oy = t / a.s.Wo;
+      r.ox = t - r.oy * a.s.Wo;
+    }
+    return r;
+  }
+  __device__ Kc kc(int k, int K) const {
+    const int kk = k / a.s.Cin, ci = k - kk * a.s.Cin, ky = kk / a.s.KW;
+    return Kc{ky, kk - ky * a.s.KW, ci, k < K};
+  }
+  __device__ const __nv_bfloat16* a_src(const Row& r, const Kc& c) const {
+    if (!r.ok || !c.ok) return nullptr;
+    const ConvShape& s = a.s;
+    const int iy = r.oy * s.S - s.P + c.ky, ix = r.ox * s.S - s.P + c.kx;
+    if (iy < 0 || iy >= s.H || ix < 0 || ix >= s.W) return nullptr;
+    const long long pix = ((long long)r.n * s.H + iy) * s.W + ix;
+    if (c.ci < s.C0) return a.x0 + pix * s.C0 + c.ci;
+    return a.x1 + pix * (s.Cin - s.C0) + (c.ci - s.C0);
+  }
+  __device__ const __nv_bfloat16* b_src(int n, int k) const {
+    return a.w + (long long)n * (a.s.KH * a.s.KW * a.s.Cin) + k;
+  }
+  __device__ const void* dummy() const { return a.w; }
+  __device__ void store(int m, int n0, const float* v, int cnt) const {
+    float* p = a.out0 + (long long)m * a.s.Cout + n0;
+    for (int j = 0; j < cnt; ++j) p[j] = a.accumulate ? p[j] + v[j] : v[j];
+  }
+};
+
+struct ConvDgradOp {
+  GemmArgs a;
+  struct Row { int n, iy, ix; bool ok; };
+  struct Kc { int ky, kx, co; bool ok; };
+  __device__ Row row(int m, int M) const {
+    Row r{0, 0, 0, m < M};
+    if (r.ok) {
+      const int hw = a.s.H * a.s.W;
+      r.n = m / hw;
+      const int t = m - r.n * hw;
+      r.iy = t / a.s.W;
+      r.ix = t - r.iy * a.s.W;
+    }
+    return r;
+  }
+  __device__ Kc kc(int k, int K) const {
+    const int kk = k / a.s.Cout, co = k - kk * a.s.Cout, ky = kk / a.s.KW;
+    return Kc{ky, kk - ky * a.s.KW, co, k < K};
+  }
+  __device__ const __nv_bfloat16* a_src(const Row& r, const Kc& c) const {
+    if (!r.ok || !c.ok) return nullptr;
+    const ConvShape& s = a.s;
+    const int ty = r.iy + s.P - c.ky, tx = r.ix + s.P - c.kx;
+    if (ty < 0 || tx < 0) return nullptr;
+    const int oy = ty / s.S, ox = tx / s.S;
+    if (oy * s.S != ty || ox * s.S != tx || oy >= s.Ho || ox >= s.Wo) return nullptr;
+    return a.dy + (((long long)r.n * s.Ho + oy) * s.Wo + ox) * s.Cout + c.co;
+  }
+  __device__ const __nv_bfloat16* b_src(int n, int k) const {
+    return a.w + (long long)n * (a.s.KH * a.s.KW * a.s.Cout) + k;
+  }
+  __device__ const void* dummy() const { return a.w; }
+  __device__ void store(int m, int n0, const float* v, int cnt) const {
+    const ConvShape& s = a.s;
+    const int c1 = s.Cin - s.C0;
+    for (int j = 0; j < cnt; ++j) {
+      const int n = n0 + j;
+      float* p = n < s.C0 ? a.out0 + (long long)m * s.C0 + n : a.out1 + (long long)m * c1 + (n - s.C0);
+      *p = a.accumulate ? *p + v[j] : v[j];
+    }
+  }
+};
 
 }  // namespace unet
 }  // namespace cdx

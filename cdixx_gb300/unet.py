@@ -20,7 +20,7 @@ from cdixx_gb300 import native
 class UNetConfig(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int), ("levels", ctypes.c_int), ("base", ctypes.c_int), ("batch", ctypes.c_int),
                 ("groups", ctypes.c_int), ("slope", ctypes.c_float), ("support_weight", ctypes.c_float),
-                ("seed", ctypes.c_ulonglong)]
+                ("seed", ctypes.c_ulonglong), ("umma", ctypes.c_int)]
 
 
 def _ptr(t):

@@ -23,8 +23,9 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--levels", type=int, default=4)
     ap.add_argument("--base", type=int, default=32)
+    ap.add_argument("--umma", type=int, default=0, help="1: tcgen05 convolutions, 0: mma.sync")
     a = ap.parse_args(argv)
-    net = unet.UNet(n=a.n, levels=a.levels, base=a.base, batch=a.batch, seed=1)
+    net = unet.UNet(n=a.n, levels=a.levels, base=a.base, batch=a.batch, seed=1, umma=a.umma)
     I, amp, ph, sup = unet.forward_model(a.n, a.batch, 7, 0, 1e6)
     net.train_step(I, amp, ph, sup)
     torch.cuda.synchronize()
@@ -35,7 +36,8 @@ def main(argv=None):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / a.steps
     ok = bool(np.isfinite(losses).all())
-    print(f"n={a.n} batch={a.batch} levels={a.levels} base={a.base}: {ms:.2f} ms/step, loss {losses[-1]:.5f}, "
+    print(f"n={a.n} batch={a.batch} levels={a.levels} base={a.base} umma={a.umma}: {ms:.2f} ms/step, "
+          f"loss {losses[-1]:.5f}, "
           f"finite={ok}")
     net.close()
     return 0 if ok else 1

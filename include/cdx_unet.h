@@ -42,6 +42,9 @@ typedef struct {
   float slope;        /* LeakyReLU negative slope */
   float support_weight; /* w_s */
   unsigned long long seed; /* weight initialisation */
+  int umma;           /* 1: forward and data-gradient convolutions on tcgen05/TMEM; 0 (default):
+                         warp-level mma.sync, faster for these channel counts (the weight gradient
+                         is mma.sync in both; the two give the same bits) */
 } cdx_unet_config;
 
 int cdx_unet_config_default(cdx_unet_config* c);

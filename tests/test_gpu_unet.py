@@ -167,3 +167,28 @@ def test_warm_start_gain_over_random_phase_hio(cdx, torch_cuda):
     print(f"loss {losses[0]:.4f} -> {np.mean(losses[-10:]):.4f}; reached R<=0.02: random {f0:.2f} (error {e0:.3f}), "
           f"warm {f1:.2f} (error {e1:.3f})")
     assert f1 >= f0 + 0.25 and e1 < e0
+
+
+def test_tcgen05_and_mma_sync_convolutions_agree(cdx, torch_cuda):
+    """The forward and data-gradient convolutions on tcgen05/TMEM and on
+    mma.sync (default) give the same network output and gradients (measured:
+    the same bits -- both add exact BF16 products in 16-term chunks in the
+    same K order; the bound allows FP32 accumulation-order differences)."""
+    torch = torch_cuda
+    from cdixx_gb300 import unet
+    n, levels, base, batch = 64, 3, 16, 2
+    I, amp, ph, sup = small_case(n, batch)
+    p = U.init_params(n, levels, base, seed=9)
+    dev = [torch.from_numpy(x).cuda() for x in (I, amp, ph, sup)]
+    res = []
+    for mode in (1, 0):
+        with unet.UNet(n=n, levels=levels, base=base, batch=batch, groups=8, umma=mode) as net:
+            net.set_params(p)
+            out = net.forward(dev[0]).cpu().numpy()
+            loss = net.loss_backward(*dev)
+            res.append((out, loss, net.grads().astype(np.float64)))
+    (o1, l1, g1), (o0, l0, g0) = res
+    ro = np.linalg.norm(o1 - o0) / np.linalg.norm(o0)
+    rg = np.linalg.norm(g1 - g0) / np.linalg.norm(g0)
+    print(f"tcgen05 vs mma.sync: output {ro:.2e}, loss {abs(l1 - l0) / l0:.2e}, gradient {rg:.2e}")
+    assert ro < 5e-3 and abs(l1 - l0) <= 2e-3 * l0 and rg < 3e-2
