@@ -397,7 +397,7 @@ def run_gpu(args):
                        "patterns_per_s": value / JOB_ITERS, "path": "fused FP32 (column pass + row pass)"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                         "kernel": "one fused iteration (col_pass_kernel<2048> + row_pass_kernel<2048>)",
+                         "kernel": "one fused iteration (col_pass_rk<2048> + row_pass_rk<2048>)",
                          "t_iter_us": t_iter * 1e6},
             "e2e": {"value": e2e, "unit": "iter/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "step": "whole 2000-iteration job via cdx_phase_retrieve_host"},

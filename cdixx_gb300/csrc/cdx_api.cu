@@ -59,6 +59,14 @@ int twiddles(int n, float2** out) {
   return CDX_OK;
 }
 
+}  // namespace
+
+namespace cdx {
+int device_twiddles(int n, float2** out) { return twiddles(n, out); }
+}  // namespace cdx
+
+namespace {
+
 int check_len(int n) {
   if (!size_supported(n) || n > 4096 || !prep_launcher(n))
     return set_error(CDX_ERR_SIZE, "unsupported length " + std::to_string(n) +

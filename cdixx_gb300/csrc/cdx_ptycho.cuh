@@ -1,0 +1,267 @@
+// Per-scan-position kernels of the ptychographic sweep, on the register-handoff
+// FFT engine of cdx_rfft.cuh.  One position of ptycho::iterate
+// (util/ptycho.cpp:514-560) is three launches:
+//   forward row pass   psi = P * O_window, row FFT            -> W (column-tiled)
+//   column pass        column FFT, applyModAccurate, column IFFT -> W
+//   update row pass    row IFFT * norm = psi', diff = psi - psi', rPIE update of
+//                      the object window (and the probe step), O written back
+// so the exit wave is never stored and the object window is read twice and
+// written once per position.  The scan index of the position comes from the
+// device (order[iteration * nscan + k], iteration counter in device memory),
+// so one sweep can be captured once and replayed.
+#pragma once
+#include "cdx_rfft.cuh"
+
+namespace cdx {
+
+struct PtyArgs {
+  float2* W;               // work, column-tiled with width 2^tl
+  float2* obj;             // object, row-major obj_rows x obj_cols
+  const float2* probe;     // rows x cols
+  float2* step;            // probe step accumulator (probe phase)
+  const float* pats;       // nscan patterns, column-tiled, pat_stride floats apart
+  const float* bs;         // beamstop, column-tiled, or null
+  const int* order;        // scan index per slot (iteration * nscan + k)
+  const int* iter;         // device iteration counter (relative to the run)
+  const int2* win;         // window origin per scan index
+  const float* scal;       // [0] max |P|^2, [1] object maximum (probe phase)
+  const float2* tw;        // twiddles of the kernel's line length
+  long long pat_stride;
+  int rows, cols, obj_rows, obj_cols, tl, k, nscan, probe_phase;
+  float norm;              // 1/sqrt(rows cols) (util/ptycho.cpp:439)
+  float maximum;           // 0.95 * vars.scale, the saturation level of applyModAccurate
+  float obj_step;          // rPIE step of the object: 1, or 0.5 in the probe phase
+  float pss;               // probe step size 1/nscan
+};
+
+constexpr float kPtyAlpha = 0.1f;   // ALPHA, src/gpu/ptycho.cu:5
+constexpr float kPtyBeta = 0.5f;    // BETA, src/gpu/ptycho.cu:6
+
+// rPIE (src/gpu/ptycho.cu:55-61): target -= conj(s) d * step / ((1-p)|s|^2 + p max(maxi, 1e-5)).
+// The denominator is summed and divided in float (the reference: in double).
+__device__ __forceinline__ float2 pty_rpie(float2 t, float2 s, float2 d, float maxi, float param, float stepsize) {
+  float den = s.x * s.x + s.y * s.y;
+  den = stepsize / ((1.f - param) * den + param * fmaxf(maxi, 1e-5f));
+  t.x -= (s.x * d.x + s.y * d.y) * den;
+  t.y -= (s.x * d.y - s.y * d.x) * den;
+  return t;
+}
+// rPIE_step (src/gpu/ptycho.cu:62-68): -conj(s) d / ((1-p)|s|^2 + p max(maxi, 1e-5)).
+__device__ __forceinline__ float2 pty_rpie_step(float2 s, float2 d, float maxi, float param) {
+  float den = s.x * s.x + s.y * s.y;
+  den = 1.f / ((1.f - param) * den + param * fmaxf(maxi, 1e-5f));
+  return make_float2(-(s.x * d.x + s.y * d.y) * den, -(s.x * d.y - s.y * d.x) * den);
+}
+
+// applyModAccurate, 4-argument form (src/gpu/cdi.cu:351-388).
+__device__ __forceinline__ float2 pty_modacc(float2 s, float inten, float bsv, bool has_bs, float norm,
+                                             float maximum) {
+  const float mod2 = fmaxf(0.f, inten);
+  float rx = s.x, ry = s.y;
+  if (norm != 1.f) { rx *= norm; ry *= norm; }
+  if (has_bs && bsv > 0.5f) return make_float2(rx, ry);
+  const float src = rx * rx + ry * ry;
+  if (src == 0.f) return s;
+  if (mod2 >= maximum && src >= mod2) return make_float2(rx, ry);
+  const float sc = sqrtf(mod2 / src);
+  return make_float2(sc * rx, sc * ry);
+}
+
+__device__ __forceinline__ long long pty_tiled(int r, int c, int rows, int tl) {
+  return ((((long long)(c >> tl)) * rows + r) << tl) + (c & ((1 << tl) - 1));
+}
+
+// ------------------------------------------------------- forward row pass
+template <int N>
+__global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_ROW) pty_fwd_rk(PtyArgs a) {
+  using G = Geom<N>;
+  constexpr int L = G::L;
+  using F0 = RFirst<N, 0>;
+  using FL = RLast<N, 0>;
+  extern __shared__ float2 smem[];
+  const int row0 = blockIdx.x * L;
+  const int nrows = min(L, a.rows - row0);
+  const int cb = min(a.tl, rfft_cb_max<N>());
+  const int si = a.order[*a.iter * a.nscan + a.k];
+  const int2 w = a.win[si];
+  const long long OC = a.obj_cols;
+  float2 v0[F0::B][F0::R];
+#pragma unroll
+  for (int b = 0; b < F0::B; ++b) {
+    int l, j;
+    if (!bfly_of<N, F0::R>(b, cb, l, j)) continue;
+#pragma unroll
+    for (int r = 0; r < F0::R; ++r) {
+      const int c = j + r * F0::NR, row = row0 + l;
+      float2 y = make_float2(0.f, 0.f);
+      if (l < nrows) {
+        const int ox = w.x + row, oy = w.y + c;
+        if (ox >= 0 && ox < a.obj_rows && oy >= 0 && oy < a.obj_cols)
+          y = cmul(__ldg(a.probe + (long long)row * N + c), a.obj[ox * OC + oy]);
+      }
+      v0[b][r] = y;
+    }
+  }
+  float2 v[FL::B][FL::R];
+  rfft<N, 0, false>(v0, v, smem, a.tw, cb);
+#pragma unroll
+  for (int b = 0; b < FL::B; ++b) {
+    int l, j;
+    if (!bfly_of<N, FL::R>(b, cb, l, j) || l >= nrows) continue;
+#pragma unroll
+    for (int r = 0; r < FL::R; ++r) __stcg(a.W + pty_tiled(row0 + l, j + r * FL::NS, a.rows, a.tl), v[b][r]);
+  }
+}
+
+// ------------------------------------------------------------ column pass
+template <int N>
+__global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_COL) pty_col_rk(PtyArgs a) {
+  using G = Geom<N>;
+  constexpr int L = G::L, T = G::T;
+  using F0 = RFirst<N, 0>;
+  using FL = RLast<N, 0>;
+  using IL = RLast<N, 1>;
+  extern __shared__ float2 smem[];
+  const int c0 = blockIdx.x * L;
+  const int ncols = min(L, a.cols - c0);
+  const long long tile = (long long)blockIdx.x * N * L;
+  float* int_s = reinterpret_cast<float*>(smem + L * G::LD);
+  float* bs_s = int_s + L * N;
+  const int si = a.order[*a.iter * a.nscan + a.k];
+  const float* pat = a.pats + si * a.pat_stride + tile;
+  const bool has_bs = a.bs != nullptr;
+#pragma unroll 4
+  for (int q = threadIdx.x; q < L * N / 4; q += T) {
+    cp_async16(int_s + 4 * q, pat + 4 * q, true);
+    if (has_bs) cp_async16(bs_s + 4 * q, a.bs + tile + 4 * q, true);
+  }
+  cp_commit();
+  float2 v0[F0::B][F0::R];
+#pragma unroll
+  for (int b = 0; b < F0::B; ++b) {
+    int l, j;
+    if (!bfly_of<N, F0::R>(b, 0, l, j)) continue;
+#pragma unroll
+    for (int r = 0; r < F0::R; ++r) v0[b][r] = __ldcg(a.W + tile + (long long)(j + r * F0::NR) * L + l);
+  }
+  float2 v[FL::B][FL::R];
+  rfft<N, 0, false>(v0, v, smem, a.tw, 0);
+  cp_wait<0>();
+  __syncthreads();
+#pragma unroll
+  for (int b = 0; b < FL::B; ++b) {
+    int l, j;
+    if (!bfly_of<N, FL::R>(b, 0, l, j)) continue;
+#pragma unroll
+    for (int r = 0; r < FL::R; ++r) {
+      const int t = (j + r * FL::NS) * L + l;
+      const float2 z = pty_modacc(v[b][r], int_s[t], has_bs ? bs_s[t] : 0.f, has_bs, a.norm, a.maximum);
+      v[b][r] = l < ncols ? z : make_float2(0.f, 0.f);
+    }
+  }
+  float2 o[IL::B][IL::R];
+  rfft<N, 1, true>(v, o, smem, a.tw, 0);
+#pragma unroll
+  for (int b = 0; b < IL::B; ++b) {
+    int l, j;
+    if (!bfly_of<N, IL::R>(b, 0, l, j)) continue;
+#pragma unroll
+    for (int r = 0; r < IL::R; ++r) __stcg(a.W + tile + (long long)(j + r * IL::NS) * L + l, o[b][r]);
+  }
+}
+
+// -------------------------------------------------------- update row pass
+template <int N>
+__global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_ROW) pty_upd_rk(PtyArgs a) {
+  using G = Geom<N>;
+  constexpr int L = G::L;
+  using F0 = RFirst<N, 0>;
+  using FL = RLast<N, 0>;
+  extern __shared__ float2 smem[];
+  const int row0 = blockIdx.x * L;
+  const int nrows = min(L, a.rows - row0);
+  const int cb = min(a.tl, rfft_cb_max<N>());
+  const int si = a.order[*a.iter * a.nscan + a.k];
+  const int2 w = a.win[si];
+  const long long OC = a.obj_cols;
+  float2 v0[F0::B][F0::R];
+#pragma unroll
+  for (int b = 0; b < F0::B; ++b) {
+    int l, j;
+    if (!bfly_of<N, F0::R>(b, cb, l, j)) continue;
+#pragma unroll
+    for (int r = 0; r < F0::R; ++r)
+      v0[b][r] = l < nrows ? __ldcg(a.W + pty_tiled(row0 + l, j + r * F0::NR, a.rows, a.tl)) : make_float2(0.f, 0.f);
+  }
+  float2 v[FL::B][FL::R];
+  rfft<N, 0, true>(v0, v, smem, a.tw, cb);
+  const float pmax = a.scal[0], omax = a.scal[1];
+#pragma unroll
+  for (int b = 0; b < FL::B; ++b) {
+    int l, j;
+    if (!bfly_of<N, FL::R>(b, cb, l, j) || l >= nrows) continue;
+#pragma unroll
+    for (int r = 0; r < FL::R; ++r) {
+      const int c = j + r * FL::NS, row = row0 + l;
+      float2 pp = v[b][r];                       // IFFT, then applyNorm(Fn, norm)
+      pp.x *= a.norm;
+      pp.y *= a.norm;
+      const int ox = w.x + row, oy = w.y + c;
+      const bool inb = ox >= 0 && ox < a.obj_rows && oy >= 0 && oy < a.obj_cols;
+      float2 o = inb ? a.obj[ox * OC + oy] : make_float2(0.f, 0.f);
+      const long long pi = (long long)row * N + c;
+      const float2 p = __ldg(a.probe + pi);
+      float2 d = cmul(p, o);                     // esw = P * O_window, then esw += Fn * (-1)
+      d.x -= pp.x;
+      d.y -= pp.y;
+      o = pty_rpie(o, p, d, pmax, kPtyAlpha, a.obj_step);
+      if (a.probe_phase) {
+        const float2 st = pty_rpie_step(o, d, omax, kPtyBeta);
+        float2 acc = a.step[pi];
+        acc.x = acc.x + st.x * a.pss;
+        acc.y = acc.y + st.y * a.pss;
+        a.step[pi] = acc;
+      }
+      if (inb) a.obj[ox * OC + oy] = o;
+    }
+  }
+}
+
+// Launchers of the three kernels for line length N (host side).
+template <int N>
+cudaError_t pty_prepare() {
+  using G = Geom<N>;
+  cudaError_t e = cudaFuncSetAttribute(pty_fwd_rk<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM_LINES);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(pty_upd_rk<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM_LINES);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(pty_col_rk<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             G::SMEM_LINES + 2 * G::L * N * (int)sizeof(float));
+  return e;
+}
+template <int N>
+cudaError_t pty_launch_fwd(const PtyArgs& a, cudaStream_t st) {
+  using G = Geom<N>;
+  pty_fwd_rk<N><<<(a.rows + G::L - 1) / G::L, G::T, G::SMEM_LINES, st>>>(a);
+  return cudaGetLastError();
+}
+template <int N>
+cudaError_t pty_launch_upd(const PtyArgs& a, cudaStream_t st) {
+  using G = Geom<N>;
+  pty_upd_rk<N><<<(a.rows + G::L - 1) / G::L, G::T, G::SMEM_LINES, st>>>(a);
+  return cudaGetLastError();
+}
+template <int N>
+cudaError_t pty_launch_col(const PtyArgs& a, cudaStream_t st) {
+  using G = Geom<N>;
+  pty_col_rk<N><<<(a.cols + G::L - 1) / G::L, G::T, G::SMEM_LINES + 2 * G::L * N * (int)sizeof(float), st>>>(a);
+  return cudaGetLastError();
+}
+
+#define CDX_PTY_INSTANTIATE(N)                                               \
+  template cudaError_t pty_prepare<N>();                                     \
+  template cudaError_t pty_launch_fwd<N>(const PtyArgs&, cudaStream_t);      \
+  template cudaError_t pty_launch_upd<N>(const PtyArgs&, cudaStream_t);      \
+  template cudaError_t pty_launch_col<N>(const PtyArgs&, cudaStream_t);
+
+}  // namespace cdx

@@ -110,6 +110,23 @@ _SIGS = {
     "cdx_unet_warm_start": [_P, _P, _P, _I, _I, _P, _P],
     "cdx_gemm_bf16_tc": [_P, _P, _P, _I, _I, _I, _P, _P],
     "cdx_forward_model": [_I, _I, ctypes.c_ulonglong, _LL, ctypes.c_double, _P, _P, _P, _P, _P],
+    # include/cdx_ptycho.h
+    "cdx_pty_params_default": [_P],
+    "cdx_pty_create": [_P, _P, ctypes.POINTER(_P)],
+    "cdx_pty_destroy": [_P],
+    "cdx_pty_set_scan": [_P, _P, _P],
+    "cdx_pty_set_patterns": [_P, _P],
+    "cdx_pty_get_patterns": [_P, _P],
+    "cdx_pty_set_object": [_P, _P],
+    "cdx_pty_get_object": [_P, _P],
+    "cdx_pty_set_probe": [_P, _P],
+    "cdx_pty_get_probe": [_P, _P],
+    "cdx_pty_get_pupil": [_P, _P],
+    "cdx_pty_init_object": [_P, ctypes.c_ulonglong],
+    "cdx_pty_simulate": [_P],
+    "cdx_pty_iterate": [_P, _I, _I, _P, ctypes.c_uint],
+    "cdx_pty_last_ms": [_P, ctypes.POINTER(ctypes.c_float)],
+    "cdx_pty_scan_orders": [_I, _I, ctypes.c_uint, _P],
 }
 _RESTYPE = {"cdx_last_error": ctypes.c_char_p, "cdx_version": ctypes.c_char_p, "cdx_unet_destroy": None,
             "cdx_unet_param_count": ctypes.c_longlong}

@@ -1,0 +1,105 @@
+/* C ABI of the GB300 ptychographic reconstruction (rPIE object and probe
+ * updates with mPIE momentum): the reference's ptycho::iterate
+ * (util/ptycho.cpp:429-736) and the kernels it calls (src/gpu/ptycho.cu:9-113,
+ * applyModAccurate src/gpu/cdi.cu:351-388, the angular-spectrum propagator
+ * src/post_gpu/propagator.cc:31-49), plus the set-up steps of its driver
+ * (initObject util/ptycho.cpp:363-369, the noise-free part of createPattern
+ * 310-359).
+ *
+ * The reference keeps this path in an executable (util/ptycho.cpp main) that
+ * owns its buffers through the process-wide memory pool; here a handle owns
+ * them.  Every call returns CDX_OK (0) or a CDX_ERR_* code of cdx.h with the
+ * message in cdx_last_error(); no call aborts the process.  Host pointers
+ * are plain row-major arrays; complex values are interleaved float pairs
+ * (the reference's complexFormat).
+ */
+#ifndef CDX_PTYCHO_H
+#define CDX_PTYCHO_H
+
+#include "cdx.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+#pragma GCC visibility push(default)
+
+typedef struct cdx_pty cdx_pty;
+
+/* The fields ptycho::iterate reads (include/readConfig.hpp:25-35, where the
+ * real-valued ones are double) and the sizes the driver derives. */
+typedef struct cdx_pty_params {
+  int rows, cols;          /* probe and pattern size (row, column); 2^a 3^b in [16, 4096] */
+  int obj_rows, obj_cols;  /* object size (row_O, column_O) */
+  int nscan;               /* scan positions */
+  double lambda;           /* wavelength */
+  double d;                /* sample-detector distance */
+  double dpupil;           /* pupil-sample distance (propagate_pupil.distance) */
+  double pixelsize;        /* detector pixel size */
+  double pupil_size;       /* pupil diameter in pixels (pupilSize) */
+  double exposure;         /* patterns are stored scaled by 1/exposure */
+  int mpie;                /* momentum step after each sweep (mPIE, default 1) */
+  int use_bs;              /* beamstop of radius beam_stop_size at the pattern centre (useBS) */
+  int beam_stop_size;
+} cdx_pty_params;
+
+/* Defaults of readConfig (include/readConfig.hpp): mPIE 1, pupilSize 500,
+ * beamStopSize 5, exposure 1; sizes and optics are the caller's. */
+int cdx_pty_params_default(cdx_pty_params* p);
+
+/* Allocates the object, probe, pattern stack, work buffers and device
+ * scalars on the current device.  `stream` may be NULL (a stream of its own). */
+int cdx_pty_create(const cdx_pty_params* p, void* stream, cdx_pty** out);
+int cdx_pty_destroy(cdx_pty* t);
+
+/* Scan positions in object pixels (scanposx/scanposy, util/ptycho.cpp:46-47):
+ * the window of position i starts at round(x_i), round(y_i); the overlap mask
+ * takes them truncated, as the reference's int parameters do. */
+int cdx_pty_set_scan(cdx_pty* t, const float* posx, const float* posy);
+
+/* nscan stacked rows x cols patterns in FFT (unshifted) order, scaled by
+ * 1/exposure, as ptycho::patterns holds them (util/ptycho.cpp:355-358, 713-716). */
+int cdx_pty_set_patterns(cdx_pty* t, const float* patterns);
+int cdx_pty_get_patterns(cdx_pty* t, float* patterns);
+
+int cdx_pty_set_object(cdx_pty* t, const float* obj);     /* obj_rows x obj_cols complex */
+int cdx_pty_get_object(cdx_pty* t, float* obj);
+int cdx_pty_set_probe(cdx_pty* t, const float* probe);    /* rows x cols complex, sample plane */
+int cdx_pty_get_probe(cdx_pty* t, float* probe);
+/* The probe back-propagated to the pupil plane, which is what the reference
+ * leaves in pupilpatternWave after iterate() (util/ptycho.cpp:705). */
+int cdx_pty_get_pupil(cdx_pty* t, float* pupil);
+
+/* initObject (util/ptycho.cpp:363-369): the object set to unit modulus with a
+ * uniform random phase (a counter-based generator keyed by seed and pixel,
+ * not curand MRG32k3a), the probe to the pupil disk of pupil_size
+ * (pupilFunc, src/gpu/ptycho.cu:123-130) propagated by dpupil. */
+int cdx_pty_init_object(cdx_pty* t, unsigned long long seed);
+
+/* createPattern without detector noise (util/ptycho.cpp:310-359): pattern i =
+ * |FFT(probe * window_i(object))|^2 / (rows cols), from the current object and
+ * probe, stored as the context's patterns. */
+int cdx_pty_simulate(cdx_pty* t);
+
+/* ptycho::iterate: n_iter sweeps starting at iteration index first_iter
+ * (the reference always starts at 0; from index 400 the probe is updated and
+ * constrained).  orders: n_iter x nscan scan indices, one permutation per
+ * sweep, or NULL to draw them as the reference does (shuffle_array with a
+ * rand() stream seeded by `seed`, the generator of the C library restated).
+ * Fresh per-call state as in the reference (zero momentum history and probe
+ * step).  The reference refines scan positions from iteration 500 on; that
+ * step is not built, so first_iter + n_iter must be <= 500.  The final object
+ * has its global phase removed (util/ptycho.cpp:731-735). */
+int cdx_pty_iterate(cdx_pty* t, int first_iter, int n_iter, const int* orders, unsigned int seed);
+
+/* Device time of the last cdx_pty_iterate in milliseconds. */
+int cdx_pty_last_ms(cdx_pty* t, float* ms);
+
+/* The scan orders the reference's rand()-driven shuffle gives for a seed
+ * (n_iter x nscan), for callers that want to log or replay them. */
+int cdx_pty_scan_orders(int nscan, int n_iter, unsigned int seed, int* orders);
+
+#pragma GCC visibility pop
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -25,3 +25,19 @@ $CXX -c "$SHIM/cdxref_stubs.cc" -o "$OUT/obj/cdxref_stubs.o"
 $CXX -c "$SHIM/ref_harness.cc" -o "$OUT/obj/ref_harness.o"
 g++ -o "$OUT/ref_harness" "$OUT"/obj/*.o
 echo "built $OUT/ref_harness"
+
+# Ptychography pin: the reference's ptycho driver (util/ptycho.cpp, compiled
+# into pty_harness.cc), its kernels (src/gpu/ptycho.cu), the propagator and
+# the misc helpers (findMiddle, createCircleMask, shiftWave) it calls.
+PO="$OUT/obj_pty"
+mkdir -p "$PO"
+sed "$LAUNCH" "$REF/src/gpu/ptycho.cu" | $CXX -x c++ - -I"$REF/src/gpu" -c -o "$PO/ptycho.cu.o"
+$CXX -c "$REF/src/post_gpu/propagator.cc" -o "$PO/propagator.cc.o"
+$CXX -c "$REF/src/post_gpu/misc.cc" -o "$PO/misc.cc.o"
+$CXX -DCDXREF_WITH_PROPAGATOR -DCDXREF_WITH_MISC -c "$SHIM/cdxref_stubs.cc" -o "$PO/cdxref_stubs.o"
+$CXX -c "$SHIM/pty_stubs.cc" -o "$PO/pty_stubs.o"
+$CXX -include "$SHIM/cdxref_ptycho.h" -DCDXREF_PTYCHO_CPP="\"$REF/util/ptycho.cpp\"" -c "$SHIM/pty_harness.cc" \
+  -o "$PO/pty_harness.o"
+g++ -o "$OUT/pty_harness" "$PO"/*.o "$OUT/obj/cudaConfig.cu.o" "$OUT/obj/cdi.cu.o" "$OUT/obj/cub_wrap.cu.o" \
+  "$OUT/obj/memManager.cc.o" "$OUT/obj/readConfig.cc.o"
+echo "built $OUT/pty_harness"

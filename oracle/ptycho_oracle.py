@@ -1,0 +1,402 @@
+"""CPU oracle for the ptychographic reconstruction (rPIE object and probe updates).
+
+TEST INFRASTRUCTURE ONLY.  Only ``tests/``, ``__graft_entry__.smoke()`` and the
+``cpu_baseline`` / ``--impl reference`` legs of ``bench.py`` may import this
+module.  It is the checker, never the product: the product path lives in
+``cdixx_gb300`` (``cdx_pty_*`` in include/cdx_ptycho.h).
+
+NumPy restatement of the reference's ``ptycho::iterate`` (util/ptycho.cpp:429-736)
+and the kernels it calls (src/gpu/ptycho.cu, src/gpu/cdi.cu, src/gpu/cudaConfig.cu,
+src/post_gpu/propagator.cc, src/post_gpu/misc.cc), in complex64 / float32 with
+the reference's scalar types (float parameters; the double literals and double
+config fields where the reference has them).  The FFT is the unnormalised DFT
+via NumPy (cuFFT's published transform), reductions accumulate in float64.
+
+Scope: the iteration without Fresnel propagation, Zernike/FISTA pupil steps and
+position refinement (the reference starts refining at iteration 500, so runs
+are limited to 500 iterations).  It is pinned by the reference's own driver
+built as host code (oracle/build_ref.sh -> oracle/_ref/pty_harness).
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+from dataclasses import dataclass
+
+import numpy as np
+
+F32 = np.float32
+C64 = np.complex64
+
+ALPHA = F32(0.1)    # src/gpu/ptycho.cu:5
+BETA = F32(0.5)     # src/gpu/ptycho.cu:6
+UPDATE_PROBE_ITER = 400      # util/ptycho.cpp:441
+POSITION_UPDATE_ITER = 500   # util/ptycho.cpp:442
+
+
+# --------------------------------------------------------------------------- FFT
+def fft2_u(a):
+    """Unnormalised forward 2-D DFT (myFFT, CUFFT_FORWARD)."""
+    return np.fft.fft2(a).astype(C64)
+
+
+def ifft2_u(a):
+    """Unnormalised inverse 2-D DFT (myIFFT, CUFFT_INVERSE)."""
+    n = a.shape[0] * a.shape[1]
+    return (np.fft.ifft2(a) * n).astype(C64)
+
+
+def convert_fo(a):
+    """cudaConvertFO (src/gpu/cudaConfig.cu:202-212): swap the quadrants
+    (an fftshift for the even sizes used here)."""
+    return np.fft.fftshift(a)
+
+
+# ----------------------------------------------------------- rand() and order
+class GlibcRand:
+    """glibc's rand()/srand() through ctypes: the reference shuffles the scan
+    order with rand() (util/ptycho.cpp:28-38) after the process's srand()."""
+
+    def __init__(self, seed: int):
+        self.libc = ctypes.CDLL(None)
+        self.libc.srand(ctypes.c_uint(seed))
+
+    def rand(self) -> int:
+        return int(self.libc.rand())
+
+
+def shuffle_array(order, rng):
+    """shuffle_array (util/ptycho.cpp:28-38): Fisher-Yates from the top with rand() % (i + 1)."""
+    n = len(order)
+    for i in range(n - 1, 0, -1):
+        j = rng.rand() % (i + 1)
+        order[i], order[j] = order[j], order[i]
+
+
+def scan_orders(nscan: int, n_iter: int, seed: int):
+    """The scan order of every iteration: iterOrder starts as the identity and
+    is shuffled in place once per iteration (util/ptycho.cpp:466-469, 512)."""
+    rng = GlibcRand(seed)
+    order = list(range(nscan))
+    out = []
+    for _ in range(n_iter):
+        shuffle_array(order, rng)
+        out.append(list(order))
+    return np.array(out, np.int32).reshape(n_iter, nscan)
+
+
+# --------------------------------------------------------------------- masks
+def circle_mask(rows, cols, x0, y0, r, is_freq=False):
+    """createCircleMask (src/post_gpu/misc.cc:161-170) -> createMask<C_circle>
+    (src/gpu/cudaConfig.cu:1291-1299, C_circle::isInside 93-97): 1 where
+    sqrtf(dx^2 + dy^2) < r, dx = x - x0 in float; the centre is stored in the
+    int members of C_circle (include/cudaConfig.hpp:217-221), so a fractional
+    x0, y0 is truncated."""
+    x = np.arange(rows)[:, None]
+    y = np.arange(cols)[None, :]
+    if is_freq:
+        x = np.where(x >= rows // 2, x - rows // 2, x + rows // 2)
+        y = np.where(y >= cols // 2, y - cols // 2, y + cols // 2)
+    dx = (x - int(F32(x0))).astype(F32)
+    dy = (y - int(F32(y0))).astype(F32)
+    dr = np.sqrt((dx * dx + dy * dy).astype(F32))
+    return (dr < F32(r)).astype(F32)
+
+
+def pupil_func(rows, cols, pupilsize):
+    """pupilFunc (src/gpu/ptycho.cu:123-130): 1 + 0i inside the disk
+    shiftx^2 + shifty^2 <= pupilsize^2 / 4 about (rows/2, cols/2), else 0."""
+    sx = np.arange(rows)[:, None] - rows // 2
+    sy = np.arange(cols)[None, :] - cols // 2
+    ps = F32(pupilsize)
+    inside = (sx * sx + sy * sy).astype(F32) <= F32(ps * ps) / F32(4)
+    return inside.astype(C64)
+
+
+def masksum(rows, cols, obj_rows, obj_cols, scanx, scany, pupil_size):
+    """The overlap mask of util/ptycho.cpp:470-479: a disk of diameter
+    pupilSize at the centre of the probe frame added at every scan position
+    (addWindow, src/gpu/ptycho.cu:35-41; the float position is truncated to
+    int by the call), then bitMap(> 0.5)."""
+    disk = circle_mask(rows, cols, rows >> 1, cols >> 1, F32(np.float64(pupil_size) / 2))
+    acc = np.zeros((obj_rows, obj_cols), F32)
+    for px, py in zip(scanx, scany):
+        sx, sy = int(F32(px)), int(F32(py))
+        _add_window(acc, sx, sy, disk)
+    return (acc > F32(0.5)).astype(F32)
+
+
+def _window_ranges(shape_o, sx, sy, rows, cols):
+    x0, y0 = max(0, -sx), max(0, -sy)
+    x1, y1 = min(rows, shape_o[0] - sx), min(cols, shape_o[1] - sy)
+    return x0, x1, y0, y1
+
+
+def _add_window(obj, sx, sy, win):
+    rows, cols = win.shape
+    x0, x1, y0, y1 = _window_ranges(obj.shape, sx, sy, rows, cols)
+    if x1 > x0 and y1 > y0:
+        obj[x0 + sx:x1 + sx, y0 + sy:y1 + sy] = (win[x0:x1, y0:y1] + obj[x0 + sx:x1 + sx, y0 + sy:y1 + sy]).astype(obj.dtype)
+
+
+def get_window(obj, sx, sy, rows, cols):
+    """getWindow (src/gpu/ptycho.cu:18-24): the rows x cols window at (sx, sy),
+    zero outside the object."""
+    w = np.zeros((rows, cols), obj.dtype)
+    x0, x1, y0, y1 = _window_ranges(obj.shape, sx, sy, rows, cols)
+    if x1 > x0 and y1 > y0:
+        w[x0:x1, y0:y1] = obj[x0 + sx:x1 + sx, y0 + sy:y1 + sy]
+    return w
+
+
+def update_window(obj, sx, sy, win):
+    """updateWindow (src/gpu/ptycho.cu:26-30): write the window back inside the object."""
+    rows, cols = win.shape
+    x0, x1, y0, y1 = _window_ranges(obj.shape, sx, sy, rows, cols)
+    if x1 > x0 and y1 > y0:
+        obj[x0 + sx:x1 + sx, y0 + sy:y1 + sy] = win[x0:x1, y0:y1]
+
+
+def c_round(v) -> int:
+    """round() of the C library (halves away from zero) as passed to an int parameter."""
+    v = float(F32(v))
+    return int(math.floor(abs(v) + 0.5)) * (1 if v >= 0 else -1)
+
+
+# ----------------------------------------------------------------- kernels
+def apply_mod_accurate(F, pattern, norm, scale, bs=None):
+    """applyModAccurate, 4-argument form (src/gpu/cdi.cu:351-388): F * norm,
+    replaced by sqrt(I / |F norm|^2) * F norm except where the beamstop
+    blocks (kept scaled), where |F norm| == 0 (left as it was) and where the
+    pixel is saturated (I >= 0.95 scale and |F norm|^2 >= I: kept scaled)."""
+    mod2 = np.maximum(F32(0), pattern.astype(F32))
+    rx = (F.real * F32(norm)).astype(F32) if norm != 1 else F.real.astype(F32)
+    ry = (F.imag * F32(norm)).astype(F32) if norm != 1 else F.imag.astype(F32)
+    src = (rx * rx + ry * ry).astype(F32)
+    maximum = F32(F32(scale) * F32(0.95))
+    with np.errstate(divide="ignore", invalid="ignore"):
+        s = np.sqrt((mod2 / np.where(src == 0, F32(1), src)).astype(F32))
+    keep = (mod2 >= maximum) & (src >= mod2)
+    s = np.where(keep, F32(1), s).astype(F32)
+    out = ((s * rx).astype(F32) + 1j * (s * ry).astype(F32)).astype(C64)
+    out = np.where(src == 0, F, out)
+    if bs is not None:
+        blocked = bs > F32(0.5)
+        out = np.where(blocked, (rx + 1j * ry).astype(C64), out)
+    return out.astype(C64)
+
+
+def _rpie_denom(source_mod2, maxi, param, stepsize):
+    """The denominator of rPIE / rPIE_step (src/gpu/ptycho.cu:55-68):
+    stepsize / ((1 - param) |s|^2 + param max(maxi, 1e-5)), the max and the
+    sum in double (max(float, double)), the result stored as float."""
+    a = ((F32(1) - F32(param)) * source_mod2).astype(F32).astype(np.float64)
+    b = np.float64(F32(param)) * max(np.float64(F32(maxi)), 1e-5)
+    return (np.float64(stepsize) / (a + b)).astype(F32)
+
+
+def rpie(target, source, diff, maxi, param, stepsize=1.0):
+    """rPIE (src/gpu/ptycho.cu:55-61): target -= conj(source) diff * denom."""
+    sx, sy = source.real.astype(F32), source.imag.astype(F32)
+    dx, dy = diff.real.astype(F32), diff.imag.astype(F32)
+    d = _rpie_denom((sx * sx + sy * sy).astype(F32), maxi, param, stepsize)
+    tx = (target.real - ((sx * dx + sy * dy).astype(F32) * d).astype(F32)).astype(F32)
+    ty = (target.imag - ((sx * dy - sy * dx).astype(F32) * d).astype(F32)).astype(F32)
+    return (tx + 1j * ty).astype(C64)
+
+
+def rpie_step(source, diff, maxi, param):
+    """rPIE_step (src/gpu/ptycho.cu:62-68): -conj(source) diff * denom (stepsize 1)."""
+    sx, sy = source.real.astype(F32), source.imag.astype(F32)
+    dx, dy = diff.real.astype(F32), diff.imag.astype(F32)
+    d = _rpie_denom((sx * sx + sy * sy).astype(F32), maxi, param, 1.0)
+    return (-((sx * dx + sy * dy).astype(F32) * d) - 1j * ((sx * dy - sy * dx).astype(F32) * d)).astype(C64)
+
+
+def angular_spectrum(field, lam, distance, pixelsize, reverse=False):
+    """propagator::angularSpectrumPropagate / ...Reverse (src/post_gpu/propagator.cc:31-49)
+    with multiplyPropagatePhase (src/gpu/cudaConfig.cu:669-679): FFT, 1/(rows cols),
+    centre, multiply by exp(i a sqrt(1 - ((x - r/2)^2 + (y - c/2)^2) b)) (0 where
+    the root is imaginary), uncentre, inverse FFT.  The propagator's members are
+    float; a = 2 pi distance / lambda is evaluated in double."""
+    rows, cols = field.shape
+    lam32, dist32, ps32 = F32(lam), F32(distance), F32(pixelsize)
+    if not reverse:
+        a = F32(2 * math.pi * np.float64(dist32) / np.float64(lam32))
+        loi = F32(lam32 / F32(ps32 * F32(rows)))
+        b = F32(loi * loi)
+    else:
+        a = F32(-2 * math.pi * np.float64(dist32) / np.float64(lam32))
+        iol = F32(F32(ps32 * F32(rows)) / lam32)
+        b = F32(1.0 / np.float64(F32(iol * iol)))
+    out = fft2_u(field)
+    out = (out * F32(1.0 / (rows * cols))).astype(C64)
+    out = convert_fo(out)
+    x = np.arange(rows)[:, None] - (rows >> 1)
+    y = np.arange(cols)[None, :] - (cols >> 1)
+    square = (F32(1) - ((x * x + y * y).astype(F32) * b).astype(F32)).astype(F32)
+    ok = square >= 0
+    phase = (a * np.sqrt(np.where(ok, square, F32(0))).astype(F32)).astype(F32)
+    ph = phase.astype(np.float64)
+    fac = (np.cos(ph) + 1j * np.sin(ph)).astype(C64)
+    out = np.where(ok, (out * fac).astype(C64), 0).astype(C64)
+    out = convert_fo(out)
+    return ifft2_u(out)
+
+
+def find_middle(m):
+    """findMiddle of a float field (src/post_gpu/misc.cc:27-42) with multiplyx/multiplyy
+    (src/gpu/cudaConfig.cu:1427-1437): centroid in units of the size, coordinate
+    (x + 0.5)/rows - 0.5 (in double), sums then a float division."""
+    rows, cols = m.shape
+    m64 = m.astype(np.float64)
+    cx = ((np.arange(rows) + 0.5) / rows - 0.5)[:, None]
+    cy = ((np.arange(cols) + 0.5) / cols - 0.5)[None, :]
+    wx = (m64 * cx).astype(F32).astype(np.float64)
+    wy = (m64 * cy).astype(F32).astype(np.float64)
+    s = F32(m64.sum())
+    return F32(F32(wx.sum()) / s), F32(F32(wy.sum()) / s)
+
+
+def multiply_shift(wave, shiftx, shifty):
+    """multiplyShift (src/gpu/cudaConfig.cu:373-378): wave * exp(-2 pi i (shiftx (x - r/2)/r
+    + shifty (y - c/2)/c)), the bracket in float."""
+    rows, cols = wave.shape
+    x = (np.arange(rows) - rows // 2).astype(F32)[:, None]
+    y = (np.arange(cols) - cols // 2).astype(F32)[None, :]
+    t = ((F32(shiftx) * x).astype(F32) / F32(rows)).astype(F32) + ((F32(shifty) * y).astype(F32) / F32(cols)).astype(F32)
+    ph = (F32(-2 * math.pi) * t.astype(F32)).astype(F32).astype(np.float64)
+    return (wave * (np.cos(ph) + 1j * np.sin(ph)).astype(C64)).astype(C64)
+
+
+# --------------------------------------------------------------- the driver
+@dataclass
+class PtyParams:
+    """The config fields ``ptycho::iterate`` reads (include/readConfig.hpp:25-35; REALVAR are double)."""
+    lam: float = 0.5
+    d: float = 2e4
+    dpupil: float = 1e3
+    pixelsize: float = 20.0
+    pupil_size: float = 32.0
+    exposure: float = 1.0
+    mpie: bool = True
+    use_bs: bool = False
+    beam_stop_size: int = 5
+
+    def resolution(self, rows):
+        """resolution = lambda d / pixelsize / row (util/ptycho.cpp:246), stored as float."""
+        return F32(self.lam * self.d / self.pixelsize / rows)
+
+
+def simulate_patterns(obj, probe, scanx, scany, exposure=1.0):
+    """The noise-free part of ptycho::createPattern (util/ptycho.cpp:310-359):
+    I_i = |FFT(P O_window)|^2 / (rows cols), times exposure then times float(1/exposure)."""
+    rows, cols = probe.shape
+    out = []
+    for px, py in zip(scanx, scany):
+        w = get_window(obj, c_round(px), c_round(py), rows, cols)
+        F = fft2_u((probe * w).astype(C64))
+        I = ((F.real * F.real + F.imag * F.imag).astype(F32) * F32(1.0 / (rows * cols))).astype(F32)
+        I = (I * F32(exposure)).astype(F32)
+        I = (I * F32(1.0 / exposure)).astype(F32)
+        out.append(I)
+    return np.stack(out)
+
+
+def iterate(obj0, probe0, patterns, scanx, scany, n_iter, params: PtyParams, orders, start_iter=0):
+    """ptycho::iterate (util/ptycho.cpp:429-736) for n_iter <= 500: per scan
+    position (in the given order) the window times the probe, FFT, applyModAccurate,
+    inverse FFT, the difference of exit waves and the rPIE object update
+    (updateObject; from iteration 400 updateObjectAndProbeStep with the probe
+    step accumulated and added after the sweep, the object clamped and the
+    object/probe scales balanced first); from iteration 400 the pupil
+    constraint after the sweep (back-propagate, disk of pupilSize, propagate,
+    recentre the far field); mPIE momentum (FISTA-type, with the global phase
+    of the covered object removed) when enabled.  After the last iteration the
+    probe is back-propagated to the pupil plane and the object's global phase
+    removed, as the reference leaves them.  Returns (object, pupil)."""
+    rows, cols = probe0.shape
+    orow, ocol = obj0.shape
+    if n_iter > POSITION_UPDATE_ITER:
+        raise ValueError("position refinement (iterations >= 500) is outside this restatement")
+    O = obj0.astype(C64).copy()
+    Oprev = np.zeros_like(O)
+    P = probe0.astype(C64).copy()
+    step = np.zeros_like(P)
+    nscan = len(scanx)
+    norm = F32(1.0 / math.sqrt(rows * cols))
+    scale = F32(1.0 / params.exposure)
+    probe_step_size = F32(1.0 / nscan)
+    pd = int(params.pupil_size)
+    res = params.resolution(rows)
+    pupil_support = circle_mask(pd, pd, F32((pd + 1) / 2.0), F32((pd + 1) / 2.0), F32(pd / 2.0))
+    msum = masksum(rows, cols, orow, ocol, scanx, scany, params.pupil_size)
+    bs = circle_mask(rows, cols, rows >> 1, cols >> 1, params.beam_stop_size, True) if params.use_bs else None
+    tk = F32(0.5 + math.sqrt(1.25))
+    wins = [(c_round(F32(x)), c_round(F32(y))) for x, y in zip(scanx, scany)]
+    for it in range(start_iter, start_iter + n_iter):
+        probe_max = F32(np.max((P.real * P.real + P.imag * P.imag).astype(F32)))
+        obj_max = F32(0)
+        if it >= UPDATE_PROBE_ITER:
+            m2 = ((O.real * O.real + O.imag * O.imag).astype(F32) * msum).astype(F32)
+            obj_max = F32(np.max(m2))
+            thr = F32(math.sqrt(obj_max))
+            om2 = (O.real * O.real + O.imag * O.imag).astype(F32)
+            big = om2 > thr
+            with np.errstate(divide="ignore", invalid="ignore"):
+                f = np.sqrt((thr / np.where(big, om2, F32(1))).astype(F32)).astype(F32)
+            O = np.where(big, ((f * O.real).astype(F32) + 1j * (f * O.imag).astype(F32)), O).astype(C64)
+            sf = F32((np.float64(F32(probe_max / obj_max))) ** 0.25)
+            O = (O * sf).astype(C64)
+            Oprev = (Oprev * sf).astype(C64)
+            P = (P * F32(1.0 / np.float64(sf))).astype(C64)
+            obj_max = probe_max = F32(math.sqrt(np.float64(F32(obj_max * probe_max))))
+        for i in orders[it - start_iter]:
+            sx, sy = wins[i]
+            w = get_window(O, sx, sy, rows, cols)
+            esw = (P * w).astype(C64)
+            F = fft2_u(esw)
+            F = apply_mod_accurate(F, patterns[i], norm, scale, bs)
+            F = (ifft2_u(F) * norm).astype(C64)
+            diff = (esw - F).astype(C64)
+            if it < UPDATE_PROBE_ITER:
+                w = rpie(w, P, diff, probe_max, ALPHA, 1.0)
+            else:
+                w = rpie(w, P, diff, probe_max, ALPHA, 0.5)
+                step = (step + (rpie_step(w, diff, obj_max, BETA) * probe_step_size)).astype(C64)
+            update_window(O, sx, sy, w)
+        if it >= UPDATE_PROBE_ITER:
+            P = (P + step).astype(C64)
+            step = (step * F32(0)).astype(C64)
+            P = angular_spectrum(P, params.lam, params.dpupil, res, reverse=True)
+            r0, c0 = (rows - pd) // 2, (cols - pd) // 2
+            crop = P[r0:r0 + pd, c0:c0 + pd] * (pupil_support > F32(0.5))
+            P = np.zeros_like(P)
+            P[r0:r0 + pd, c0:c0 + pd] = crop
+            P = angular_spectrum(P, params.lam, params.dpupil, res, reverse=False)
+            far = convert_fo(fft2_u(P))
+            mx, my = find_middle((far.real * far.real + far.imag * far.imag).astype(F32))
+            P = multiply_shift(P, F32(np.float64(F32(mx * F32(rows))) - 0.5), F32(np.float64(F32(my * F32(cols))) - 0.5))
+        if params.mpie:
+            s = (O * msum).astype(C64).astype(np.complex128).sum()
+            s = complex(np.complex64(s))
+            s = np.complex64(s / abs(s))
+            O = (O * np.conj(s)).astype(C64)
+            Oprev = (Oprev * np.conj(s)).astype(C64)
+            Oprev = (O - Oprev).astype(C64)
+            tkp1 = F32(0.5 + math.sqrt(0.25 + np.float64(F32(tk * tk))))
+            c = F32(F32(tk - F32(1)) / tkp1)
+            Oprev = (O + (Oprev * c).astype(C64)).astype(C64)
+            O, Oprev = Oprev, O
+            tk = tkp1
+    pupil = angular_spectrum(P, params.lam, params.dpupil, res, reverse=True)
+    s = complex(np.complex64(O.astype(np.complex128).sum()))
+    s = np.complex64(s / F32(math.hypot(s.real, s.imag)))
+    O = (O * np.conj(s)).astype(C64)
+    return O, pupil, P
+
+
+def rel_err(a, b):
+    a = np.asarray(a, np.complex128)
+    b = np.asarray(b, np.complex128)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))

@@ -66,14 +66,18 @@ extern "C" void writeFloatImage(const char* name, void* data, int row, int colum
   fwrite(data, sizeof(Real), (size_t)row * column, f);
   fclose(f);
 }
+#ifndef CDXREF_WITH_MISC
 complexFormat findMiddle(Real*, int) { return 0; }
 complexFormat findMiddle(complexFormat*, int) { return 0; }
 Real* createBeamStop(int, int, int) { abort(); }
 void readComplexWaveFront(const char*, const char*, Real*&, Real*&, int&, int&) { abort(); }
+#endif
 void FISTA(Real*, Real*, Real, int, void (*)(Real*, Real*)) { abort(); }
 mnistData::mnistData(const char*) {}
 mnistData::~mnistData() {}
 cuMnist::cuMnist(const char* d, int, int, int, int) : mnistData(d) {}
 void cuMnist::cuRead(void*) { abort(); }
+#ifndef CDXREF_WITH_PROPAGATOR
 void propagator::multiplyFresnelPhase(complexFormat*) { abort(); }
 void propagator::removeFresnelPhase(complexFormat*) { abort(); }
+#endif

@@ -1,4 +1,5 @@
 #pragma once
+#include <string>
 #include "core.h"
 namespace fmt {
 struct ostream {
@@ -7,4 +8,5 @@ struct ostream {
   void close() { if (f) fclose(f); f = nullptr; }
 };
 inline ostream output_file(const char* name) { return ostream{fopen(name, "w")}; }
+inline ostream output_file(const std::string& name) { return ostream{fopen(name.c_str(), "w")}; }
 }  // namespace fmt

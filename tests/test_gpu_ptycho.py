@@ -1,0 +1,142 @@
+"""GPU parity of the ptychographic reconstruction (include/cdx_ptycho.h) against
+the reference's own ptycho::iterate runs (tests/golden/ptycho_cases.npz) and
+against the oracle (oracle/ptycho_oracle.py) one sweep at a time, plus the
+set-up steps (initObject, createPattern) and the argument checks."""
+import numpy as np
+import pytest
+
+from oracle import ptycho_oracle as PO
+from tests.test_ptycho_oracle import CASES, load, obj_bound, pupil_bound
+
+pytestmark = pytest.mark.gpu
+
+# One sweep from the same state: float32 rounding of two FFT implementations.
+STEP_BOUND = 1e-5
+
+
+@pytest.fixture(scope="module")
+def PT(cdx):
+    from cdixx_gb300 import ptycho
+    return ptycho
+
+
+def make(PT, c, prm, rows=None, obj_shape=None):
+    rows = rows or c["probe0"].shape[0]
+    orow, ocol = obj_shape or c["obj0"].shape
+    t = PT.Ptycho(rows, c["probe0"].shape[1], orow, ocol, c["scanx"], c["scany"], lam=prm.lam, d=prm.d,
+                  dpupil=prm.dpupil, pixelsize=prm.pixelsize, pupil_size=prm.pupil_size, exposure=prm.exposure,
+                  mpie=prm.mpie, use_bs=prm.use_bs, beam_stop_size=prm.beam_stop_size)
+    t.objectWave = c["obj0"]
+    t.probe = c["probe0"]
+    t.patterns = c["pats"]
+    return t
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_gpu_matches_reference_run(PT, name):
+    c, prm, n_iter, seed = load(name)
+    with make(PT, c, prm) as t:
+        t.iterate(n_iter, orders=c["orders"])
+        assert PO.rel_err(t.objectWave, c["ref_object"]) < 2 * obj_bound(name)
+        assert PO.rel_err(t.pupil, c["ref_pupil"]) < 2 * pupil_bound(name)
+
+
+def test_gpu_draws_the_reference_orders_from_the_seed(PT):
+    c, prm, n_iter, seed = load("obj20_nompie")
+    with make(PT, c, prm) as a, make(PT, c, prm) as b:
+        a.iterate(n_iter, seed=seed)
+        b.iterate(n_iter, orders=c["orders"])
+        assert np.array_equal(a.objectWave, b.objectWave)
+
+
+@pytest.mark.parametrize("first", [0, 7, 400, 450])
+@pytest.mark.parametrize("mpie", [False, True])
+def test_one_sweep_matches_oracle(PT, first, mpie):
+    """Per-iterate parity: one sweep (object phase, or probe phase from 400) from
+    the same object and probe as the oracle."""
+    c, prm, _n, _s = load("obj3")
+    prm.mpie = mpie
+    rng = np.random.default_rng(first)
+    obj = (c["obj0"] * (0.5 + rng.random(c["obj0"].shape))).astype(np.complex64)
+    orders = np.array([rng.permutation(len(c["scanx"]))], np.int32)
+    with make(PT, c, prm) as t:
+        t.objectWave = obj
+        t.iterate(1, first_iter=first, orders=orders)
+        O, pupil, P = PO.iterate(obj, c["probe0"], c["pats"], c["scanx"], c["scany"], 1, prm, orders, start_iter=first)
+        assert PO.rel_err(t.objectWave, O) < STEP_BOUND
+        assert PO.rel_err(t.probe, P) < STEP_BOUND
+        assert PO.rel_err(t.pupil, pupil) < STEP_BOUND
+
+
+def test_large_sweep_matches_oracle_and_reconstructs(PT):
+    """256^2 probe on a 640^2 object, 16 positions: one sweep against the oracle,
+    then 60 sweeps lower the far-field error of the simulated data."""
+    R, RO = 256, 640
+    prm = PO.PtyParams(lam=0.5, d=2e5, dpupil=2e3, pixelsize=20.0, pupil_size=160.0, exposure=1.0, mpie=True)
+    res = prm.resolution(R)
+    rng = np.random.default_rng(3)
+    x = np.linspace(-1, 1, RO)[:, None]
+    y = np.linspace(-1, 1, RO)[None, :]
+    truth = ((0.6 + 0.4 * np.cos(5 * x) * np.sin(3 * y)) * np.exp(1.5j * np.sin(4 * x + 2 * y))).astype(np.complex64)
+    probe = PO.angular_spectrum(PO.pupil_func(R, R, prm.pupil_size), prm.lam, prm.dpupil, res)
+    sx = np.array([60 + 80 * i + 0.4 * j for i in range(4) for j in range(4)], np.float32)
+    sy = np.array([60 + 80 * j + 0.7 * i for i in range(4) for j in range(4)], np.float32)
+    pats = PO.simulate_patterns(truth, probe, sx, sy)
+    pats = (pats / pats.max() * 0.9).astype(np.float32)
+    obj0 = np.exp(2j * np.pi * rng.random((RO, RO))).astype(np.complex64)
+    c = {"obj0": obj0, "probe0": probe, "pats": pats, "scanx": sx, "scany": sy}
+    orders = PO.scan_orders(16, 1, 5)
+    with make(PT, c, prm) as t:
+        t.iterate(1, orders=orders)
+        O, _pu, _P = PO.iterate(obj0, probe, pats, sx, sy, 1, prm, orders)
+        assert PO.rel_err(t.objectWave, O) < STEP_BOUND
+
+        def far_error(obj):
+            sim = PO.simulate_patterns(obj, probe, sx, sy)
+            return float(np.abs(np.sqrt(sim) - np.sqrt(pats)).sum() / np.sqrt(pats).sum())
+
+        e0 = far_error(t.objectWave)
+        t.iterate(60, seed=9)
+        e1 = far_error(t.objectWave)
+        assert e1 < 0.5 * e0, (e0, e1)
+
+
+def test_simulate_matches_oracle(PT):
+    c, prm, _n, _s = load("offedge")
+    with make(PT, c, prm) as t:
+        rng = np.random.default_rng(1)
+        truth = (np.exp(1j * rng.random(c["obj0"].shape)) * rng.random(c["obj0"].shape)).astype(np.complex64)
+        t.objectWave = truth
+        t.createPattern()
+        ref = PO.simulate_patterns(truth, c["probe0"], c["scanx"], c["scany"], prm.exposure)
+        got = t.patterns
+        assert got.shape == ref.shape
+        assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 2e-6
+
+
+def test_init_object_matches_oracle(PT):
+    c, prm, _n, _s = load("obj3")
+    with make(PT, c, prm) as t:
+        t.initObject(seed=4)
+        o = t.objectWave
+        assert np.allclose(np.abs(o), 1, atol=2e-6)
+        ph = np.angle(o)
+        assert ph.std() > 1.5   # uniform phase on (-pi, pi]: std pi/sqrt(3)
+        ref = PO.angular_spectrum(PO.pupil_func(32, 32, prm.pupil_size), prm.lam, prm.dpupil, prm.resolution(32))
+        assert PO.rel_err(t.probe, ref) < 2e-6
+
+
+def test_argument_checks(PT, cdx):
+    c, prm, _n, _s = load("obj3")
+    with make(PT, c, prm) as t:
+        with pytest.raises(cdx.CdxError):
+            t.iterate(10, first_iter=495)          # position refinement from 500 is not built
+        bad = c["orders"][:2].copy()
+        bad[0, 0] = 99
+        with pytest.raises(cdx.CdxError):
+            t.iterate(2, orders=bad)
+    with pytest.raises(cdx.CdxError) as e:
+        PT.Ptycho(40, 40, 64, 64, c["scanx"], c["scany"], lam=0.5, d=2e4, dpupil=1e3, pixelsize=20, pupil_size=16)
+    assert e.value.code == cdx.CDX_ERR_SIZE
+    with pytest.raises(cdx.CdxError):
+        PT.Ptycho(32, 32, 64, 64, c["scanx"], c["scany"], lam=0.5, d=2e4, dpupil=1e3, pixelsize=20, pupil_size=40)
