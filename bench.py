@@ -284,6 +284,67 @@ def batched_section():
             "contexts": len(ctxs), "launch": "one CUDA graph (cdx_group) with one branch per size"}
 
 
+# Ptychography: the reference's own configuration (html/default/ptycho.cfg optics,
+# 512^2 probe, row_O = column_O = 1280, initScan_triangle with stepSize 250).
+PTY_R, PTY_RO, PTY_STEP = 512, 1280, 250.0
+PTY_OPTICS = dict(lam=0.6328, d=125e3, dpupil=6.8e3, pixelsize=13.0, pupil_size=335.0083, exposure=0.01)
+PTY_SWEEPS = 100
+
+
+def ptycho_section(cpu=True):
+    """rPIE + mPIE sweeps (ptycho::iterate, object phase) on the reference's
+    configuration with noise-free simulated patterns of a smooth synthetic object:
+    sweeps/s from CUDA events around cdx_pty_iterate, a probe-phase sweep time,
+    the roofline of a sweep and the oracle on one sweep as the CPU baseline."""
+    from cdixx_gb300 import ptycho as PT
+    sx, sy = PT.scan_triangle(PTY_RO, PTY_RO, PTY_R, PTY_R, PTY_STEP)
+    t = PT.Ptycho(PTY_R, PTY_R, PTY_RO, PTY_RO, sx, sy, **PTY_OPTICS)
+    x = np.linspace(-1, 1, PTY_RO, dtype=np.float32)[:, None]
+    y = np.linspace(-1, 1, PTY_RO, dtype=np.float32)[None, :]
+    truth = ((0.6 + 0.4 * np.cos(9 * x) * np.sin(7 * y)) * np.exp(1.2j * np.sin(5 * x + 3 * y))).astype(np.complex64)
+    t.initObject(seed=SEED)
+    obj0, probe0 = t.objectWave, t.probe
+    t.objectWave = truth
+    t.createPattern()
+    t.objectWave = obj0
+    t.iterate(3, seed=1)                      # warm-up (graph capture)
+    t.objectWave = obj0
+    t.probe = probe0
+    ms = t.iterate(PTY_SWEEPS, seed=1)
+    sweeps_s = PTY_SWEEPS / (ms / 1000.0)
+    t.probe = probe0
+    ms_probe = t.iterate(20, first_iter=400, seed=2)
+    n, on, ns = PTY_R * PTY_R, PTY_RO * PTY_RO, len(sx)
+    # algorithmic bytes of a sweep: per position the object window read and written,
+    # the probe and the pattern read (8 + 8 + 8 + 4 B/px); the momentum step reads the
+    # object, its history and the overlap mask and writes both (36 B/px of the object)
+    alg = ns * 28 * n + 36 * on
+    achieved = alg / (ms / PTY_SWEEPS / 1000.0) / 1e9
+    peak, peak_kind = peaks()
+    out = {"metric": "ptycho sweeps/s", "value": sweeps_s, "positions_per_s": sweeps_s * ns,
+           "config": {"probe": PTY_R, "object": PTY_RO, "positions": ns, "scan": "initScan_triangle, stepSize 250",
+                      "optics": PTY_OPTICS, "sweeps": PTY_SWEEPS, "mPIE": True,
+                      "data": "noise-free patterns of a synthetic smooth object (createPattern)"},
+           "ms_per_sweep": ms / PTY_SWEEPS, "ms_per_probe_phase_sweep": ms_probe / 20,
+           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                        "alg_bytes_per_sweep": alg, "peak_kind": peak_kind},
+           "gpu_launches_per_sweep": 3 * ns + 8}
+    if cpu:
+        from oracle import ptycho_oracle as PO
+        prm = PO.PtyParams(lam=PTY_OPTICS["lam"], d=PTY_OPTICS["d"], dpupil=PTY_OPTICS["dpupil"],
+                           pixelsize=PTY_OPTICS["pixelsize"], pupil_size=PTY_OPTICS["pupil_size"],
+                           exposure=PTY_OPTICS["exposure"], mpie=True)
+        pats = t.patterns
+        orders = PO.scan_orders(ns, 1, 1)
+        t0 = time.perf_counter()
+        PO.iterate(obj0, probe0, pats, sx, sy, 1, prm, orders)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": 1.0 / dt, "unit": "sweeps/s", "cores": 1, "kind": "port",
+                               "sample": f"1 sweep of the same case, NumPy oracle ({dt:.2f} s)"}
+    t.close()
+    return out
+
+
 def run_gpu(args):
     import torch
     from cdixx_gb300 import native as cdx
@@ -382,7 +443,9 @@ def run_gpu(args):
         cpu = {"value": v, "unit": "iter/s", "cores": threads, "kind": "port",
                "sample": "2 RAAR iterations of the 2048^2 pattern, float32 oracle, "
                          f"scipy.fft with {threads} workers ({dt:.2f} s)"}
-    warm = batched = None
+    warm = batched = pty = None
+    if rank == 0 and not args.no_ptycho:
+        pty = ptycho_section(cpu=not args.no_cpu)
     if rank == 0 and not args.no_warm:
         warm = warm_start_section()
     if rank == 0 and not args.no_batched:
@@ -406,6 +469,7 @@ def run_gpu(args):
             "gpu_launches": launches_per_step * args.steps,
             "warm_start": warm,
             "batched": batched,
+            "ptycho": pty,
         }
         print(json.dumps(line))
     ctx.close()
@@ -423,6 +487,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-warm", action="store_true", help="skip the learned warm-start section")
     ap.add_argument("--no-batched", action="store_true", help="skip the uneven-size batch section")
+    ap.add_argument("--no-ptycho", action="store_true", help="skip the ptychography section")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -32,6 +32,33 @@ def _c64(a, shape):
     return a
 
 
+def scan_triangle(row_O, column_O, row, column, step_size):
+    """ptycho::initScan_triangle (util/ptycho.cpp:139-175): a 3 x 3 grid without
+    its (2, 1) point, odd columns shifted by half a step (the middle column
+    stretched), centred on the object; positions in object pixels (float)."""
+    sx, sy = [], []
+    maxx = maxy = 0
+    minx = miny = row_O
+    for i in range(3):
+        for j in range(3):
+            if i == 2 and j == 1:
+                continue
+            xstep = np.float32(i + (0 if j % 2 == 0 else 0.5))
+            ystep = np.float32(j * 1)
+            if j == 1:
+                xstep = np.float32(xstep * 2 - 1)
+            py = np.float32(xstep * np.float32(step_size))
+            px = np.float32(ystep * np.float32(step_size))
+            sx.append(px)
+            sy.append(py)
+            maxx, maxy = max(maxx, int(px)), max(maxy, int(py))   # the int bounds truncate
+            minx, miny = min(minx, int(px)), min(miny, int(py))
+    ox = (minx + maxx - row_O + row) >> 1
+    oy = (miny + maxy - column_O + column) >> 1
+    return (np.array(sx, np.float32) - np.float32(ox)).astype(np.float32), \
+        (np.array(sy, np.float32) - np.float32(oy)).astype(np.float32)
+
+
 def scan_orders(nscan: int, n_iter: int, seed: int) -> np.ndarray:
     """The per-sweep scan orders the reference's shuffle_array gives after srand(seed)."""
     out = np.zeros((n_iter, nscan), np.int32)
