@@ -328,7 +328,7 @@ def ptycho_section(cpu=True):
            "ms_per_sweep": ms / PTY_SWEEPS, "ms_per_probe_phase_sweep": ms_probe / 20,
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                         "alg_bytes_per_sweep": alg, "peak_kind": peak_kind},
-           "gpu_launches_per_sweep": 3 * ns + 8}
+           "gpu_launches_per_sweep": 3 * ns + 4}
     if cpu:
         from oracle import ptycho_oracle as PO
         prm = PO.PtyParams(lam=PTY_OPTICS["lam"], d=PTY_OPTICS["d"], dpupil=PTY_OPTICS["dpupil"],

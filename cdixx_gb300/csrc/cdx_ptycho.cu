@@ -54,7 +54,7 @@ CDX_PTY_EXTERN(3072) CDX_PTY_EXTERN(4096)
 
 namespace {
 
-constexpr int kRedBlocks = 152;        // reduction CTAs (one per SM)
+constexpr int kRedBlocks = 608;        // reduction CTAs (four per SM); the fused finalisers assume 256 threads
 constexpr int kUpdateProbeIter = 400;  // util/ptycho.cpp:441
 constexpr int kPositionUpdateIter = 500;   // util/ptycho.cpp:442
 
@@ -92,8 +92,42 @@ inline unsigned grid1(long long n, int t = 256) {
 }
 
 // ------------------------------------------------------------------ kernels
+// util/ptycho.cpp:485-509: the probe maximum; from iteration 400 the object
+// maximum over the covered area, its threshold, the scale balance
+// sf = (max|P|^2 / objMax)^(1/4) and the balanced maxima sqrt(objMax max|P|^2).
+__device__ void pty_balance(PtyScal* s, int probe_phase) {
+  const float pm = __uint_as_float(atomicAdd(&s->maxb[0], 0u));
+  s->pmax = pm;
+  if (!probe_phase) return;
+  const float om = __uint_as_float(atomicAdd(&s->maxb[1], 0u));
+  s->thr = sqrtf(om);
+  const float sf = (float)pow((double)(pm / om), 0.25);
+  s->sf = sf;
+  s->isf = (float)(1.0 / (double)sf);
+  const float m = sqrtf(om * pm);
+  s->pmax = m;
+  s->omax = m;
+}
+
+// True in one thread of the CTA that finishes last (the others' results are
+// then visible); that thread resets the counter for the next launch.
+__device__ __forceinline__ bool pty_last_block(unsigned* count) {
+  __shared__ bool last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(count, 1u) == gridDim.x - 1;
+    if (last) *count = 0;
+  }
+  __syncthreads();
+  if (last) __threadfence();
+  return last;
+}
+
+// max |x|^2 (times the mask) as float bits by atomic max; the CTA that
+// finishes last computes the balance (balance < 0: none)
 __global__ void k_pty_max_mod2(const float2* __restrict__ x, const float* __restrict__ mask, long long n,
-                               unsigned* out) {
+                               unsigned* out, PtyScal* s, unsigned* count, int balance) {
   float m = 0.f;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const float2 v = x[i];
@@ -103,23 +137,8 @@ __global__ void k_pty_max_mod2(const float2* __restrict__ x, const float* __rest
   }
   for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
   if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));
-}
-
-// util/ptycho.cpp:485-509: the probe maximum; from iteration 400 the object
-// maximum over the covered area, its threshold, the scale balance
-// sf = (max|P|^2 / objMax)^(1/4) and the balanced maxima sqrt(objMax max|P|^2).
-__global__ void k_pty_balance(PtyScal* s, int probe_phase) {
-  const float pm = __uint_as_float(s->maxb[0]);
-  s->pmax = pm;
-  if (!probe_phase) return;
-  const float om = __uint_as_float(s->maxb[1]);
-  s->thr = sqrtf(om);
-  const float sf = (float)pow((double)(pm / om), 0.25);
-  s->sf = sf;
-  s->isf = (float)(1.0 / (double)sf);
-  const float m = sqrtf(om * pm);
-  s->pmax = m;
-  s->omax = m;
+  if (balance < 0) return;
+  if (pty_last_block(count) && threadIdx.x == 0) pty_balance(s, balance);
 }
 
 // applyThreshold(O, O, sqrt(objMax)) (src/gpu/cudaConfig.cu:397-406), then applyNorm by sf of O and its history.
@@ -215,7 +234,8 @@ __global__ void k_pty_pupil_mask(float2* __restrict__ P, int rows, int cols, int
 
 // findMiddle of |cudaConvertFO(FFT(P))|^2 (src/post_gpu/misc.cc:27-42): per-CTA sums of
 // m, m ((x + 0.5)/rows - 0.5), m ((y + 0.5)/cols - 0.5) at the centred coordinates.
-__global__ void k_pty_far_part(const float2* __restrict__ F, int rows, int cols, double* part) {
+__global__ void k_pty_far_part(const float2* __restrict__ F, int rows, int cols, double* part, PtyScal* s,
+                               unsigned* count) {
   __shared__ double red[3][8];
   const long long n = (long long)rows * cols;
   double s0 = 0, s1 = 0, s2 = 0;
@@ -243,14 +263,24 @@ __global__ void k_pty_far_part(const float2* __restrict__ F, int rows, int cols,
     part[3 * blockIdx.x + 1] = t1;
     part[3 * blockIdx.x + 2] = t2;
   }
-}
-// middle = (sum_x / sum, sum_y / sum) in float; multiplyShift(P, mid.x rows - 0.5, mid.y cols - 0.5)
-__global__ void k_pty_far_fin(const double* part, int nb, PtyScal* s, int rows, int cols) {
+  // the CTA that finishes last sums the partials in index order:
+  // middle = (sum_x / sum, sum_y / sum) in float; multiplyShift(P, mid.x rows - 0.5, mid.y cols - 0.5)
+  if (!pty_last_block(count)) return;
+  __shared__ double fin[8];
   double t0 = 0, t1 = 0, t2 = 0;
-  for (int k = 0; k < nb; ++k) { t0 += part[3 * k]; t1 += part[3 * k + 1]; t2 += part[3 * k + 2]; }
-  const float mx = (float)t1 / (float)t0, my = (float)t2 / (float)t0;
-  s->shx = (float)((double)(mx * rows) - 0.5);
-  s->shy = (float)((double)(my * cols) - 0.5);
+  for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) {
+    t0 += __ldcg(part + 3 * k);
+    t1 += __ldcg(part + 3 * k + 1);
+    t2 += __ldcg(part + 3 * k + 2);
+  }
+  t0 = block_sum_d<256>(t0, fin);
+  t1 = block_sum_d<256>(t1, fin);
+  t2 = block_sum_d<256>(t2, fin);
+  if (threadIdx.x == 0) {
+    const float mx = (float)t1 / (float)t0, my = (float)t2 / (float)t0;
+    s->shx = (float)((double)(mx * rows) - 0.5);
+    s->shy = (float)((double)(my * cols) - 0.5);
+  }
 }
 // multiplyShift (src/gpu/cudaConfig.cu:373-378)
 __global__ void k_pty_mshift(float2* __restrict__ P, int rows, int cols, const PtyScal* s) {
@@ -266,16 +296,22 @@ __global__ void k_pty_mshift(float2* __restrict__ P, int rows, int cols, const P
   }
 }
 
-// findSum of O (times the overlap mask for the momentum step), per-CTA partials
-__global__ void k_pty_csum_part(const float2* __restrict__ O, const float* __restrict__ m, long long n, double* part) {
+// findSum of O (times the overlap mask for the momentum step): float sums per
+// thread (the reference's CUB sum is float), double across threads and CTAs in
+// a fixed order; the CTA that finishes last forms the unit phase:
+// sum /= |sum| with cabs in double for the momentum step (util/ptycho.cpp:672-673),
+// with the float hypot for the final phase removal (733)
+__global__ void k_pty_csum(const float2* __restrict__ O, const float* __restrict__ m, long long n, double* part,
+                           PtyScal* s, unsigned* count, int final_phase) {
   __shared__ double red[2][8];
-  double sx = 0, sy = 0;
+  float ax = 0.f, ay = 0.f;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     float2 v = O[i];
     if (m) { const float f = m[i]; v.x *= f; v.y *= f; }
-    sx += v.x;
-    sy += v.y;
+    ax += v.x;
+    ay += v.y;
   }
+  double sx = ax, sy = ay;
   for (int o = 16; o; o >>= 1) {
     sx += __shfl_xor_sync(0xffffffffu, sx, o);
     sy += __shfl_xor_sync(0xffffffffu, sy, o);
@@ -289,12 +325,16 @@ __global__ void k_pty_csum_part(const float2* __restrict__ O, const float* __res
     part[2 * blockIdx.x] = a;
     part[2 * blockIdx.x + 1] = b;
   }
-}
-// sum /= |sum|: cabs in double for the momentum step (util/ptycho.cpp:672-673), hypot of
-// the float parts for the final phase removal (733)
-__global__ void k_pty_csum_fin(const double* part, int nb, PtyScal* s, int final_phase) {
+  if (!pty_last_block(count)) return;
+  __shared__ double fin[8];
   double a = 0, b = 0;
-  for (int k = 0; k < nb; ++k) { a += part[2 * k]; b += part[2 * k + 1]; }
+  for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) {
+    a += __ldcg(part + 2 * k);
+    b += __ldcg(part + 2 * k + 1);
+  }
+  a = block_sum_d<256>(a, fin);
+  b = block_sum_d<256>(b, fin);
+  if (threadIdx.x != 0) return;
   const float re = (float)a, im = (float)b;
   if (final_phase) {
     const float h = hypotf(re, im);
@@ -483,6 +523,7 @@ struct cdx_pty {
   int *order = nullptr, *iter = nullptr;
   PtyScal* scal = nullptr;
   double* part = nullptr;
+  unsigned* cnt = nullptr;   // last-CTA tickets of the fused reductions (reset by their last CTA)
   int order_cap = 0, coef_cap = 0;
   bool have_scan = false, have_pats = false, have_obj = false, have_probe = false;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};   // one sweep: object phase, probe phase
@@ -570,9 +611,10 @@ int enqueue_sweep(cdx_pty* t, bool probe_phase) {
   cudaStream_t st = t->st;
   const long long n = t->npx, on = t->onpx;
   PTY_CK(cudaMemsetAsync(t->scal->maxb, 0, sizeof(t->scal->maxb), st));
-  k_pty_max_mod2<<<grid1(n), 256, 0, st>>>(t->P, nullptr, n, &t->scal->maxb[0]);
-  if (probe_phase) k_pty_max_mod2<<<grid1(on), 256, 0, st>>>(t->O, t->msum, on, &t->scal->maxb[1]);
-  k_pty_balance<<<1, 1, 0, st>>>(t->scal, probe_phase);
+  k_pty_max_mod2<<<grid1(n), 256, 0, st>>>(t->P, nullptr, n, &t->scal->maxb[0], t->scal, t->cnt,
+                                            probe_phase ? -1 : 0);
+  if (probe_phase)
+    k_pty_max_mod2<<<grid1(on), 256, 0, st>>>(t->O, t->msum, on, &t->scal->maxb[1], t->scal, t->cnt + 1, 1);
   if (probe_phase) {
     k_pty_obj_balance<<<grid1(on), 256, 0, st>>>(t->O, t->Op, on, t->scal);
     k_pty_scale<<<grid1(n), 256, 0, st>>>(t->P, n, &t->scal->isf);
@@ -593,13 +635,11 @@ int enqueue_sweep(cdx_pty* t, bool probe_phase) {
     k_pty_pupil_mask<<<grid1(n), 256, 0, st>>>(t->P, t->p.rows, t->p.cols, (int)t->p.pupil_size);
     PTY_RET(angular_spectrum(t, t->P, false));
     PTY_RET(fft2(t, t->P, t->tmp, false));
-    k_pty_far_part<<<kRedBlocks, 256, 0, st>>>(t->tmp, t->p.rows, t->p.cols, t->part);
-    k_pty_far_fin<<<1, 1, 0, st>>>(t->part, kRedBlocks, t->scal, t->p.rows, t->p.cols);
+    k_pty_far_part<<<kRedBlocks, 256, 0, st>>>(t->tmp, t->p.rows, t->p.cols, t->part, t->scal, t->cnt + 2);
     k_pty_mshift<<<grid1(n), 256, 0, st>>>(t->P, t->p.rows, t->p.cols, t->scal);
   }
   if (t->p.mpie) {
-    k_pty_csum_part<<<kRedBlocks, 256, 0, st>>>(t->O, t->msum, on, t->part);
-    k_pty_csum_fin<<<1, 1, 0, st>>>(t->part, kRedBlocks, t->scal, 0);
+    k_pty_csum<<<kRedBlocks, 256, 0, st>>>(t->O, t->msum, on, t->part, t->scal, t->cnt + 3, 0);
     k_pty_momentum<<<grid1(on), 256, 0, st>>>(t->O, t->Op, on, t->scal, t->coef, t->iter);
   }
   k_pty_next<<<1, 1, 0, st>>>(t->iter);
@@ -694,13 +734,14 @@ int cdx_pty_create(const cdx_pty_params* p, void* stream, cdx_pty** out) {
       (r = dalloc(&t->pupil, t->npx)) || (r = dalloc(&t->W, t->pat_stride)) ||
       (r = dalloc(&t->pats, t->pat_stride * p->nscan)) || (r = dalloc(&t->bs, t->pat_stride)) ||
       (r = dalloc(&t->win, p->nscan)) || (r = dalloc(&t->tpos, p->nscan)) || (r = dalloc(&t->iter, 1)) ||
-      (r = dalloc(&t->scal, 1)) || (r = dalloc(&t->part, 3 * kRedBlocks)))
+      (r = dalloc(&t->scal, 1)) || (r = dalloc(&t->part, 3 * kRedBlocks)) || (r = dalloc(&t->cnt, 4)))
     return fail(r);
   e = cudaMemsetAsync(t->W, 0, sizeof(float2) * t->pat_stride, t->st);
   if (e == cudaSuccess) e = cudaMemsetAsync(t->pats, 0, sizeof(float) * t->pat_stride * p->nscan, t->st);
   if (e == cudaSuccess) e = cudaMemsetAsync(t->bs, 0, sizeof(float) * t->pat_stride, t->st);
   if (e == cudaSuccess) e = cudaMemsetAsync(t->step, 0, sizeof(float2) * t->npx, t->st);
   if (e == cudaSuccess) e = cudaMemsetAsync(t->scal, 0, sizeof(PtyScal), t->st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(t->cnt, 0, sizeof(unsigned) * 4, t->st);
   if (e == cudaSuccess && p->use_bs) {
     k_pty_beamstop<<<grid1(t->npx), 256, 0, t->st>>>(t->bs, p->rows, p->cols, t->tl, (float)p->beam_stop_size);
     e = cudaGetLastError();
@@ -724,7 +765,7 @@ int cdx_pty_destroy(cdx_pty* t) {
   for (auto& g : t->graph)
     if (g) cudaGraphExecDestroy(g);
   void* bufs[] = {t->O, t->Op, t->P, t->step, t->W, t->tmp, t->pupil, t->pats, t->bs, t->msum, t->coef,
-                  t->win, t->tpos, t->order, t->iter, t->scal, t->part};
+                  t->win, t->tpos, t->order, t->iter, t->scal, t->part, t->cnt};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (t->e0) cudaEventDestroy(t->e0);
@@ -934,8 +975,7 @@ int cdx_pty_iterate(cdx_pty* t, int first_iter, int n_iter, const int* orders, u
   for (int it = first_iter; it < first_iter + n_iter; ++it)
     PTY_CK(cudaGraphLaunch(t->graph[it >= kUpdateProbeIter ? 1 : 0], st));
   // final global phase of the object (util/ptycho.cpp:731-735)
-  k_pty_csum_part<<<kRedBlocks, 256, 0, st>>>(t->O, nullptr, t->onpx, t->part);
-  k_pty_csum_fin<<<1, 1, 0, st>>>(t->part, kRedBlocks, t->scal, 1);
+  k_pty_csum<<<kRedBlocks, 256, 0, st>>>(t->O, nullptr, t->onpx, t->part, t->scal, t->cnt + 3, 1);
   k_pty_conj_phase<<<grid1(t->onpx), 256, 0, st>>>(t->O, t->onpx, t->scal);
   PTY_CK(cudaGetLastError());
   PTY_CK(cudaEventRecord(t->e1, st));

@@ -71,6 +71,35 @@ __device__ __forceinline__ long long pty_tiled(int r, int c, int rows, int tl) {
   return ((((long long)(c >> tl)) * rows + r) << tl) + (c & ((1 << tl) - 1));
 }
 
+// Row kernels stage the CTA's object-window rows and probe rows in shared
+// memory with 8-byte cp.async (the window may start at any column; pixels
+// outside the object are zero-filled), line stride N + 8 so the lines a warp
+// reads together fall on different bank halves.
+template <int N>
+struct PtyRow {
+  static constexpr int SN = N + 8;
+  static constexpr int STAGE = 2 * Geom<N>::L * SN * (int)sizeof(float2);
+  static constexpr int SMEM = Geom<N>::SMEM_LINES + STAGE;
+};
+
+template <int N>
+__device__ __forceinline__ void pty_stage_rows(const PtyArgs& a, float2* o_s, float2* p_s, int row0, int nrows,
+                                               int2 w) {
+  using G = Geom<N>;
+  constexpr int L = G::L, T = G::T, SN = PtyRow<N>::SN;
+  const long long OC = a.obj_cols;
+  for (int e = threadIdx.x; e < L * N; e += T) {
+    const int l = e / N, c = e - l * N;
+    const int row = row0 + l;
+    const bool rok = l < nrows;
+    const int ox = w.x + row, oy = w.y + c;
+    const bool inb = rok && ox >= 0 && ox < a.obj_rows && oy >= 0 && oy < a.obj_cols;
+    cp_async8(o_s + l * SN + c, inb ? (const void*)(a.obj + ox * OC + oy) : (const void*)a.obj, inb);
+    cp_async8(p_s + l * SN + c, rok ? (const void*)(a.probe + (long long)row * N + c) : (const void*)a.probe, rok);
+  }
+  cp_commit();
+}
+
 // ------------------------------------------------------- forward row pass
 template <int N>
 __global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_ROW) pty_fwd_rk(PtyArgs a) {
@@ -78,13 +107,17 @@ __global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_ROW) pty_fwd_rk(Pty
   constexpr int L = G::L;
   using F0 = RFirst<N, 0>;
   using FL = RLast<N, 0>;
+  constexpr int SN = PtyRow<N>::SN;
   extern __shared__ float2 smem[];
+  float2* o_s = smem + L * G::LD;
+  float2* p_s = o_s + L * SN;
   const int row0 = blockIdx.x * L;
   const int nrows = min(L, a.rows - row0);
   const int cb = min(a.tl, rfft_cb_max<N>());
   const int si = a.order[*a.iter * a.nscan + a.k];
-  const int2 w = a.win[si];
-  const long long OC = a.obj_cols;
+  pty_stage_rows<N>(a, o_s, p_s, row0, nrows, a.win[si]);
+  cp_wait<0>();
+  __syncthreads();
   float2 v0[F0::B][F0::R];
 #pragma unroll
   for (int b = 0; b < F0::B; ++b) {
@@ -92,14 +125,8 @@ __global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_ROW) pty_fwd_rk(Pty
     if (!bfly_of<N, F0::R>(b, cb, l, j)) continue;
 #pragma unroll
     for (int r = 0; r < F0::R; ++r) {
-      const int c = j + r * F0::NR, row = row0 + l;
-      float2 y = make_float2(0.f, 0.f);
-      if (l < nrows) {
-        const int ox = w.x + row, oy = w.y + c;
-        if (ox >= 0 && ox < a.obj_rows && oy >= 0 && oy < a.obj_cols)
-          y = cmul(__ldg(a.probe + (long long)row * N + c), a.obj[ox * OC + oy]);
-      }
-      v0[b][r] = y;
+      const int t = l * SN + j + r * F0::NR;   // multiply(esw, probe, window): zero outside the object
+      v0[b][r] = cmul(p_s[t], o_s[t]);
     }
   }
   float2 v[FL::B][FL::R];
@@ -177,13 +204,17 @@ __global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_ROW) pty_upd_rk(Pty
   constexpr int L = G::L;
   using F0 = RFirst<N, 0>;
   using FL = RLast<N, 0>;
+  constexpr int SN = PtyRow<N>::SN;
   extern __shared__ float2 smem[];
+  float2* o_s = smem + L * G::LD;
+  float2* p_s = o_s + L * SN;
   const int row0 = blockIdx.x * L;
   const int nrows = min(L, a.rows - row0);
   const int cb = min(a.tl, rfft_cb_max<N>());
   const int si = a.order[*a.iter * a.nscan + a.k];
   const int2 w = a.win[si];
   const long long OC = a.obj_cols;
+  pty_stage_rows<N>(a, o_s, p_s, row0, nrows, w);   // lands during the inverse FFT
   float2 v0[F0::B][F0::R];
 #pragma unroll
   for (int b = 0; b < F0::B; ++b) {
@@ -195,6 +226,8 @@ __global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_ROW) pty_upd_rk(Pty
   }
   float2 v[FL::B][FL::R];
   rfft<N, 0, true>(v0, v, smem, a.tw, cb);
+  cp_wait<0>();
+  __syncthreads();
   const float pmax = a.scal[0], omax = a.scal[1];
 #pragma unroll
   for (int b = 0; b < FL::B; ++b) {
@@ -208,9 +241,9 @@ __global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_ROW) pty_upd_rk(Pty
       pp.y *= a.norm;
       const int ox = w.x + row, oy = w.y + c;
       const bool inb = ox >= 0 && ox < a.obj_rows && oy >= 0 && oy < a.obj_cols;
-      float2 o = inb ? a.obj[ox * OC + oy] : make_float2(0.f, 0.f);
+      float2 o = o_s[l * SN + c];                // getWindow: zero outside the object
       const long long pi = (long long)row * N + c;
-      const float2 p = __ldg(a.probe + pi);
+      const float2 p = p_s[l * SN + c];
       float2 d = cmul(p, o);                     // esw = P * O_window, then esw += Fn * (-1)
       d.x -= pp.x;
       d.y -= pp.y;
@@ -231,9 +264,9 @@ __global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_ROW) pty_upd_rk(Pty
 template <int N>
 cudaError_t pty_prepare() {
   using G = Geom<N>;
-  cudaError_t e = cudaFuncSetAttribute(pty_fwd_rk<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM_LINES);
+  cudaError_t e = cudaFuncSetAttribute(pty_fwd_rk<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, PtyRow<N>::SMEM);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(pty_upd_rk<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM_LINES);
+    e = cudaFuncSetAttribute(pty_upd_rk<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, PtyRow<N>::SMEM);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(pty_col_rk<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              G::SMEM_LINES + 2 * G::L * N * (int)sizeof(float));
@@ -242,13 +275,13 @@ cudaError_t pty_prepare() {
 template <int N>
 cudaError_t pty_launch_fwd(const PtyArgs& a, cudaStream_t st) {
   using G = Geom<N>;
-  pty_fwd_rk<N><<<(a.rows + G::L - 1) / G::L, G::T, G::SMEM_LINES, st>>>(a);
+  pty_fwd_rk<N><<<(a.rows + G::L - 1) / G::L, G::T, PtyRow<N>::SMEM, st>>>(a);
   return cudaGetLastError();
 }
 template <int N>
 cudaError_t pty_launch_upd(const PtyArgs& a, cudaStream_t st) {
   using G = Geom<N>;
-  pty_upd_rk<N><<<(a.rows + G::L - 1) / G::L, G::T, G::SMEM_LINES, st>>>(a);
+  pty_upd_rk<N><<<(a.rows + G::L - 1) / G::L, G::T, PtyRow<N>::SMEM, st>>>(a);
   return cudaGetLastError();
 }
 template <int N>
