@@ -115,6 +115,41 @@ __device__ __forceinline__ double block_sum_d(double v, double* red) {
   return r;
 }
 
+// ------------------------------------------------ programmatic dependent launch
+// The pass kernels are launched with programmatic stream serialisation allowed
+// (cudaLaunchAttributeProgrammaticStreamSerialization): each CTA first waits
+// until the preceding grid has completed and its writes are visible
+// (griddepcontrol.wait: a no-op for a normal launch), then lets the next
+// kernel of the stream be scheduled (griddepcontrol.launch_dependents; it
+// starts once every CTA of this grid has done so or exited).  The next
+// kernel's CTAs thus fill the SMs this grid's last wave leaves idle and wait
+// there, instead of being launched after it drains.
+__device__ __forceinline__ void pdl_wait_and_release() {
+  asm volatile("griddepcontrol.wait;\n" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+}
+
+#ifndef CDX_PDL
+#define CDX_PDL 1
+#endif
+// Launch of a register-handoff pass kernel with programmatic dependent launch
+// allowed (the kernel waits for its predecessor itself: pdl_wait_and_release).
+template <class A>
+cudaError_t launch_pdl(void (*kernel)(A), dim3 grid, int block, int smem, cudaStream_t st, const A& a,
+                       bool allow = true) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = (CDX_PDL && allow) ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kernel, a);
+}
+
 // ------------------------------------------------------------ async copies
 // cp.async global -> shared; with `valid` false the destination is zero-filled
 // and nothing is read.

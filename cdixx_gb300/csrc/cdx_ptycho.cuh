@@ -109,6 +109,7 @@ __global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_ROW) pty_fwd_rk(Pty
   using FL = RLast<N, 0>;
   constexpr int SN = PtyRow<N>::SN;
   extern __shared__ float2 smem[];
+  pdl_wait_and_release();
   float2* o_s = smem + L * G::LD;
   float2* p_s = o_s + L * SN;
   const int row0 = blockIdx.x * L;
@@ -149,6 +150,7 @@ __global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_COL) pty_col_rk(Pty
   using FL = RLast<N, 0>;
   using IL = RLast<N, 1>;
   extern __shared__ float2 smem[];
+  pdl_wait_and_release();
   const int c0 = blockIdx.x * L;
   const int ncols = min(L, a.cols - c0);
   const long long tile = (long long)blockIdx.x * N * L;
@@ -206,6 +208,7 @@ __global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_ROW) pty_upd_rk(Pty
   using FL = RLast<N, 0>;
   constexpr int SN = PtyRow<N>::SN;
   extern __shared__ float2 smem[];
+  pdl_wait_and_release();
   float2* o_s = smem + L * G::LD;
   float2* p_s = o_s + L * SN;
   const int row0 = blockIdx.x * L;
@@ -275,20 +278,18 @@ cudaError_t pty_prepare() {
 template <int N>
 cudaError_t pty_launch_fwd(const PtyArgs& a, cudaStream_t st) {
   using G = Geom<N>;
-  pty_fwd_rk<N><<<(a.rows + G::L - 1) / G::L, G::T, PtyRow<N>::SMEM, st>>>(a);
-  return cudaGetLastError();
+  return launch_pdl(pty_fwd_rk<N>, dim3((a.rows + G::L - 1) / G::L), G::T, PtyRow<N>::SMEM, st, a);
 }
 template <int N>
 cudaError_t pty_launch_upd(const PtyArgs& a, cudaStream_t st) {
   using G = Geom<N>;
-  pty_upd_rk<N><<<(a.rows + G::L - 1) / G::L, G::T, PtyRow<N>::SMEM, st>>>(a);
-  return cudaGetLastError();
+  return launch_pdl(pty_upd_rk<N>, dim3((a.rows + G::L - 1) / G::L), G::T, PtyRow<N>::SMEM, st, a);
 }
 template <int N>
 cudaError_t pty_launch_col(const PtyArgs& a, cudaStream_t st) {
   using G = Geom<N>;
-  pty_col_rk<N><<<(a.cols + G::L - 1) / G::L, G::T, G::SMEM_LINES + 2 * G::L * N * (int)sizeof(float), st>>>(a);
-  return cudaGetLastError();
+  return launch_pdl(pty_col_rk<N>, dim3((a.cols + G::L - 1) / G::L), G::T,
+                    G::SMEM_LINES + 2 * G::L * N * (int)sizeof(float), st, a);
 }
 
 #define CDX_PTY_INSTANTIATE(N)                                               \

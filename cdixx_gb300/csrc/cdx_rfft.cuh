@@ -217,6 +217,7 @@ __global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_COL) col_pass_rk(Co
   static_assert(FL::R == RFirst<N, 1>::R && FL::B == RFirst<N, 1>::B, "plan 1 starts where plan 0 ends");
   extern __shared__ float2 smem[];
   __shared__ double red[T / 32];
+  pdl_wait_and_release();
   const float2* __restrict__ tw = a.tw;
   float2* buf = smem;
   const int c0 = blockIdx.x * L;
@@ -489,6 +490,7 @@ __device__ __forceinline__ void row_pass_body(const RowArgs& a) {
 // holds a single update and no switch.
 template <int N, int MODE, int ALGO>
 __global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_ROW) row_pass_rk(RowArgs a) {
+  pdl_wait_and_release();
   if (a.state && (a.state[blockIdx.y].flags & 4)) return;   // frozen pattern
   row_pass_body<N, MODE, ALGO>(a);
 }
