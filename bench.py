@@ -345,6 +345,22 @@ def ptycho_section(cpu=True):
     return out
 
 
+def replica_throughput(local_ms, local_units, dist=None, device=None):
+    """Whole-job throughput of independent replicas: every rank times its own
+    units between two barriers; the job time is the slowest rank's (MAX), the
+    work the sum over ranks, so value = sum(units) / max(ms).  No data-path
+    collective: the two reductions run once, outside the timed region."""
+    if dist is None:
+        return local_units / (local_ms / 1000.0), local_ms
+    import torch
+    t = torch.tensor([float(local_ms), float(local_units)], dtype=torch.float64, device=device)
+    ms = t[:1].clone()
+    units = t[1:].clone()
+    dist.all_reduce(ms, op=dist.ReduceOp.MAX)
+    dist.all_reduce(units, op=dist.ReduceOp.SUM)
+    return float(units.item()) / (float(ms.item()) / 1000.0), float(ms.item())
+
+
 def run_gpu(args):
     import torch
     from cdixx_gb300 import native as cdx
@@ -392,12 +408,8 @@ def run_gpu(args):
     step_ms = [a.elapsed_time(b) for a, b in ev]
     total_ms = float(sum(step_ms))
     clk = clocks.stop()
-    if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
     iters = SW_EVERY * args.steps
-    value = world * iters / (total_ms / 1000.0)
+    value, total_ms = replica_throughput(total_ms, iters, dist, device="cuda")
 
     # roofline: pure iterations, events around each block of 50, L2 flushed before each
     it_ms = []
