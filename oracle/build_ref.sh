@@ -1,6 +1,6 @@
 #!/bin/sh
 # Builds the reference's hot-path sources (src/gpu/cdi.cu, cudaConfig.cu,
-# cub_wrap.cu, src/post_gpu/cdi.cc, src/independant/readConfig.cc,
+# cub_wrap.cu, src/post_gpu/cdi.cc, misc.cc, src/independant/readConfig.cc,
 # memManager.cc) as HOST code from where they lie in the reference checkout,
 # through the emulation headers in oracle/refshim, into oracle/_ref/ref_harness.
 # The kernels' explicit "<<<grid, block>>>" launches are rewritten on the way
@@ -18,10 +18,10 @@ for f in src/gpu/cdi.cu src/gpu/cudaConfig.cu src/gpu/cub_wrap.cu; do
   o="$OUT/obj/$(basename "$f").o"
   sed "$LAUNCH" "$REF/$f" | $CXX -x c++ - -I"$REF/$(dirname "$f")" -c -o "$o"
 done
-for f in src/post_gpu/cdi.cc src/independant/readConfig.cc src/independant/memManager.cc; do
+for f in src/post_gpu/cdi.cc src/post_gpu/misc.cc src/independant/readConfig.cc src/independant/memManager.cc; do
   $CXX -c "$REF/$f" -o "$OUT/obj/$(basename "$f").o"
 done
-$CXX -c "$SHIM/cdxref_stubs.cc" -o "$OUT/obj/cdxref_stubs.o"
+$CXX -DCDXREF_WITH_MISC -c "$SHIM/cdxref_stubs.cc" -o "$OUT/obj/cdxref_stubs.o"
 $CXX -c "$SHIM/ref_harness.cc" -o "$OUT/obj/ref_harness.o"
 g++ -o "$OUT/ref_harness" "$OUT"/obj/*.o
 echo "built $OUT/ref_harness"
@@ -33,11 +33,10 @@ PO="$OUT/obj_pty"
 mkdir -p "$PO"
 sed "$LAUNCH" "$REF/src/gpu/ptycho.cu" | $CXX -x c++ - -I"$REF/src/gpu" -c -o "$PO/ptycho.cu.o"
 $CXX -c "$REF/src/post_gpu/propagator.cc" -o "$PO/propagator.cc.o"
-$CXX -c "$REF/src/post_gpu/misc.cc" -o "$PO/misc.cc.o"
-$CXX -DCDXREF_WITH_PROPAGATOR -DCDXREF_WITH_MISC -c "$SHIM/cdxref_stubs.cc" -o "$PO/cdxref_stubs.o"
+$CXX -DCDXREF_WITH_PROPAGATOR -DCDXREF_WITH_MISC -DCDXREF_WITH_PTYCHO_KERNELS -c "$SHIM/cdxref_stubs.cc" -o "$PO/cdxref_stubs.o"
 $CXX -c "$SHIM/pty_stubs.cc" -o "$PO/pty_stubs.o"
 $CXX -include "$SHIM/cdxref_ptycho.h" -DCDXREF_PTYCHO_CPP="\"$REF/util/ptycho.cpp\"" -c "$SHIM/pty_harness.cc" \
   -o "$PO/pty_harness.o"
 g++ -o "$OUT/pty_harness" "$PO"/*.o "$OUT/obj/cudaConfig.cu.o" "$OUT/obj/cdi.cu.o" "$OUT/obj/cub_wrap.cu.o" \
-  "$OUT/obj/memManager.cc.o" "$OUT/obj/readConfig.cc.o"
+  "$OUT/obj/misc.cc.o" "$OUT/obj/memManager.cc.o" "$OUT/obj/readConfig.cc.o"
 echo "built $OUT/pty_harness"

@@ -5,7 +5,11 @@
 //
 // ref_harness <pattern.bin (centred float)> <restart.bin (complex, FFT order)>
 //             <algorithm> <oversampling_spt> <shrinkThreshold> <exposure>
-//             <simCCDbit> <noiseLevel> <out prefix>
+//             <simCCDbit> <noiseLevel> <out prefix> [prtfIter [saveState]]
+// With prtfIter the reference also computes the PRTF from that iteration on
+// and writes prtf.txt into the working directory (cdi.cc:355-380, 424-440);
+// with saveState != 0 it then runs CDI::saveState (its plotted fields are
+// dumped when CDXREF_PLOT_DUMP names a directory, its "mid=" line printed).
 #include <cstdio>
 #include <cstdlib>
 
@@ -38,13 +42,17 @@ int main(int argc, char** argv) {
   c.restart = 1;
   c.runSim = 0;
   c.useBS = 0;
-  c.prtfIter = 1 << 30;
+  c.prtfIter = argc > 10 ? atoi(argv[10]) : 1 << 30;
   c.verbose = 0;
   c.readFiles();
   c.init();
   c.prepareIter();
   c.phaseRetrieve();
   const std::string pre = argv[9];
+  if (argc > 11 && atoi(argv[11])) {
+    writeComplexImage((pre + "_rho_before_save.bin").c_str(), c.objectWave, c.row, c.column);
+    c.saveState();
+  }
   writeComplexImage((pre + "_rho.bin").c_str(), c.objectWave, c.row, c.column);
   writeComplexImage((pre + "_psi.bin").c_str(), c.patternWave, c.row, c.column);
   writeFloatImage((pre + "_support.bin").c_str(), c.support, c.row, c.column);

@@ -40,6 +40,11 @@ CASES = [(f"hio_{k}", f"{k}*HIO", 2.0, 0.1, 1.0, 0, 0) for k in range(1, 11)] + 
 ]
 
 
+# (name, algorithm, prtfIter): spt 2, shrinkThreshold 0.1, exposure 1, beta_HIO 1
+PRTF_CASES = [("prtf_er", "30*ER", 10), ("prtf_hio", "12*HIO+10*ER", 6)]
+SAVE_ALGO = "2*(10*HIO+1*shrinkWrap)+4*ER"
+
+
 def main(ref=None):
     ref = ref or os.environ.get("CDX_REFERENCE", "/root/reference")
     subprocess.run([str(ROOT / "oracle" / "build_ref.sh"), ref], check=True)
@@ -64,6 +69,34 @@ def main(ref=None):
             data[f"{name}/scalars"] = np.array([float(sc["threshold"]), float(sc["residual"])])
             data[f"{name}/params"] = np.array([spt, thr, exposure, ccd, noise])
             data[f"{name}/algorithm"] = np.array(alg)
+        # PRTF from prtfIter on: the reference writes prtf.txt ("i, prtf[i]/weights[i]")
+        for name, alg, prtf_iter in PRTF_CASES:
+            O.write_bin(td / "pattern.bin", np.fft.fftshift(I))
+            O.write_bin(td / "restart.bin", psi0)
+            subprocess.run([str(exe), "pattern.bin", "restart.bin", alg, "2.0", "0.1", "1.0", "0", "0", "out",
+                            str(prtf_iter)], cwd=td, check=True, capture_output=True)
+            rows = [ln.split(",") for ln in open(td / "prtf.txt") if ln.strip()]
+            data[f"{name}/prtf"] = np.array([float(r[1]) for r in rows], np.float64)
+            data[f"{name}/rho"] = O.read_bin(td / "out_rho.bin")
+            data[f"{name}/algorithm"] = np.array(alg)
+            data[f"{name}/prtf_iter"] = np.array(prtf_iter)
+        # saveState after a run with shrinkwraps: the plotted fields are dumped raw
+        # (CDXREF_PLOT_DUMP), the centroid is printed as "mid= x,y"
+        plots = td / "plots"
+        plots.mkdir()
+        O.write_bin(td / "pattern.bin", np.fft.fftshift(I))
+        O.write_bin(td / "restart.bin", psi0)
+        r = subprocess.run([str(exe), "pattern.bin", "restart.bin", SAVE_ALGO, "2.0", "0.1", "1.0", "0", "0", "out",
+                            str(1 << 30), "1"], cwd=td, check=True, capture_output=True, text=True,
+                           env={**os.environ, "CDXREF_PLOT_DUMP": str(plots)})
+        mid = [float(v) for v in r.stdout.split("mid=")[1].split()[0].split(",")]
+        data["savestate/algorithm"] = np.array(SAVE_ALGO)
+        data["savestate/mid"] = np.array(mid)
+        data["savestate/rho"] = O.read_bin(td / "out_rho_before_save.bin")
+        data["savestate/psi"] = O.read_bin(td / "restart.bin")          # saveState writes Psi there
+        data["savestate/support"] = O.read_bin(plots / "support.bin")   # after bitMap
+        data["savestate/wave"] = O.read_bin(plots / "recon_wave.bin")   # object cropped about mid
+        data["savestate/autocorrelation"] = O.read_bin(plots / "autocorrelation_recon.bin")
         # one step from the reference's own state after k-1 HIO steps: restart from
         # its Psi_{k-1} (prepareIter recomputes rho_{k-1} = IFFT(Psi_{k-1})/N)
         prev = psi0

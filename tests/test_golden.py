@@ -8,6 +8,10 @@ Two levels (tests/_bounds.py):
   * trajectory cases (hio_k, raar_er, mixed, shrinkwrap, ccd, ...): k steps
     from Psi0, bounded by the divergence a 1e-7 perturbation of Psi0 produces
     over the same steps (never below 1e-5); shrinkwrap masks agree >= 99.9 %.
+  * PRTF cases: the reference's prtf.txt column (printed with 6 decimals),
+    within the trajectory bound of the run plus the print resolution;
+  * saveState: the reference's centroid ("mid=" line), the object cropped
+    about it and the autocorrelation FFT(|Psi|^2), as its plotter received them.
 """
 from pathlib import Path
 
@@ -19,7 +23,9 @@ from tests._bounds import STEP_TOL, rel_l2 as rel, trajectory_bound
 
 GOLDEN = Path(__file__).resolve().parent / "golden" / "reference_cases.npz"
 Z = np.load(GOLDEN)
-CASES = sorted({k.split("/")[0] for k in Z.files if "/" in k and not k.startswith("step_")})
+CASES = sorted({k.split("/")[0] for k in Z.files
+                if "/" in k and not k.startswith(("step_", "prtf_", "savestate"))})
+PRTF_CASES = sorted({k.split("/")[0] for k in Z.files if k.startswith("prtf_")})
 STEPS = list(range(1, 11))
 
 
@@ -93,3 +99,94 @@ def test_cuda_trajectory_matches_reference(cdx, name):
     if "shrinkWrap" in c["alg"]:
         ref = Z[f"{name}/support"]
         assert np.mean((spt > s["threshold"]) == (ref > thr)) >= 0.999
+
+
+# ------------------------------------------------------------------ PRTF
+def prtf_bound(name):
+    alg = str(Z[f"{name}/algorithm"])
+    _, tol = trajectory_bound(Z["psi0"], Z["intensity"], alg, oversampling_spt=2.0, shrink_threshold=0.1)
+    return 4 * tol
+
+
+@pytest.mark.parametrize("name", PRTF_CASES)
+def test_oracle_prtf_matches_reference(name):
+    alg, k = str(Z[f"{name}/algorithm"]), int(Z[f"{name}/prtf_iter"])
+    st = O.phase_retrieve(Z["psi0"], Z["intensity"], alg, oversampling_spt=2.0, shrink_threshold=0.1, prtf_iter=k)
+    ref = Z[f"{name}/prtf"]
+    assert st.prtf.shape == ref.shape
+    assert np.max(np.abs(st.prtf - ref)) <= prtf_bound(name) * np.max(np.abs(ref)) + 1e-6
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", PRTF_CASES)
+def test_cuda_prtf_matches_reference(cdx, name):
+    alg, k = str(Z[f"{name}/algorithm"]), int(Z[f"{name}/prtf_iter"])
+    I = Z["intensity"]
+    n = I.shape[0]
+    p = cdx.default_params(n, n, oversampling_spt=2.0, shrink_threshold=0.1, prtf_iter=k)
+    with cdx.Context(p) as ctx:
+        ctx.set_pattern(0, I)
+        ctx.set_initial(0, np.asarray(Z["psi0"], np.complex64))
+        ctx.run(alg)
+        got = ctx.get_prtf(0)
+    ref = Z[f"{name}/prtf"]
+    e = np.max(np.abs(got - ref)) / np.max(np.abs(ref))
+    print(f"{name}: PRTF max rel diff vs the reference {e:.2e}")
+    assert np.max(np.abs(got - ref)) <= prtf_bound(name) * np.max(np.abs(ref)) + 1e-6
+
+
+# ------------------------------------------------------------------ saveState
+def test_oracle_savestate_matches_reference():
+    """find_middle, crop_about and the autocorrelation applied to the reference's
+    own support, object and Psi reproduce what its saveState computed; the
+    oracle's run reaches the same object."""
+    mid = Z["savestate/mid"]
+    spt, rho, psi = Z["savestate/support"], Z["savestate/rho"], Z["savestate/psi"]
+    mx, my = O.find_middle(spt)
+    assert abs(mx - mid[0]) <= 1e-6 and abs(my - mid[1]) <= 1e-6     # printed with 6 decimals
+    wave = Z["savestate/wave"]
+    assert np.array_equal(O.crop_about(rho, wave.shape[0], wave.shape[1], mid[0], mid[1]), wave)
+    ac = np.fft.fft2(np.abs(psi.astype(np.complex128)) ** 2)
+    assert rel(Z["savestate/autocorrelation"], ac) <= 1e-6
+    alg = str(Z["savestate/algorithm"])
+    st, tol = trajectory_bound(Z["psi0"], Z["intensity"], alg, oversampling_spt=2.0, shrink_threshold=0.1)
+    assert rel(st.rho, rho) <= tol
+
+
+@pytest.mark.gpu
+def test_cdi_run_savestate_matches_reference(cdx, tmp_path):
+    """cdi_run (the config-driven C++ entry) on the same inputs: its saveState
+    dumps against the reference's (nIter = 0: no restart passes after the first
+    reconstruction, util/cdi.cpp:35-46)."""
+    import subprocess
+    lib = Path(__file__).resolve().parents[1] / "cdixx_gb300" / "_lib"
+    I = Z["intensity"]
+    O.write_bin(tmp_path / "pattern.bin", np.fft.fftshift(I))
+    O.write_bin(tmp_path / "restart.bin", Z["psi0"])
+    alg = str(Z["savestate/algorithm"])
+    (tmp_path / "cdi.cfg").write_text(f"""
+InputImages = {{ default = {{ Pattern = "pattern.bin"; restart = "restart.bin"; }}; }};
+Job = {{
+  algorithm = "{alg}";
+  oversampling_spt = 2.;
+  shrinkThreshold = 0.1;
+  exposure = 1.;
+  nIter = 0;
+  doIteration = True;
+  restart = True;
+  outputDir = "./";
+}};
+""")
+    r = subprocess.run([str(lib / "cdi_run"), "cdi.cfg"], cwd=tmp_path, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    _, tol = trajectory_bound(Z["psi0"], I, alg, oversampling_spt=2.0, shrink_threshold=0.1)
+    mid = [float(v) for v in r.stdout.split("mid=")[1].split()[0].split(",")]
+    spt = O.read_bin(tmp_path / "support.bin")
+    assert np.mean(spt == Z["savestate/support"]) >= 0.999
+    assert np.max(np.abs(np.array(mid) - Z["savestate/mid"])) <= 2e-3
+    wave = O.read_bin(tmp_path / "recon_wave.bin")
+    assert wave.shape == Z["savestate/wave"].shape
+    if np.allclose(mid, Z["savestate/mid"], atol=1e-6):   # same crop window: same pixels
+        assert rel(wave, Z["savestate/wave"]) <= tol
+    ac = O.read_bin(tmp_path / "autocorrelation_recon.bin")
+    assert rel(ac, Z["savestate/autocorrelation"]) <= 2 * tol
