@@ -12,6 +12,7 @@
 // dumped when CDXREF_PLOT_DUMP names a directory, its "mid=" line printed).
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 
 #include "cdi.hpp"
 #include "cudaConfig.hpp"
@@ -24,8 +25,34 @@ struct cudaVars {   // layout of __constant__ vars in src/gpu/cdi.cu:8-14
   Real threshold;
 };
 extern cudaVars vars;
+extern "C" void writeFloatImage(const char* name, void* data, int row, int column);
+
+// ref_harness --sim <intensity.bin> <phase.bin or -> <oversampling> <phaseModulation> <exposure> <out.bin>
+// runs the noise-free simulation of readFiles/prepareIter (runSim, cdi.cc:62-82,
+// 161-200) and writes the simulated patternData.
+static int run_sim(int argc, char** argv) {
+  if (argc < 8) return 2;
+  CDI c("none.cfg");
+  c.runSim = 1;
+  c.common.Intensity = argv[2];
+  c.common.Phase = strcmp(argv[3], "-") ? argv[3] : nullptr;
+  c.oversampling = atof(argv[4]);
+  c.phaseModulation = atof(argv[5]);
+  c.exposure = atof(argv[6]);
+  c.intensityModulation = 1;
+  c.simCCDbit = 0;
+  c.restart = 0;
+  c.useBS = 0;
+  c.verbose = 0;
+  c.readFiles();
+  c.init();
+  c.prepareIter();
+  writeFloatImage(argv[7], c.patternData, c.row, c.column);
+  return 0;
+}
 
 int main(int argc, char** argv) {
+  if (argc > 1 && !strcmp(argv[1], "--sim")) return run_sim(argc, argv);
   if (argc < 10) {
     fprintf(stderr, "usage: ref_harness pattern restart algorithm spt thr exposure ccd noise prefix\n");
     return 2;

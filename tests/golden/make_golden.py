@@ -43,6 +43,7 @@ CASES = [(f"hio_{k}", f"{k}*HIO", 2.0, 0.1, 1.0, 0, 0) for k in range(1, 11)] + 
 # (name, algorithm, prtfIter): spt 2, shrinkThreshold 0.1, exposure 1, beta_HIO 1
 PRTF_CASES = [("prtf_er", "30*ER", 10), ("prtf_hio", "12*HIO+10*ER", 6)]
 SAVE_ALGO = "2*(10*HIO+1*shrinkWrap)+4*ER"
+SIM_OVERSAMPLING, SIM_PHASEMOD, SIM_EXPOSURE = 2.0, 0.7, 0.5
 
 
 def main(ref=None):
@@ -97,6 +98,21 @@ def main(ref=None):
         data["savestate/support"] = O.read_bin(plots / "support.bin")   # after bitMap
         data["savestate/wave"] = O.read_bin(plots / "recon_wave.bin")   # object cropped about mid
         data["savestate/autocorrelation"] = O.read_bin(plots / "autocorrelation_recon.bin")
+        # the noise-free runSim simulation (readObjectWave + prepareIter, cdi.cc:62-82, 161-200)
+        rng = np.random.default_rng(11)
+        m = 32
+        x = np.linspace(-1, 1, m)[:, None]
+        y = np.linspace(-1, 1, m)[None, :]
+        inten = ((x ** 2 + y ** 2) < 0.8) * (0.5 + 0.5 * rng.random((m, m)))
+        phase = rng.random((m, m))
+        O.write_bin(td / "sim_i.bin", inten.astype(np.float32))
+        O.write_bin(td / "sim_p.bin", phase.astype(np.float32))
+        subprocess.run([str(exe), "--sim", "sim_i.bin", "sim_p.bin", str(SIM_OVERSAMPLING), str(SIM_PHASEMOD),
+                        str(SIM_EXPOSURE), "sim_out.bin"], cwd=td, check=True, capture_output=True)
+        data["sim/intensity"] = inten.astype(np.float32)
+        data["sim/phase"] = phase.astype(np.float32)
+        data["sim/params"] = np.array([SIM_OVERSAMPLING, SIM_PHASEMOD, SIM_EXPOSURE])
+        data["sim/pattern"] = O.read_bin(td / "sim_out.bin")
         # one step from the reference's own state after k-1 HIO steps: restart from
         # its Psi_{k-1} (prepareIter recomputes rho_{k-1} = IFFT(Psi_{k-1})/N)
         prev = psi0

@@ -24,7 +24,7 @@ from tests._bounds import STEP_TOL, rel_l2 as rel, trajectory_bound
 GOLDEN = Path(__file__).resolve().parent / "golden" / "reference_cases.npz"
 Z = np.load(GOLDEN)
 CASES = sorted({k.split("/")[0] for k in Z.files
-                if "/" in k and not k.startswith(("step_", "prtf_", "savestate"))})
+                if "/" in k and not k.startswith(("step_", "prtf_", "savestate", "sim/"))})
 PRTF_CASES = sorted({k.split("/")[0] for k in Z.files if k.startswith("prtf_")})
 STEPS = list(range(1, 11))
 
@@ -190,3 +190,42 @@ Job = {{
         assert rel(wave, Z["savestate/wave"]) <= tol
     ac = O.read_bin(tmp_path / "autocorrelation_recon.bin")
     assert rel(ac, Z["savestate/autocorrelation"]) <= 2 * tol
+
+
+# ------------------------------------------------------------------ runSim
+def test_oracle_sim_pattern_matches_reference():
+    """The noise-free runSim pattern of the reference (readObjectWave + prepareIter)."""
+    os_, pm, _ex = Z["sim/params"]
+    got = O.sim_pattern(Z["sim/intensity"], Z["sim/phase"], float(os_), float(pm))
+    assert rel(got, Z["sim/pattern"]) <= 1e-6
+
+
+@pytest.mark.gpu
+def test_cpp_runsim_pattern_matches_reference(cdx, tmp_path):
+    """The C++ CDI layer's runSim set-up (cdi_shim readObjectWave) on the same images."""
+    import subprocess
+    root = Path(__file__).resolve().parents[1]
+    lib = root / "cdixx_gb300" / "_lib"
+    exe = tmp_path / "sim_dump"
+    subprocess.run(["g++", "-std=c++17", "-O1", f"-I{root / 'include'}", "-I/usr/local/cuda/include",
+                    str(root / "tests" / "cpp" / "sim_dump.cc"), "-o", str(exe), f"-L{lib}", "-lcdx",
+                    "-L/usr/local/cuda/lib64", "-lcudart", f"-Wl,-rpath,{lib}"], check=True)
+    O.write_bin(tmp_path / "i.bin", Z["sim/intensity"])
+    O.write_bin(tmp_path / "p.bin", Z["sim/phase"])
+    os_, pm, ex = Z["sim/params"]
+    (tmp_path / "sim.cfg").write_text(f"""
+InputImages = {{ default = {{ Intensity = "i.bin"; Phase = "p.bin"; }}; }};
+Job = {{
+  runSim = True;
+  oversampling = {float(os_)};
+  phaseModulation = {float(pm)};
+  exposure = {float(ex)};
+  oversampling_spt = 2.;
+  outputDir = "./";
+}};
+""")
+    r = subprocess.run([str(exe), "sim.cfg", "sim_out.bin"], cwd=tmp_path, capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    got = O.read_bin(tmp_path / "sim_out.bin")
+    assert got.shape == Z["sim/pattern"].shape
+    assert rel(got, Z["sim/pattern"]) <= 2e-6
