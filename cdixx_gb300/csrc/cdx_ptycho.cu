@@ -57,6 +57,8 @@ namespace {
 constexpr int kRedBlocks = 608;        // reduction CTAs (four per SM); the fused finalisers assume 256 threads
 constexpr int kUpdateProbeIter = 400;  // util/ptycho.cpp:441
 constexpr int kPositionUpdateIter = 500;   // util/ptycho.cpp:442
+constexpr int kNoiseProjIter = 2000;       // applyMod instead of applyModAccurate (util/ptycho.cpp:536-545)
+constexpr float kRcolor = 65535.f;         // rcolor (include/format.hpp:21)
 
 typedef cudaError_t (*PtyPrep)();
 typedef cudaError_t (*PtyLaunch)(const PtyArgs&, cudaStream_t);
@@ -526,7 +528,7 @@ struct cdx_pty {
   unsigned* cnt = nullptr;   // last-CTA tickets of the fused reductions (reset by their last CTA)
   int order_cap = 0, coef_cap = 0;
   bool have_scan = false, have_pats = false, have_obj = false, have_probe = false;
-  cudaGraphExec_t graph[2] = {nullptr, nullptr};   // one sweep: object phase, probe phase
+  cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};   // one sweep: object, probe, probe + noise projection
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   float last_ms = 0.f;
   float lam = 0, dist = 0, res = 0;   // propagate_pupil members (float)
@@ -578,7 +580,7 @@ int angular_spectrum(cdx_pty* t, float2* P, bool reverse) {
   return fft2(t, t->tmp, P, true);
 }
 
-PtyArgs pass_args(cdx_pty* t, int k, bool probe_phase) {
+PtyArgs pass_args(cdx_pty* t, int k, bool probe_phase, bool noise_proj = false) {
   PtyArgs a{};
   a.W = t->W;
   a.obj = t->O;
@@ -603,11 +605,15 @@ PtyArgs pass_args(cdx_pty* t, int k, bool probe_phase) {
   a.maximum = (float)(1. / t->p.exposure) * 0.95f;
   a.obj_step = probe_phase ? 0.5f : 1.f;
   a.pss = (float)(1. / t->p.nscan);
+  a.noise_proj = noise_proj;
+  a.noise_level = t->p.noise_level;
+  a.ccd_scale = (float)(1. / t->p.exposure);
+  a.rcolor = kRcolor;
   return a;
 }
 
 // One sweep of ptycho::iterate (util/ptycho.cpp:484-690) for the iteration the device counter names.
-int enqueue_sweep(cdx_pty* t, bool probe_phase) {
+int enqueue_sweep(cdx_pty* t, bool probe_phase, bool noise_proj) {
   cudaStream_t st = t->st;
   const long long n = t->npx, on = t->onpx;
   PTY_CK(cudaMemsetAsync(t->scal->maxb, 0, sizeof(t->scal->maxb), st));
@@ -621,7 +627,7 @@ int enqueue_sweep(cdx_pty* t, bool probe_phase) {
   }
   PTY_CK(cudaGetLastError());
   for (int k = 0; k < t->p.nscan; ++k) {
-    PtyArgs a = pass_args(t, k, probe_phase);
+    PtyArgs a = pass_args(t, k, probe_phase, noise_proj);
     a.tw = t->tw_c;
     PTY_CK(t->kc.fwd(a, st));
     a.tw = t->tw_r;
@@ -647,12 +653,15 @@ int enqueue_sweep(cdx_pty* t, bool probe_phase) {
   return CDX_OK;
 }
 
-int ensure_graph(cdx_pty* t, bool probe_phase) {
-  cudaGraphExec_t& g = t->graph[probe_phase ? 1 : 0];
+// sweep kind of iteration `it`: 0 object phase, 1 probe phase, 2 probe phase with applyMod
+int sweep_kind(int it) { return it < kUpdateProbeIter ? 0 : (it < kNoiseProjIter ? 1 : 2); }
+
+int ensure_graph(cdx_pty* t, int kind) {
+  cudaGraphExec_t& g = t->graph[kind];
   if (g) return CDX_OK;
   cudaGraph_t graph = nullptr;
   PTY_CK(cudaStreamBeginCapture(t->st, cudaStreamCaptureModeThreadLocal));
-  const int r = enqueue_sweep(t, probe_phase);
+  const int r = enqueue_sweep(t, kind >= 1, kind == 2);
   const cudaError_t e = cudaStreamEndCapture(t->st, &graph);
   if (r != CDX_OK) {
     if (graph) cudaGraphDestroy(graph);
@@ -698,6 +707,8 @@ int cdx_pty_create(const cdx_pty_params* p, void* stream, cdx_pty** out) {
   if (!p || !out) return set_error(CDX_ERR_ARG, "null argument");
   *out = nullptr;
   if (p->nscan < 1 || p->obj_rows < 1 || p->obj_cols < 1) return set_error(CDX_ERR_ARG, "bad scan count or object size");
+  if (p->noise_level < 0 || !(p->position_uncertainty >= 0))
+    return set_error(CDX_ERR_ARG, "noise_level and position_uncertainty must be >= 0");
   if (!(p->lambda > 0) || !(p->pixelsize > 0) || !(p->d > 0) || !(p->exposure > 0))
     return set_error(CDX_ERR_ARG, "lambda, d, pixelsize and exposure must be positive");
   const int pd = (int)p->pupil_size;
@@ -917,9 +928,9 @@ int cdx_pty_simulate(cdx_pty* t) {
 int cdx_pty_iterate(cdx_pty* t, int first_iter, int n_iter, const int* orders, unsigned int seed) {
   if (!t) return set_error(CDX_ERR_ARG, "null argument");
   if (first_iter < 0 || n_iter < 0) return set_error(CDX_ERR_ARG, "negative iteration index or count");
-  if (first_iter + n_iter > kPositionUpdateIter)
-    return set_error(CDX_ERR_ARG, "iterations from 500 on refine the scan positions, which is not built "
-                                  "(first_iter + n_iter must be <= 500)");
+  if (first_iter + n_iter > kPositionUpdateIter && t->p.position_uncertainty > 0)
+    return set_error(CDX_ERR_ARG, "iterations from 500 on refine the scan positions (position_uncertainty > 0), "
+                                  "which is not built: first_iter + n_iter must be <= 500");
   if (!t->have_scan || !t->have_pats || !t->have_obj || !t->have_probe)
     return set_error(CDX_ERR_STATE, "scan positions, patterns, object and probe must be set first");
   const int ns = t->p.nscan;
@@ -969,11 +980,9 @@ int cdx_pty_iterate(cdx_pty* t, int first_iter, int n_iter, const int* orders, u
                                                      t->p.obj_cols, (float)(t->p.pupil_size / 2));
   k_pty_bitmap<<<grid1(t->onpx), 256, 0, st>>>(t->msum, t->onpx);
   PTY_CK(cudaGetLastError());
-  PTY_RET(ensure_graph(t, false));
-  if (first_iter + n_iter > kUpdateProbeIter) PTY_RET(ensure_graph(t, true));
+  for (int it = first_iter; it < first_iter + n_iter; ++it) PTY_RET(ensure_graph(t, sweep_kind(it)));
   PTY_CK(cudaEventRecord(t->e0, st));
-  for (int it = first_iter; it < first_iter + n_iter; ++it)
-    PTY_CK(cudaGraphLaunch(t->graph[it >= kUpdateProbeIter ? 1 : 0], st));
+  for (int it = first_iter; it < first_iter + n_iter; ++it) PTY_CK(cudaGraphLaunch(t->graph[sweep_kind(it)], st));
   // final global phase of the object (util/ptycho.cpp:731-735)
   k_pty_csum<<<kRedBlocks, 256, 0, st>>>(t->O, nullptr, t->onpx, t->part, t->scal, t->cnt + 3, 1);
   k_pty_conj_phase<<<grid1(t->onpx), 256, 0, st>>>(t->O, t->onpx, t->scal);

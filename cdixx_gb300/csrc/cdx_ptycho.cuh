@@ -32,6 +32,10 @@ struct PtyArgs {
   float maximum;           // 0.95 * vars.scale, the saturation level of applyModAccurate
   float obj_step;          // rPIE step of the object: 1, or 0.5 in the probe phase
   float pss;               // probe step size 1/nscan
+  int noise_proj;          // iteration >= 2000: applyMod (noise-tolerant) instead of applyModAccurate
+  int noise_level;         // noiseLevel
+  float ccd_scale;         // vars.scale = 1/exposure
+  float rcolor;            // vars.rcolor
 };
 
 constexpr float kPtyAlpha = 0.1f;   // ALPHA, src/gpu/ptycho.cu:5
@@ -64,6 +68,26 @@ __device__ __forceinline__ float2 pty_modacc(float2 s, float inten, float bsv, b
   if (src == 0.f) return s;
   if (mod2 >= maximum && src >= mod2) return make_float2(rx, ry);
   const float sc = sqrtf(mod2 / src);
+  return make_float2(sc * rx, sc * ry);
+}
+
+// applyMod, 5-argument form with bsnorm (src/gpu/cdi.cu:438-485): the
+// noise-tolerant projection the reference switches to from iteration 2000.
+__device__ __forceinline__ float2 pty_modnoise(float2 s, float inten, float bsv, bool has_bs, float norm, int noise,
+                                               float scale, float rcolor) {
+  float mod2 = fmaxf(0.f, inten);
+  if (has_bs && bsv > 0.5f) return norm != 1.f ? make_float2(s.x * norm, s.y * norm) : s;
+  float rx = s.x, ry = s.y;
+  if (norm != 1.f) { rx *= norm; ry *= norm; }
+  const float src = rx * rx + ry * ry;
+  if (mod2 >= scale * 0.95f) mod2 = fmaxf(mod2, src);
+  const float tol = sqrtf(noise + mod2 * rcolor / scale) * scale / rcolor;
+  const float diff = mod2 - src;
+  float val = mod2;
+  if (diff > tol) val -= tol;
+  else if (diff < -tol) val += tol;
+  if (src == 0.f) return make_float2(val, 0.f);
+  const float sc = sqrtf(fmaxf(val, 0.f) / src);
   return make_float2(sc * rx, sc * ry);
 }
 
@@ -184,7 +208,10 @@ __global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_COL) pty_col_rk(Pty
 #pragma unroll
     for (int r = 0; r < FL::R; ++r) {
       const int t = (j + r * FL::NS) * L + l;
-      const float2 z = pty_modacc(v[b][r], int_s[t], has_bs ? bs_s[t] : 0.f, has_bs, a.norm, a.maximum);
+      const float bsv = has_bs ? bs_s[t] : 0.f;
+      const float2 z = a.noise_proj ? pty_modnoise(v[b][r], int_s[t], bsv, has_bs, a.norm, a.noise_level,
+                                                   a.ccd_scale, a.rcolor)
+                                    : pty_modacc(v[b][r], int_s[t], bsv, has_bs, a.norm, a.maximum);
       v[b][r] = l < ncols ? z : make_float2(0.f, 0.f);
     }
   }

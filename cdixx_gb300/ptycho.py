@@ -22,7 +22,8 @@ class PtyParams(ctypes.Structure):
                 ("obj_cols", ctypes.c_int), ("nscan", ctypes.c_int), ("lambda_", ctypes.c_double),
                 ("d", ctypes.c_double), ("dpupil", ctypes.c_double), ("pixelsize", ctypes.c_double),
                 ("pupil_size", ctypes.c_double), ("exposure", ctypes.c_double), ("mpie", ctypes.c_int),
-                ("use_bs", ctypes.c_int), ("beam_stop_size", ctypes.c_int)]
+                ("use_bs", ctypes.c_int), ("beam_stop_size", ctypes.c_int), ("noise_level", ctypes.c_int),
+                ("position_uncertainty", ctypes.c_double)]
 
 
 def _c64(a, shape):
@@ -70,7 +71,8 @@ class Ptycho:
     """GPU ptychography context: rows x cols probe and patterns, obj_rows x obj_cols object."""
 
     def __init__(self, rows, cols, obj_rows, obj_cols, scanposx, scanposy, *, lam, d, dpupil, pixelsize,
-                 pupil_size=500.0, exposure=1.0, mpie=True, use_bs=False, beam_stop_size=5, stream=None):
+                 pupil_size=500.0, exposure=1.0, mpie=True, use_bs=False, beam_stop_size=5, noise_level=0,
+                 position_uncertainty=0.0, stream=None):
         p = PtyParams()
         check(lib().cdx_pty_params_default(ctypes.byref(p)))
         p.rows, p.cols, p.obj_rows, p.obj_cols = rows, cols, obj_rows, obj_cols
@@ -82,6 +84,7 @@ class Ptycho:
         p.lambda_, p.d, p.dpupil, p.pixelsize = lam, d, dpupil, pixelsize
         p.pupil_size, p.exposure, p.mpie = pupil_size, exposure, int(bool(mpie))
         p.use_bs, p.beam_stop_size = int(bool(use_bs)), beam_stop_size
+        p.noise_level, p.position_uncertainty = noise_level, position_uncertainty
         self.params = p
         self.row, self.column, self.row_O, self.column_O, self.nscan = rows, cols, obj_rows, obj_cols, p.nscan
         self._h = ctypes.c_void_p()

@@ -40,6 +40,8 @@ typedef struct cdx_pty_params {
   int mpie;                /* momentum step after each sweep (mPIE, default 1) */
   int use_bs;              /* beamstop of radius beam_stop_size at the pattern centre (useBS) */
   int beam_stop_size;
+  int noise_level;         /* noiseLevel: tolerance of the modulus projection from iteration 2000 */
+  double position_uncertainty; /* positionUncertainty: > 0 asks for scan-position refinement (not built) */
 } cdx_pty_params;
 
 /* Defaults of readConfig (include/readConfig.hpp): mPIE 1, pupilSize 500,
@@ -82,13 +84,17 @@ int cdx_pty_simulate(cdx_pty* t);
 
 /* ptycho::iterate: n_iter sweeps starting at iteration index first_iter
  * (the reference always starts at 0; from index 400 the probe is updated and
- * constrained).  orders: n_iter x nscan scan indices, one permutation per
+ * constrained, from 2000 the modulus projection is the noise-tolerant
+ * applyMod).  orders: n_iter x nscan scan indices, one permutation per
  * sweep, or NULL to draw them as the reference does (shuffle_array with a
  * rand() stream seeded by `seed`, the generator of the C library restated).
  * Fresh per-call state as in the reference (zero momentum history and probe
- * step).  The reference refines scan positions from iteration 500 on; that
- * step is not built, so first_iter + n_iter must be <= 500.  The final object
- * has its global phase removed (util/ptycho.cpp:731-735). */
+ * step).  From iteration 500 the reference refines the scan positions every
+ * 20 sweeps; with position_uncertainty = 0 (its default) that step leaves
+ * the positions at zero shift and the object unchanged up to the rounding of
+ * an FFT round trip, which is not repeated here; with position_uncertainty > 0
+ * runs past iteration 500 are refused (refinement not built).  The final
+ * object has its global phase removed (util/ptycho.cpp:731-735). */
 int cdx_pty_iterate(cdx_pty* t, int first_iter, int n_iter, const int* orders, unsigned int seed);
 
 /* Device time of the last cdx_pty_iterate in milliseconds. */

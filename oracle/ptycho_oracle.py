@@ -13,8 +13,11 @@ config fields where the reference has them).  The FFT is the unnormalised DFT
 via NumPy (cuFFT's published transform), reductions accumulate in float64.
 
 Scope: the iteration without Fresnel propagation, Zernike/FISTA pupil steps and
-position refinement (the reference starts refining at iteration 500, so runs
-are limited to 500 iterations).  It is pinned by the reference's own driver
+scan-position refinement.  From iteration 500 the reference refines the
+positions every 20 sweeps; with positionUncertainty = 0 (its default) that
+leaves every shift at zero and the object changed only by the rounding of an
+FFT round trip, which is not repeated here; runs with positionUncertainty > 0
+past iteration 500 are refused.  It is pinned by the reference's own driver
 built as host code (oracle/build_ref.sh -> oracle/_ref/pty_harness).
 """
 from __future__ import annotations
@@ -32,6 +35,8 @@ ALPHA = F32(0.1)    # src/gpu/ptycho.cu:5
 BETA = F32(0.5)     # src/gpu/ptycho.cu:6
 UPDATE_PROBE_ITER = 400      # util/ptycho.cpp:441
 POSITION_UPDATE_ITER = 500   # util/ptycho.cpp:442
+NOISE_PROJ_ITER = 2000       # applyMod instead of applyModAccurate, util/ptycho.cpp:536-545
+RCOLOR = F32(65535)          # include/format.hpp:21
 
 
 # --------------------------------------------------------------------------- FFT
@@ -186,6 +191,28 @@ def apply_mod_accurate(F, pattern, norm, scale, bs=None):
     return out.astype(C64)
 
 
+def apply_mod_noise(F, pattern, norm, scale, noise_level, bs=None):
+    """applyMod, 5-argument form with bsnorm (src/gpu/cdi.cu:438-485): the projection
+    toward the measured intensity stops a tolerance sqrt(noise + I rcolor/scale)
+    scale/rcolor short of it; saturated pixels (I >= 0.95 scale) take max(I, |F|^2)."""
+    mod2 = np.maximum(F32(0), pattern.astype(F32))
+    rx = (F.real * F32(norm)).astype(F32) if norm != 1 else F.real.astype(F32)
+    ry = (F.imag * F32(norm)).astype(F32) if norm != 1 else F.imag.astype(F32)
+    src = (rx * rx + ry * ry).astype(F32)
+    sc = F32(scale)
+    mod2 = np.where(mod2 >= F32(sc * F32(0.95)), np.maximum(mod2, src), mod2).astype(F32)
+    tol = (np.sqrt((F32(noise_level) + ((mod2 * RCOLOR).astype(F32) / sc).astype(F32)).astype(F32)) * sc / RCOLOR).astype(F32)
+    diff = (mod2 - src).astype(F32)
+    val = np.where(diff > tol, mod2 - tol, np.where(diff < -tol, mod2 + tol, mod2)).astype(F32)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        s = np.sqrt((np.maximum(val, F32(0)) / np.where(src == 0, F32(1), src)).astype(F32)).astype(F32)
+    out = ((s * rx).astype(F32) + 1j * (s * ry).astype(F32)).astype(C64)
+    out = np.where(src == 0, (val + 0j).astype(C64), out)
+    if bs is not None:
+        out = np.where(bs > F32(0.5), (rx + 1j * ry).astype(C64), out)
+    return out.astype(C64)
+
+
 def _rpie_denom(source_mod2, maxi, param, stepsize):
     """The denominator of rPIE / rPIE_step (src/gpu/ptycho.cu:55-68):
     stepsize / ((1 - param) |s|^2 + param max(maxi, 1e-5)), the max and the
@@ -282,6 +309,8 @@ class PtyParams:
     mpie: bool = True
     use_bs: bool = False
     beam_stop_size: int = 5
+    noise_level: int = 0
+    position_uncertainty: float = 0.0
 
     def resolution(self, rows):
         """resolution = lambda d / pixelsize / row (util/ptycho.cpp:246), stored as float."""
@@ -304,7 +333,7 @@ def simulate_patterns(obj, probe, scanx, scany, exposure=1.0):
 
 
 def iterate(obj0, probe0, patterns, scanx, scany, n_iter, params: PtyParams, orders, start_iter=0):
-    """ptycho::iterate (util/ptycho.cpp:429-736) for n_iter <= 500: per scan
+    """ptycho::iterate (util/ptycho.cpp:429-736): per scan
     position (in the given order) the window times the probe, FFT, applyModAccurate,
     inverse FFT, the difference of exit waves and the rPIE object update
     (updateObject; from iteration 400 updateObjectAndProbeStep with the probe
@@ -317,8 +346,8 @@ def iterate(obj0, probe0, patterns, scanx, scany, n_iter, params: PtyParams, ord
     removed, as the reference leaves them.  Returns (object, pupil)."""
     rows, cols = probe0.shape
     orow, ocol = obj0.shape
-    if n_iter > POSITION_UPDATE_ITER:
-        raise ValueError("position refinement (iterations >= 500) is outside this restatement")
+    if start_iter + n_iter > POSITION_UPDATE_ITER and params.position_uncertainty > 0:
+        raise ValueError("position refinement (iterations >= 500, positionUncertainty > 0) is outside this restatement")
     O = obj0.astype(C64).copy()
     Oprev = np.zeros_like(O)
     P = probe0.astype(C64).copy()
@@ -356,7 +385,10 @@ def iterate(obj0, probe0, patterns, scanx, scany, n_iter, params: PtyParams, ord
             w = get_window(O, sx, sy, rows, cols)
             esw = (P * w).astype(C64)
             F = fft2_u(esw)
-            F = apply_mod_accurate(F, patterns[i], norm, scale, bs)
+            if it < NOISE_PROJ_ITER:
+                F = apply_mod_accurate(F, patterns[i], norm, scale, bs)
+            else:
+                F = apply_mod_noise(F, patterns[i], norm, scale, params.noise_level, bs)
             F = (ifft2_u(F) * norm).astype(C64)
             diff = (esw - F).astype(C64)
             if it < UPDATE_PROBE_ITER:

@@ -10,7 +10,7 @@
 // pty_harness <object.bin> <probe.bin> <patterns.bin (nscan stacked, FFT order,
 //             scaled 1/exposure)> <scan.txt ("x y" per line)> <nIter> <mPIE>
 //             <lambda> <d> <dpupil> <pixelsize> <pupilSize> <exposure>
-//             <useBS> <beamStopSize> <rand seed> <out prefix>
+//             <useBS> <beamStopSize> <rand seed> <out prefix> [noiseLevel]
 #define main cdxref_ptycho_main
 #include CDXREF_PTYCHO_CPP
 #undef main
@@ -62,6 +62,7 @@ int main(int argc, char** argv) {
   p.exposure = atof(argv[12]);
   p.useBS = atoi(argv[13]);
   p.beamStopSize = atoi(argv[14]);
+  p.noiseLevel = argc > 17 ? atoi(argv[17]) : 0;
   // what the constructor would have taken from the config file
   p.propagate_esw.lambda = p.propagate_pupil.lambda = p.lambda;
   p.propagate_esw.distance = p.d;

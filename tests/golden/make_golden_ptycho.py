@@ -40,7 +40,10 @@ CASES = [
     ("saturated", 6, 1, 0, 5, 2.0, 200.0, "grid", 9),
     ("offedge", 6, 1, 0, 5, 1.0, 40.0, "edge", 13),
     ("probe402", 402, 1, 0, 5, 1.0, 40.0, "grid", 7),
+    ("refine520", 520, 0, 0, 5, 1.0, 40.0, "grid", 7),
+    ("noise2003", 2003, 0, 0, 5, 1.0, 40.0, "grid", 7),
 ]
+NOISE_LEVEL = {"noise2003": 20}
 OPTICS = dict(lam=0.5, d=2e4, dpupil=1e3, pixelsize=20.0, pupil_size=16.0)
 
 
@@ -89,7 +92,8 @@ def main(ref=None):
                     f.write(f"{float(a)!r} {float(b)!r}\n")
             cmd = [str(harness), f"{d}/obj.bin", f"{d}/probe.bin", f"{d}/pats.bin", f"{d}/scan.txt", str(n_iter),
                    str(mpie), str(OPTICS["lam"]), str(OPTICS["d"]), str(OPTICS["dpupil"]), str(OPTICS["pixelsize"]),
-                   str(OPTICS["pupil_size"]), str(expo), str(use_bs), str(bss), str(seed), f"{d}/out"]
+                   str(OPTICS["pupil_size"]), str(expo), str(use_bs), str(bss), str(seed), f"{d}/out",
+                   str(NOISE_LEVEL.get(name, 0))]
             subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL)
             p = f"{name}/"
             data[p + "obj0"] = obj0
@@ -98,7 +102,7 @@ def main(ref=None):
             data[p + "scanx"] = sx
             data[p + "scany"] = sy
             data[p + "orders"] = PO.scan_orders(len(sx), n_iter, seed)
-            data[p + "cfg"] = np.array([n_iter, mpie, use_bs, bss, seed], np.int64)
+            data[p + "cfg"] = np.array([n_iter, mpie, use_bs, bss, seed, NOISE_LEVEL.get(name, 0)], np.int64)
             data[p + "exposure"] = np.float64(expo)
             data[p + "ref_object"] = read_bin(f"{d}/out_object.bin").copy()
             data[p + "ref_pupil"] = read_bin(f"{d}/out_pupil.bin").copy()

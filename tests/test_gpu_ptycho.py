@@ -25,7 +25,8 @@ def make(PT, c, prm, rows=None, obj_shape=None):
     orow, ocol = obj_shape or c["obj0"].shape
     t = PT.Ptycho(rows, c["probe0"].shape[1], orow, ocol, c["scanx"], c["scany"], lam=prm.lam, d=prm.d,
                   dpupil=prm.dpupil, pixelsize=prm.pixelsize, pupil_size=prm.pupil_size, exposure=prm.exposure,
-                  mpie=prm.mpie, use_bs=prm.use_bs, beam_stop_size=prm.beam_stop_size)
+                  mpie=prm.mpie, use_bs=prm.use_bs, beam_stop_size=prm.beam_stop_size,
+                  noise_level=prm.noise_level, position_uncertainty=prm.position_uncertainty)
     t.objectWave = c["obj0"]
     t.probe = c["probe0"]
     t.patterns = c["pats"]
@@ -49,13 +50,14 @@ def test_gpu_draws_the_reference_orders_from_the_seed(PT):
         assert np.array_equal(a.objectWave, b.objectWave)
 
 
-@pytest.mark.parametrize("first", [0, 7, 400, 450])
+@pytest.mark.parametrize("first", [0, 7, 400, 450, 520, 2000])
 @pytest.mark.parametrize("mpie", [False, True])
 def test_one_sweep_matches_oracle(PT, first, mpie):
     """Per-iterate parity: one sweep (object phase, or probe phase from 400) from
     the same object and probe as the oracle."""
     c, prm, _n, _s = load("obj3")
     prm.mpie = mpie
+    prm.noise_level = 20   # the noise-tolerant projection from iteration 2000
     rng = np.random.default_rng(first)
     obj = (c["obj0"] * (0.5 + rng.random(c["obj0"].shape))).astype(np.complex64)
     orders = np.array([rng.permutation(len(c["scanx"]))], np.int32)
@@ -128,6 +130,7 @@ def test_init_object_matches_oracle(PT):
 
 def test_argument_checks(PT, cdx):
     c, prm, _n, _s = load("obj3")
+    prm.position_uncertainty = 2.0
     with make(PT, c, prm) as t:
         with pytest.raises(cdx.CdxError):
             t.iterate(10, first_iter=495)          # position refinement from 500 is not built
