@@ -527,3 +527,33 @@ def test_prtf_matches_oracle(cdx, alg, prtf_iter, tol):
         ctx.run(f"{prtf_iter - 1}*ER")
         with pytest.raises(cdx.CdxError):
             ctx.get_prtf(0)
+
+
+SHAPES = [(16, 16), (24, 48), (48, 24), (96, 256), (256, 96), (384, 1536), (1536, 384), (3072, 512), (512, 4096),
+          (4096, 4096)]
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+@pytest.mark.parametrize("algo,beta", [("HIO", 0.9), ("RAAR", 0.9)])
+def test_one_step_every_geometry(cdx, shape, algo, beta):
+    """One iteration (column pass + row pass) at square and rectangular sizes
+    that cover every launch geometry: L from 2 to 256 lines per CTA, 256- and
+    512-thread CTAs (3072, 4096), row and column lengths of different plans.
+    Against the FP64 oracle's step from the same Psi0."""
+    rows, cols = shape
+    rng = np.random.default_rng(rows * 7 + cols)
+    obj = np.zeros((rows, cols), np.complex128)
+    r0, c0 = rows // 4, cols // 4
+    obj[r0:r0 + rows // 2, c0:c0 + cols // 2] = rng.random((rows // 2, cols // 2)) * np.exp(
+        1j * rng.random((rows // 2, cols // 2)))
+    I = (np.abs(np.fft.fft2(obj)) ** 2 / (rows * cols)).astype(np.float32)
+    psi0 = (np.sqrt(I) * np.exp(2j * np.pi * rng.random((rows, cols)))).astype(np.complex64)
+    ref = O.phase_retrieve(psi0, I, f"1*{algo}", oversampling_spt=2.0, beta=beta)
+    p = cdx.default_params(rows, cols, oversampling_spt=2.0, beta=beta)
+    with cdx.Context(p) as ctx:
+        ctx.set_pattern(0, I)
+        ctx.set_initial(0, psi0)
+        ctx.run(f"1*{algo}")
+        e_rho = rel_l2(ctx.get_object(0), ref.rho)
+        e_psi = rel_l2(ctx.get_fourier(0), ref.psi)
+    assert e_rho <= 1e-5 and e_psi <= 1e-5, (shape, algo, e_rho, e_psi)
