@@ -12,6 +12,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <tuple>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -119,6 +120,11 @@ struct cdx_ctx {
   PrtfState* pr_state = nullptr;
   bool pr_valid = false;       // the last run reached prtf_iter
   bool pr_reached = false;     // set while enqueueing
+
+  // launch variant (autotune): RowArgs/ColArgs knobs, and what was measured
+  int tune_pdl_mode = 0, tune_cb_plus1 = 0;
+  bool tuned = false;
+  std::string tune_report;
 
   // graph cache
   std::string gkey;
@@ -271,6 +277,7 @@ int col_iter(cdx_ctx* c, bool from_psi, bool rf, float2* psi_proj = nullptr) {
   a.scale = 1.f;
   a.ccd_scale = 1.f / c->p.exposure;
   a.ccd_rcolor = (float)c->p.rcolor;
+  a.pdl_mode = c->tune_pdl_mode;
   CDX_CK(col_launcher(c->rows)(a, c->batch, c->st));
   return CDX_OK;
 }
@@ -295,6 +302,8 @@ int row_iter(cdx_ctx* c, int algo) {
   a.scale = 1.f;
   a.inv_n = (float)(1.0 / ((double)c->rows * c->cols));   // applyNorm(.., 1./(row*column)), cdi.cc:353
   a.beta = c->p.beta;
+  a.cb_plus1 = c->tune_cb_plus1;
+  a.pdl_mode = c->tune_pdl_mode;
   CDX_CK(row_launcher(c->cols)(a, c->batch, c->st));
   return CDX_OK;
 }
@@ -452,12 +461,108 @@ int prepare_run(cdx_ctx* c, const char* algorithm, std::vector<int>& steps, SwPl
   return CDX_OK;
 }
 
+// Autotuner: before the first run of a context with autotune set, time the
+// iteration (column pass + row pass, HIO; eight of them captured in a graph,
+// as runs execute) under each launch variant --
+// programmatic dependent launch off/on x the row pass's butterfly chunk bits
+// (the default and up to two below it) -- on a copy of the context's own
+// state, restore the state, and keep the fastest.  Decisions are cached per
+// (device, rows, cols, batch) for the process.
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, int, int>, std::pair<int, int>> g_tune;
+
+int autotune(cdx_ctx* c) {
+  const auto key = std::make_tuple(c->device, c->rows, c->cols, c->batch);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) {
+      c->tune_pdl_mode = it->second.first;
+      c->tune_cb_plus1 = it->second.second;
+      c->tuned = true;
+      c->tune_report = "cached";
+      return CDX_OK;
+    }
+  }
+  if (c->p.fft_mode != CDX_FFT_FP32) {   // the tensor-core kernels have neither knob
+    c->tuned = true;
+    return CDX_OK;
+  }
+  const size_t nrho = (size_t)c->npx * c->batch, nw = (size_t)c->wstride * c->batch;
+  float2 *srho = nullptr, *sw = nullptr;
+  if (cudaMalloc(&srho, sizeof(float2) * nrho) != cudaSuccess || cudaMalloc(&sw, sizeof(float2) * nw) != cudaSuccess) {
+    cudaGetLastError();
+    if (srho) cudaFree(srho);
+    return set_error(CDX_ERR_NOMEM, "autotune: no room for a copy of the state");
+  }
+  CDX_CK(cudaMemcpyAsync(srho, c->rho, sizeof(float2) * nrho, cudaMemcpyDeviceToDevice, c->st));
+  CDX_CK(cudaMemcpyAsync(sw, c->work, sizeof(float2) * nw, cudaMemcpyDeviceToDevice, c->st));
+  const int cbd = row_cb_default(c->cols, c->tl);
+  int best_pdl = 0, best_cb = 0;
+  double best = 1e30;
+  std::string rep;
+  int e = CDX_OK;
+  for (int pdl = 1; pdl <= 2 && e == CDX_OK; ++pdl)
+    for (int cb = cbd; cb >= std::max(0, cbd - 2) && e == CDX_OK; --cb) {
+      c->tune_pdl_mode = pdl;
+      c->tune_cb_plus1 = cb + 1;
+      // timed as the runs execute: kTimed iterations captured in one graph,
+      // launched once to warm up and once under the events
+      constexpr int kTimed = 8;
+      cudaGraph_t g = nullptr;
+      cudaGraphExec_t ge = nullptr;
+      CDX_CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+      for (int i = 0; i < kTimed && e == CDX_OK; ++i) {
+        e = col_iter(c, false, false);
+        if (e == CDX_OK) e = row_iter(c, ALGO_HIO);
+      }
+      const cudaError_t ce = cudaStreamEndCapture(c->st, &g);
+      if (e == CDX_OK && ce != cudaSuccess) e = set_error(CDX_ERR_CUDA, std::string("autotune capture: ") + cudaGetErrorString(ce));
+      if (e == CDX_OK && cudaGraphInstantiate(&ge, g, 0) != cudaSuccess) e = set_error(CDX_ERR_CUDA, "autotune graph");
+      if (g) cudaGraphDestroy(g);
+      float ms = 0.f;
+      if (e == CDX_OK) {
+        cudaError_t le = cudaGraphLaunch(ge, c->st);
+        if (le == cudaSuccess) le = cudaEventRecord(c->ev0, c->st);
+        if (le == cudaSuccess) le = cudaGraphLaunch(ge, c->st);
+        if (le == cudaSuccess) le = cudaEventRecord(c->ev1, c->st);
+        if (le == cudaSuccess) le = cudaEventSynchronize(c->ev1);
+        if (le == cudaSuccess) le = cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+        if (le != cudaSuccess) e = set_error(CDX_ERR_CUDA, std::string("autotune: ") + cudaGetErrorString(le));
+      }
+      if (ge) cudaGraphExecDestroy(ge);
+      if (e != CDX_OK) break;
+      const double us = 1000.0 * ms / kTimed;
+      char line[96];
+      snprintf(line, sizeof line, "pdl=%d chunk=%d: %.2f us\n", pdl - 1, cb, us);
+      rep += line;
+      if (us < best) { best = us; best_pdl = pdl; best_cb = cb + 1; }
+    }
+  // restore the state the runs iterated on
+  if (e == CDX_OK) {
+    CDX_CK(cudaMemcpyAsync(c->rho, srho, sizeof(float2) * nrho, cudaMemcpyDeviceToDevice, c->st));
+    CDX_CK(cudaMemcpyAsync(c->work, sw, sizeof(float2) * nw, cudaMemcpyDeviceToDevice, c->st));
+    CDX_CK(cudaStreamSynchronize(c->st));
+  }
+  cudaFree(srho);
+  cudaFree(sw);
+  if (e != CDX_OK) return e;
+  c->tune_pdl_mode = best_pdl;
+  c->tune_cb_plus1 = best_cb;
+  c->tuned = true;
+  c->tune_report = rep;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune[key] = {best_pdl, best_cb};
+  return CDX_OK;
+}
+
 int run_impl(cdx_ctx* c, const char* algorithm) {
   std::vector<int> steps;
   SwPlan sw;
   int e = prepare_run(c, algorithm, steps, sw);
   if (e) return e;
   CDX_CK(cudaSetDevice(c->device));
+  if (c->p.autotune && !c->tuned && c->last_iters > 0 && (e = autotune(c))) return e;
   const bool piw = c->psi_in_work;
   if (c->p.use_graph) {
     char key[64];
@@ -753,6 +858,17 @@ int cdx_get_prtf(cdx_ctx* c, int idx, float* out, int where) {
   for (int i = 0; i < h; ++i) v[i] = v[i] / w[i];   // prtf[i]/weights[i] (cdi.cc:437-439)
   if (where == CDX_DEVICE) CDX_CK(cudaMemcpy(out, v.data(), sizeof(float) * h, cudaMemcpyHostToDevice));
   else memcpy(out, v.data(), sizeof(float) * h);
+  return CDX_OK;
+}
+
+int cdx_get_tuning(cdx_ctx* c, int* pdl, int* row_chunk, char* report, int cap) {
+  if (!c) return set_error(CDX_ERR_ARG, "null context");
+  if (pdl) *pdl = c->tune_pdl_mode == 0 ? -1 : c->tune_pdl_mode - 1;
+  if (row_chunk) *row_chunk = c->tune_cb_plus1 - 1;
+  if (report && cap > 0) {
+    std::strncpy(report, c->tune_report.c_str(), (size_t)cap - 1);
+    report[cap - 1] = 0;
+  }
   return CDX_OK;
 }
 

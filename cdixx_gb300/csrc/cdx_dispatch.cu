@@ -1,7 +1,9 @@
 // Length -> kernel dispatch for the row/column passes, and the twiddle tables.
+#include <algorithm>
 #include <cmath>
 
 #include "cdx_fft.cuh"
+#include "cdx_rfft.cuh"
 #include "cdx_types.h"
 
 namespace cdx {
@@ -35,6 +37,11 @@ int lines_per_cta(int n) {
 int twiddle_count(int n) {
   switch (n) { CDX_FOR_EACH_SIZE(CASE_TW) default: return 0; }
 }
+#define CASE_CB(N) case N: return rfft_cb_max<N>();
+int row_cb_max(int n) {
+  switch (n) { CDX_FOR_EACH_SIZE(CASE_CB) default: return 0; }
+}
+int row_cb_default(int n, int tile_log2) { return std::min(tile_log2, row_cb_max(n)); }
 
 // Entry (r-1)*NS + k of pass p's block = W_n^(r*k*n/(NS*R)), W_n = exp(-2 pi i/n),
 // evaluated in double with the exponent reduced mod n and rounded once to float;

@@ -379,7 +379,8 @@ __device__ __forceinline__ void row_pass_body(const RowArgs& a) {
   // tiled: four (or 2^tl) threads per tile row piece; row-major: consecutive
   // threads take consecutive columns
   const bool tiled = a.in_tiled || a.out_tiled;
-  const int cb = tiled ? min(tl, rfft_cb_max<N>()) : rfft_cb_max<N>();
+  const int cb = a.cb_plus1 > 0 ? min(a.cb_plus1 - 1, rfft_cb_max<N>())
+                                : (tiled ? min(tl, rfft_cb_max<N>()) : rfft_cb_max<N>());
 
   // rho rows and support words of the CTA (ROW_ITER), landing during the inverse FFT
   constexpr int RS = G::LD;                 // rho line stride in shared memory

@@ -61,6 +61,9 @@ cudaError_t prepare_len() {
 // costs 1.3 % at 2048^2 (60.7 against 59.9 us), so that length launches plainly.
 template <int N>
 constexpr bool pass_pdl() { return N != 2048; }
+// launch mode of a pass: the per-length default, or the autotuner's choice (1 plain, 2 PDL)
+template <int N>
+bool pdl_of(int mode) { return mode == 0 ? pass_pdl<N>() : mode == 2; }
 
 template <int N>
 cudaError_t launch_row(const RowArgs& a, int batch, cudaStream_t st) {
@@ -71,14 +74,14 @@ cudaError_t launch_row(const RowArgs& a, int batch, cudaStream_t st) {
     else row_pass_kernel<N, ROW_FFT, true><<<grid, G::T, G::SMEM_LINES, st>>>(a);
   } else {
     constexpr int SM = RGeom<N>::SMEM_ROW_ITER;
-    if (a.mode != ROW_ITER) return launch_pdl(row_pass_rk<N, ROW_FFT, ALGO_ER>, grid, G::T, G::SMEM_LINES, st, a, pass_pdl<N>());
+    if (a.mode != ROW_ITER) return launch_pdl(row_pass_rk<N, ROW_FFT, ALGO_ER>, grid, G::T, G::SMEM_LINES, st, a, pdl_of<N>(a.pdl_mode));
     switch (a.algo) {   // unknown codes take the FHIO branch, as applySupport does (cdi.cc:25-36)
-      case ALGO_HIO: return launch_pdl(row_pass_rk<N, ROW_ITER, ALGO_HIO>, grid, G::T, SM, st, a, pass_pdl<N>());
-      case ALGO_RAAR: return launch_pdl(row_pass_rk<N, ROW_ITER, ALGO_RAAR>, grid, G::T, SM, st, a, pass_pdl<N>());
-      case ALGO_ER: return launch_pdl(row_pass_rk<N, ROW_ITER, ALGO_ER>, grid, G::T, SM, st, a, pass_pdl<N>());
-      case ALGO_POSER: return launch_pdl(row_pass_rk<N, ROW_ITER, ALGO_POSER>, grid, G::T, SM, st, a, pass_pdl<N>());
-      case ALGO_POSHIO: return launch_pdl(row_pass_rk<N, ROW_ITER, ALGO_POSHIO>, grid, G::T, SM, st, a, pass_pdl<N>());
-      default: return launch_pdl(row_pass_rk<N, ROW_ITER, ALGO_FHIO>, grid, G::T, SM, st, a, pass_pdl<N>());
+      case ALGO_HIO: return launch_pdl(row_pass_rk<N, ROW_ITER, ALGO_HIO>, grid, G::T, SM, st, a, pdl_of<N>(a.pdl_mode));
+      case ALGO_RAAR: return launch_pdl(row_pass_rk<N, ROW_ITER, ALGO_RAAR>, grid, G::T, SM, st, a, pdl_of<N>(a.pdl_mode));
+      case ALGO_ER: return launch_pdl(row_pass_rk<N, ROW_ITER, ALGO_ER>, grid, G::T, SM, st, a, pdl_of<N>(a.pdl_mode));
+      case ALGO_POSER: return launch_pdl(row_pass_rk<N, ROW_ITER, ALGO_POSER>, grid, G::T, SM, st, a, pdl_of<N>(a.pdl_mode));
+      case ALGO_POSHIO: return launch_pdl(row_pass_rk<N, ROW_ITER, ALGO_POSHIO>, grid, G::T, SM, st, a, pdl_of<N>(a.pdl_mode));
+      default: return launch_pdl(row_pass_rk<N, ROW_ITER, ALGO_FHIO>, grid, G::T, SM, st, a, pdl_of<N>(a.pdl_mode));
     }
   }
   return cudaGetLastError();
@@ -93,9 +96,9 @@ cudaError_t launch_col(const ColArgs& a, int batch, cudaStream_t st) {
     if (a.mode == COL_ITER) col_pass_kernel<N, COL_ITER, true><<<grid, G::T, smem_iter, st>>>(a);
     else col_pass_kernel<N, COL_FFT, true><<<grid, G::T, G::SMEM_LINES, st>>>(a);
   } else {
-    if (a.mode != COL_ITER) return launch_pdl(col_pass_rk<N, COL_FFT, PROJ_MODABS>, grid, G::T, G::SMEM_LINES, st, a, pass_pdl<N>());
-    if (a.proj == PROJ_CCD) return launch_pdl(col_pass_rk<N, COL_ITER, PROJ_CCD>, grid, G::T, smem_iter, st, a, pass_pdl<N>());
-    return launch_pdl(col_pass_rk<N, COL_ITER, PROJ_MODABS>, grid, G::T, smem_iter, st, a, pass_pdl<N>());
+    if (a.mode != COL_ITER) return launch_pdl(col_pass_rk<N, COL_FFT, PROJ_MODABS>, grid, G::T, G::SMEM_LINES, st, a, pdl_of<N>(a.pdl_mode));
+    if (a.proj == PROJ_CCD) return launch_pdl(col_pass_rk<N, COL_ITER, PROJ_CCD>, grid, G::T, smem_iter, st, a, pdl_of<N>(a.pdl_mode));
+    return launch_pdl(col_pass_rk<N, COL_ITER, PROJ_MODABS>, grid, G::T, smem_iter, st, a, pdl_of<N>(a.pdl_mode));
   }
   return cudaGetLastError();
 }

@@ -63,6 +63,8 @@ struct RowArgs {
   float scale;             // factor applied on store (1 = none)
   float inv_n;             // 1/(rows*cols) (applyNorm after the inverse FFT)
   float beta;              // vars.beta_HIO
+  int cb_plus1;            // 0: default butterfly chunk bits; k + 1: chunk bits k (autotuner)
+  int pdl_mode;            // 0: the per-length default, 1: plain launch, 2: programmatic dependent launch
 };
 
 struct ColArgs {
@@ -87,6 +89,7 @@ struct ColArgs {
   float scale;
   float ccd_scale;         // vars.scale
   float ccd_rcolor;        // vars.rcolor
+  int pdl_mode;            // as RowArgs::pdl_mode
 };
 
 // Launch helpers exported by the per-size translation units.
@@ -99,6 +102,8 @@ RowLaunch row_launcher(int n);
 ColLaunch col_launcher(int n);
 int lines_per_cta(int n);          // lines (rows or columns) per CTA for length n
 int twiddle_count(int n);          // entries of the per-pass twiddle table of length n
+int row_cb_default(int n, int tile_log2);   // butterfly chunk bits the row pass uses on tiled data
+int row_cb_max(int n);                      // largest valid chunk bits of length n
 // host: fill the per-pass twiddle table of length n (double precision, rounded once)
 void twiddle_table(int n, float2* out);
 

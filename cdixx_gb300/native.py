@@ -38,6 +38,7 @@ class Params(ctypes.Structure):
         ("shrink_mode", ctypes.c_int), ("sigma0", ctypes.c_float), ("sigma_min", ctypes.c_float),
         ("sigma_decay", ctypes.c_float), ("use_graph", ctypes.c_int), ("rf_every", ctypes.c_int),
         ("stop_rfactor", ctypes.c_float), ("fft_mode", ctypes.c_int), ("prtf_iter", ctypes.c_int),
+        ("autotune", ctypes.c_int),
     ]
 
 
@@ -79,6 +80,7 @@ _SIGS = {
     "cdx_get_fourier": [_P, _I, _P, _I],
     "cdx_get_support": [_P, _I, _P, _I],
     "cdx_get_prtf": [_P, _I, _P, _I],
+    "cdx_get_tuning": [_P, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.c_char_p, _I],
     "cdx_phase_retrieve_host": [ctypes.POINTER(Params), ctypes.c_char_p, _P, _P, ctypes.c_ulonglong,
                                 _P, _P, _P, ctypes.POINTER(Stats)],
     "cdx_fft2": [_P, _P, _I, _I, _I, _I, _P],
@@ -235,6 +237,13 @@ class Context:
 
     def __exit__(self, *a):
         self.close()
+
+    def tuning(self):
+        """(pdl, row_chunk, report) of the launch variant in use (cdx_get_tuning)."""
+        pdl, chunk = ctypes.c_int(), ctypes.c_int()
+        buf = ctypes.create_string_buffer(1024)
+        check(lib().cdx_get_tuning(self._h, ctypes.byref(pdl), ctypes.byref(chunk), buf, 1024))
+        return pdl.value, chunk.value, buf.value.decode()
 
     def set_pattern(self, idx, intensity, layout=CDX_FFT_ORDER, scale=1.0):
         p, w, _k = _buf(intensity)

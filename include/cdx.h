@@ -69,6 +69,10 @@ typedef struct cdx_params {
   int fft_mode;              /* CDX_FFT_FP32 (default) or CDX_FFT_TC_BF16 */
   int prtf_iter;             /* prtfIter: from this step on (the step counter of phaseRetrieve, shrinkwraps
                                 included) accumulate the phase-retrieval transfer function; -1 = off (default) */
+  int autotune;              /* 1: before the first run of a size, time the launch variants of the iteration
+                                (programmatic dependent launch on/off x row-pass butterfly chunk width) on the
+                                context's own data and keep the fastest (cached per device, size and batch for
+                                the process); 0 (default): the per-length defaults */
 } cdx_params;
 
 /* FFT arithmetic.  CDX_FFT_TC_BF16: the radix-16 passes run as tensor-core
@@ -156,6 +160,11 @@ int cdx_get_support(cdx_ctx* ctx, int idx, float* out, int where);  /* support (
  * divided by the angular sum of the |P_M Psi| > 1e-6 mask at prtf_iter (the
  * prtf.txt column).  CDX_ERR_STATE when the run did not reach prtf_iter. */
 int cdx_get_prtf(cdx_ctx* ctx, int idx, float* out, int where);
+/* The launch variant the iteration uses (autotune): *pdl 1 = programmatic
+ * dependent launch, 0 = plain; *row_chunk = butterfly chunk bits of the row
+ * pass (-1: the default); `report` (may be NULL) receives the timings the
+ * autotuner measured, one "pdl=<0|1> chunk=<k>: <us> us" line per variant. */
+int cdx_get_tuning(cdx_ctx* ctx, int* pdl, int* row_chunk, char* report, int cap);
 
 /* ---------------------------------------------------------------- one call, host buffers */
 /* Whole path for one pattern with HOST buffers: create, set pattern, set

@@ -557,3 +557,30 @@ def test_one_step_every_geometry(cdx, shape, algo, beta):
         e_rho = rel_l2(ctx.get_object(0), ref.rho)
         e_psi = rel_l2(ctx.get_fourier(0), ref.psi)
     assert e_rho <= 1e-5 and e_psi <= 1e-5, (shape, algo, e_rho, e_psi)
+
+
+@pytest.mark.parametrize("n,batch", [(256, 4), (2048, 1)])
+def test_autotune_keeps_results_and_caches(cdx, n, batch):
+    """autotune = 1: the launch variants it times change neither the arithmetic
+    nor the state (the tuned run equals the default run bit for bit); the
+    choice is cached for the next context of the same size."""
+    I, psi0 = blob_case(n=n) if n <= 512 else (None, None)
+    if I is None:
+        rng = np.random.default_rng(2)
+        I = (rng.random((n, n)) * 100).astype(np.float32)
+        psi0 = (np.sqrt(I) * np.exp(2j * np.pi * rng.random((n, n)))).astype(np.complex64)
+    outs = []
+    for tune in (0, 1, 1):
+        p = cdx.default_params(n, n, batch=batch, oversampling_spt=4.0, beta=0.9, autotune=tune)
+        with cdx.Context(p) as ctx:
+            for b in range(batch):
+                ctx.set_pattern(b, I)
+                ctx.set_initial(b, psi0)
+            ctx.run("10*RAAR+1*shrinkWrap+5*HIO")
+            outs.append((ctx.get_object(batch - 1), ctx.tuning()))
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][0], outs[2][0])
+    pdl, chunk, report = outs[1][1]
+    print(f"{n}^2 x{batch}: pdl={pdl} chunk={chunk}\n{report}")
+    assert pdl in (0, 1) and chunk >= 0 and report.count("us") >= 2
+    assert outs[2][1][2] == "cached" and outs[2][1][:2] == (pdl, chunk)
+    assert outs[0][1][:2] == (-1, -1)
