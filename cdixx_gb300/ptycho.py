@@ -154,7 +154,7 @@ class Ptycho:
             raise ValueError(f"expected shape {(self.nscan, self.row, self.column)}, got {a.shape}")
         check(lib().cdx_pty_set_patterns(self._h, a.ctypes.data_as(ctypes.c_void_p)))
 
-    # --- the driver's steps ---------------------------------------------------
+    # --- the steps of the reference's ptycho program ---------------------------
     def initObject(self, seed=0):
         """Random-phase unit object and the propagated pupil disk as probe (util/ptycho.cpp:363-369)."""
         check(lib().cdx_pty_init_object(self._h, seed))

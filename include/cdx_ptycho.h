@@ -26,7 +26,7 @@ extern "C" {
 typedef struct cdx_pty cdx_pty;
 
 /* The fields ptycho::iterate reads (include/readConfig.hpp:25-35, where the
- * real-valued ones are double) and the sizes the driver derives. */
+ * real-valued ones are double) and the sizes the ptycho program derives. */
 typedef struct cdx_pty_params {
   int rows, cols;          /* probe and pattern size (row, column); 2^a 3^b in [16, 4096] */
   int obj_rows, obj_cols;  /* object size (row_O, column_O) */

@@ -296,7 +296,7 @@ def multiply_shift(wave, shiftx, shifty):
     return (wave * (np.cos(ph) + 1j * np.sin(ph)).astype(C64)).astype(C64)
 
 
-# --------------------------------------------------------------- the driver
+# ------------------------------------------------- ptycho::iterate and set-up
 @dataclass
 class PtyParams:
     """The config fields ``ptycho::iterate`` reads (include/readConfig.hpp:25-35; REALVAR are double)."""
