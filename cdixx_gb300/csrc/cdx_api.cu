@@ -123,6 +123,7 @@ struct cdx_ctx {
 
   // launch variant (autotune): RowArgs/ColArgs knobs, and what was measured
   int tune_pdl_mode = 0, tune_cb_plus1 = 0;
+  int* derr = nullptr;        // bulk-copy wait timeouts of the pass kernels (bit 0)
   bool tuned = false;
   std::string tune_report;
 
@@ -278,6 +279,7 @@ int col_iter(cdx_ctx* c, bool from_psi, bool rf, float2* psi_proj = nullptr) {
   a.ccd_scale = 1.f / c->p.exposure;
   a.ccd_rcolor = (float)c->p.rcolor;
   a.pdl_mode = c->tune_pdl_mode;
+  a.err = c->derr;
   CDX_CK(col_launcher(c->rows)(a, c->batch, c->st));
   return CDX_OK;
 }
@@ -304,6 +306,7 @@ int row_iter(cdx_ctx* c, int algo) {
   a.beta = c->p.beta;
   a.cb_plus1 = c->tune_cb_plus1;
   a.pdl_mode = c->tune_pdl_mode;
+  a.err = c->derr;
   CDX_CK(row_launcher(c->cols)(a, c->batch, c->st));
   return CDX_OK;
 }
@@ -778,6 +781,7 @@ int cdx_create(const cdx_params* p, void* stream, cdx_ctx** out) {
   const size_t o_part = off; off += al(sizeof(double) * B * c->part_per_pat);
   const size_t o_pmax = off; off += al(sizeof(float) * B * kSwBlocks);
   const size_t o_state = off; off += al(sizeof(PatState) * B);
+  const size_t o_err = off; off += al(sizeof(int));
   if (cudaMalloc(&c->arena, off) != cudaSuccess) {
     cudaGetLastError();
     return fail(set_error(CDX_ERR_NOMEM, "device arena of " + std::to_string(off) + " bytes"));
@@ -795,6 +799,7 @@ int cdx_create(const cdx_params* p, void* stream, cdx_ctx** out) {
   c->part = (double*)(a + o_part);
   c->pmax = (float*)(a + o_pmax);
   c->dstate = (PatState*)(a + o_state);
+  c->derr = (int*)(a + o_err);
   if (cudaMemsetAsync(c->arena, 0, off, c->st) != cudaSuccess)
     return fail(set_error(CDX_ERR_CUDA, "arena clear failed"));
   // vars.threshold starts at 0.5 (src/gpu/cdi.cu:21)
@@ -1019,10 +1024,23 @@ int cdx_group_destroy(cdx_group* g) {
   return CDX_OK;
 }
 
+// A pass kernel whose staging copy did not complete within its bounded wait
+// leaves bit 0 in the context's error word; reported (and cleared) here.
+int check_bulk(cdx_ctx* c) {
+  int h = 0;
+  CDX_CK(cudaMemcpy(&h, c->derr, sizeof(int), cudaMemcpyDeviceToHost));
+  if (h) {
+    CDX_CK(cudaMemset(c->derr, 0, sizeof(int)));
+    return set_error(CDX_ERR_CUDA, "a pass kernel's bulk staging copy timed out; the run's results are invalid");
+  }
+  return CDX_OK;
+}
+
 int cdx_run(cdx_ctx* c, const char* algorithm, cdx_stats* stats) {
   int e = run_impl(c, algorithm);
   if (e) return e;
   CDX_CK(cudaStreamSynchronize(c->st));
+  if ((e = check_bulk(c))) return e;
   return fill_stats(c, 0, stats);
 }
 

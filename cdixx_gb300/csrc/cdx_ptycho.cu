@@ -526,6 +526,7 @@ struct cdx_pty {
   PtyScal* scal = nullptr;
   double* part = nullptr;
   unsigned* cnt = nullptr;   // last-CTA tickets of the fused reductions (reset by their last CTA)
+  int* derr = nullptr;       // bulk staging timeouts of the column kernel (bit 0)
   int order_cap = 0, coef_cap = 0;
   bool have_scan = false, have_pats = false, have_obj = false, have_probe = false;
   cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};   // one sweep: object, probe, probe + noise projection
@@ -609,6 +610,7 @@ PtyArgs pass_args(cdx_pty* t, int k, bool probe_phase, bool noise_proj = false) 
   a.noise_level = t->p.noise_level;
   a.ccd_scale = (float)(1. / t->p.exposure);
   a.rcolor = kRcolor;
+  a.err = t->derr;
   return a;
 }
 
@@ -745,7 +747,7 @@ int cdx_pty_create(const cdx_pty_params* p, void* stream, cdx_pty** out) {
       (r = dalloc(&t->pupil, t->npx)) || (r = dalloc(&t->W, t->pat_stride)) ||
       (r = dalloc(&t->pats, t->pat_stride * p->nscan)) || (r = dalloc(&t->bs, t->pat_stride)) ||
       (r = dalloc(&t->win, p->nscan)) || (r = dalloc(&t->tpos, p->nscan)) || (r = dalloc(&t->iter, 1)) ||
-      (r = dalloc(&t->scal, 1)) || (r = dalloc(&t->part, 3 * kRedBlocks)) || (r = dalloc(&t->cnt, 4)))
+      (r = dalloc(&t->scal, 1)) || (r = dalloc(&t->part, 3 * kRedBlocks)) || (r = dalloc(&t->cnt, 4)) || (r = dalloc(&t->derr, 1)))
     return fail(r);
   e = cudaMemsetAsync(t->W, 0, sizeof(float2) * t->pat_stride, t->st);
   if (e == cudaSuccess) e = cudaMemsetAsync(t->pats, 0, sizeof(float) * t->pat_stride * p->nscan, t->st);
@@ -753,6 +755,7 @@ int cdx_pty_create(const cdx_pty_params* p, void* stream, cdx_pty** out) {
   if (e == cudaSuccess) e = cudaMemsetAsync(t->step, 0, sizeof(float2) * t->npx, t->st);
   if (e == cudaSuccess) e = cudaMemsetAsync(t->scal, 0, sizeof(PtyScal), t->st);
   if (e == cudaSuccess) e = cudaMemsetAsync(t->cnt, 0, sizeof(unsigned) * 4, t->st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(t->derr, 0, sizeof(int), t->st);
   if (e == cudaSuccess && p->use_bs) {
     k_pty_beamstop<<<grid1(t->npx), 256, 0, t->st>>>(t->bs, p->rows, p->cols, t->tl, (float)p->beam_stop_size);
     e = cudaGetLastError();
@@ -776,7 +779,7 @@ int cdx_pty_destroy(cdx_pty* t) {
   for (auto& g : t->graph)
     if (g) cudaGraphExecDestroy(g);
   void* bufs[] = {t->O, t->Op, t->P, t->step, t->W, t->tmp, t->pupil, t->pats, t->bs, t->msum, t->coef,
-                  t->win, t->tpos, t->order, t->iter, t->scal, t->part, t->cnt};
+                  t->win, t->tpos, t->order, t->iter, t->scal, t->part, t->cnt, t->derr};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (t->e0) cudaEventDestroy(t->e0);
@@ -990,6 +993,12 @@ int cdx_pty_iterate(cdx_pty* t, int first_iter, int n_iter, const int* orders, u
   PTY_CK(cudaEventRecord(t->e1, st));
   PTY_CK(cudaEventSynchronize(t->e1));
   PTY_CK(cudaEventElapsedTime(&t->last_ms, t->e0, t->e1));
+  int h = 0;
+  PTY_CK(cudaMemcpy(&h, t->derr, sizeof(int), cudaMemcpyDeviceToHost));
+  if (h) {
+    PTY_CK(cudaMemset(t->derr, 0, sizeof(int)));
+    return set_error(CDX_ERR_CUDA, "a column kernel's bulk staging copy timed out; the sweep results are invalid");
+  }
   return CDX_OK;
 }
 

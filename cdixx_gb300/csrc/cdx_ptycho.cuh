@@ -36,6 +36,7 @@ struct PtyArgs {
   int noise_level;         // noiseLevel
   float ccd_scale;         // vars.scale = 1/exposure
   float rcolor;            // vars.rcolor
+  int* err;                // bit 0: a bulk staging copy timed out
 };
 
 constexpr float kPtyAlpha = 0.1f;   // ALPHA, src/gpu/ptycho.cu:5
@@ -183,12 +184,25 @@ __global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_COL) pty_col_rk(Pty
   const int si = a.order[*a.iter * a.nscan + a.k];
   const float* pat = a.pats + si * a.pat_stride + tile;
   const bool has_bs = a.bs != nullptr;
+  // the pattern tile (and the beamstop tile): contiguous L*N floats, bulk copies
+  __shared__ uint64_t stage_bar;
+  if constexpr (bulk_staging<N>()) {
+    constexpr unsigned bytes = L * N * (unsigned)sizeof(float);
+    if (threadIdx.x == 0) bulk_bar_init(&stage_bar);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      bulk_expect(&stage_bar, bytes * (has_bs ? 2u : 1u));
+      bulk_g2s(int_s, pat, bytes, &stage_bar);
+      if (has_bs) bulk_g2s(bs_s, a.bs + tile, bytes, &stage_bar);
+    }
+  } else {
 #pragma unroll 4
-  for (int q = threadIdx.x; q < L * N / 4; q += T) {
-    cp_async16(int_s + 4 * q, pat + 4 * q, true);
-    if (has_bs) cp_async16(bs_s + 4 * q, a.bs + tile + 4 * q, true);
+    for (int q = threadIdx.x; q < L * N / 4; q += T) {
+      cp_async16(int_s + 4 * q, pat + 4 * q, true);
+      if (has_bs) cp_async16(bs_s + 4 * q, a.bs + tile + 4 * q, true);
+    }
+    cp_commit();
   }
-  cp_commit();
   float2 v0[F0::B][F0::R];
 #pragma unroll
   for (int b = 0; b < F0::B; ++b) {
@@ -199,7 +213,8 @@ __global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_COL) pty_col_rk(Pty
   }
   float2 v[FL::B][FL::R];
   rfft<N, 0, false>(v0, v, smem, a.tw, 0);
-  cp_wait<0>();
+  if constexpr (bulk_staging<N>()) bulk_wait(&stage_bar, a.err);
+  else cp_wait<0>();
   __syncthreads();
 #pragma unroll
   for (int b = 0; b < FL::B; ++b) {

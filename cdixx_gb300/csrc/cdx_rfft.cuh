@@ -237,16 +237,32 @@ __global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_COL) col_pass_rk(Co
   float* int_s = amp_s + L * N;
   float* bs_s = int_s + L * N;
   const long long aux = (long long)blockIdx.y * a.aux_stride + tile;
+  // the tile's sqrt(I) (and I, beamstop for PROJ_CCD): contiguous runs of L*N
+  // floats, one bulk copy each, landing during the forward transform
+  __shared__ uint64_t stage_bar;
   if constexpr (iter) {
-#pragma unroll 4
-    for (int q = threadIdx.x; q < L * N / 4; q += T) {
-      cp_async16(amp_s + 4 * q, a.amp + aux + 4 * q, true);
-      if constexpr (PROJ == PROJ_CCD) {
-        cp_async16(int_s + 4 * q, a.inten + aux + 4 * q, true);
-        if (a.bs) cp_async16(bs_s + 4 * q, a.bs + aux + 4 * q, true);
+    if constexpr (bulk_staging<N>()) {
+      constexpr unsigned bytes = L * N * (unsigned)sizeof(float);
+      if (threadIdx.x == 0) bulk_bar_init(&stage_bar);
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        const bool two = PROJ == PROJ_CCD, three = PROJ == PROJ_CCD && a.bs != nullptr;
+        bulk_expect(&stage_bar, bytes * (1u + (two ? 1u : 0u) + (three ? 1u : 0u)));
+        bulk_g2s(amp_s, a.amp + aux, bytes, &stage_bar);
+        if (two) bulk_g2s(int_s, a.inten + aux, bytes, &stage_bar);
+        if (three) bulk_g2s(bs_s, a.bs + aux, bytes, &stage_bar);
       }
+    } else {
+#pragma unroll 4
+      for (int q = threadIdx.x; q < L * N / 4; q += T) {
+        cp_async16(amp_s + 4 * q, a.amp + aux + 4 * q, true);
+        if constexpr (PROJ == PROJ_CCD) {
+          cp_async16(int_s + 4 * q, a.inten + aux + 4 * q, true);
+          if (a.bs) cp_async16(bs_s + 4 * q, a.bs + aux + 4 * q, true);
+        }
+      }
+      cp_commit();
     }
-    cp_commit();
   }
   const float2* in = a.in + (long long)blockIdx.y * a.in_stride;
   const bool in_t = a.in_tiled != 0;
@@ -296,7 +312,8 @@ __global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_COL) col_pass_rk(Co
     }
     return;
   } else {
-    cp_wait<0>();
+    if constexpr (bulk_staging<N>()) bulk_wait(&stage_bar, a.err);
+    else cp_wait<0>();
     __syncthreads();
     // Psi complete in registers: optional R-factor partial (one loop behind
     // one uniform branch), then the projection (branch-free per element, so
@@ -388,15 +405,26 @@ __device__ __forceinline__ void row_pass_body(const RowArgs& a) {
   float2* rho_s = smem + L * G::LD;
   uint32_t* mask_s = reinterpret_cast<uint32_t*>(rho_s + L * RS);
   float2* rho = a.rho + (long long)blockIdx.y * a.rho_stride + (long long)row0 * N;
+  // with an even line stride each rho row is one bulk copy (16-byte aligned)
+  constexpr bool bulk_rho = bulk_staging<N>() && RS % 2 == 0;
+  __shared__ uint64_t rho_bar;
+  if constexpr (iter && bulk_rho) {
+    if (threadIdx.x == 0) bulk_bar_init(&rho_bar);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      bulk_expect(&rho_bar, (unsigned)nrows * N * (unsigned)sizeof(float2));
+      for (int l = 0; l < nrows; ++l) bulk_g2s(rho_s + l * RS, rho + (long long)l * N, N * (unsigned)sizeof(float2), &rho_bar);
+    }
+  }
   if constexpr (iter) {
-    if constexpr (RS % 2 == 0) {
+    if constexpr (!bulk_rho && RS % 2 == 0) {
 #pragma unroll 4
       for (int e = threadIdx.x; e < L * N / 2; e += T) {
         const int l = (2 * e) / N, c = 2 * e - l * N;
         const bool ok = l < nrows;
         cp_async16(rho_s + l * RS + c, ok ? rho + 2 * e : rho, ok);
       }
-    } else {
+    } else if constexpr (!bulk_rho) {
 #pragma unroll 4
       for (int e = threadIdx.x; e < L * N; e += T) {
         const int l = e / N, c = e - l * N;
@@ -448,6 +476,7 @@ __device__ __forceinline__ void row_pass_body(const RowArgs& a) {
     }
   } else {
     cp_wait<0>();
+    if constexpr (bulk_rho) bulk_wait(&rho_bar, a.err);
     __syncthreads();
     // rho' = IFFT/N; update against rho and the support bits
 #pragma unroll

@@ -65,6 +65,7 @@ struct RowArgs {
   float beta;              // vars.beta_HIO
   int cb_plus1;            // 0: default butterfly chunk bits; k + 1: chunk bits k (autotuner)
   int pdl_mode;            // 0: the per-length default, 1: plain launch, 2: programmatic dependent launch
+  int* err;                // optional: bit 0 set when a bulk copy's wait ran out
 };
 
 struct ColArgs {
@@ -90,6 +91,7 @@ struct ColArgs {
   float ccd_scale;         // vars.scale
   float ccd_rcolor;        // vars.rcolor
   int pdl_mode;            // as RowArgs::pdl_mode
+  int* err;                // as RowArgs::err
 };
 
 // Launch helpers exported by the per-size translation units.
