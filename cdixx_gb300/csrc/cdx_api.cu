@@ -492,12 +492,20 @@ int autotune(cdx_ctx* c) {
     return CDX_OK;
   }
   const size_t nrho = (size_t)c->npx * c->batch, nw = (size_t)c->wstride * c->batch;
-  float2 *srho = nullptr, *sw = nullptr;
-  if (cudaMalloc(&srho, sizeof(float2) * nrho) != cudaSuccess || cudaMalloc(&sw, sizeof(float2) * nw) != cudaSuccess) {
+  // copies of the state the timed iterations overwrite, freed on every path
+  struct Scratch {
+    float2 *rho = nullptr, *w = nullptr;
+    ~Scratch() {
+      if (rho) cudaFree(rho);
+      if (w) cudaFree(w);
+    }
+  } save;
+  if (cudaMalloc(&save.rho, sizeof(float2) * nrho) != cudaSuccess || cudaMalloc(&save.w, sizeof(float2) * nw) != cudaSuccess) {
     cudaGetLastError();
-    if (srho) cudaFree(srho);
     return set_error(CDX_ERR_NOMEM, "autotune: no room for a copy of the state");
   }
+  float2* const srho = save.rho;
+  float2* const sw = save.w;
   CDX_CK(cudaMemcpyAsync(srho, c->rho, sizeof(float2) * nrho, cudaMemcpyDeviceToDevice, c->st));
   CDX_CK(cudaMemcpyAsync(sw, c->work, sizeof(float2) * nw, cudaMemcpyDeviceToDevice, c->st));
   const int cbd = row_cb_default(c->cols, c->tl);
@@ -547,8 +555,6 @@ int autotune(cdx_ctx* c) {
     CDX_CK(cudaMemcpyAsync(c->work, sw, sizeof(float2) * nw, cudaMemcpyDeviceToDevice, c->st));
     CDX_CK(cudaStreamSynchronize(c->st));
   }
-  cudaFree(srho);
-  cudaFree(sw);
   if (e != CDX_OK) return e;
   c->tune_pdl_mode = best_pdl;
   c->tune_cb_plus1 = best_cb;
