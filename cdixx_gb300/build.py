@@ -88,6 +88,15 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("cdi_run link failed:\n" + r.stdout + r.stderr)
+    # the config-driven ptychography program (the reference's util/ptycho.cpp main)
+    pty_src = CSRC / "ptycho_run.cc"
+    PTY = LIBDIR / "ptycho_run"
+    if not PTY.exists() or PTY.stat().st_mtime < max(LIB.stat().st_mtime, pty_src.stat().st_mtime, hdr):
+        cmd = ["g++", "-std=c++17", "-O2", *inc, str(pty_src), "-o", str(PTY), f"-L{LIBDIR}", "-lcdx",
+               "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("ptycho_run link failed:\n" + r.stdout + r.stderr)
     if verbose:
         print(f"built {LIB}")
     return LIB

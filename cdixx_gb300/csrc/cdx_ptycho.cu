@@ -876,6 +876,15 @@ int cdx_pty_get_pupil(cdx_pty* t, float* pupil) {
   return copy_c(t, pupil, t->pupil, t->npx, cudaMemcpyDeviceToHost);
 }
 
+int cdx_pty_set_pupil(cdx_pty* t, const float* pupil) {
+  if (!t || !pupil) return set_error(CDX_ERR_ARG, "null argument");
+  PTY_RET(copy_c(t, t->P, pupil, t->npx, cudaMemcpyHostToDevice));
+  PTY_RET(angular_spectrum(t, t->P, false));
+  PTY_CK(cudaStreamSynchronize(t->st));
+  t->have_probe = true;
+  return CDX_OK;
+}
+
 int cdx_pty_init_object(cdx_pty* t, unsigned long long seed) {
   if (!t) return set_error(CDX_ERR_ARG, "null argument");
   k_pty_random<<<grid1(t->onpx), 256, 0, t->st>>>(t->O, t->onpx, seed);

@@ -124,6 +124,7 @@ _SIGS = {
     "cdx_pty_set_probe": [_P, _P],
     "cdx_pty_get_probe": [_P, _P],
     "cdx_pty_get_pupil": [_P, _P],
+    "cdx_pty_set_pupil": [_P, _P],
     "cdx_pty_init_object": [_P, ctypes.c_ulonglong],
     "cdx_pty_simulate": [_P],
     "cdx_pty_iterate": [_P, _I, _I, _P, ctypes.c_uint],

@@ -141,6 +141,12 @@ class Ptycho:
         check(lib().cdx_pty_get_pupil(self._h, out.ctypes.data_as(ctypes.c_void_p)))
         return out
 
+    @pupil.setter
+    def pupil(self, field):
+        """Set the probe to the pupil-plane field propagated by dpupil (readPupilAndObject)."""
+        a = _c64(field, (self.row, self.column))
+        check(lib().cdx_pty_set_pupil(self._h, a.ctypes.data_as(ctypes.c_void_p)))
+
     @property
     def patterns(self) -> np.ndarray:
         out = np.empty((self.nscan, self.row, self.column), np.float32)

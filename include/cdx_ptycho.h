@@ -70,6 +70,10 @@ int cdx_pty_get_probe(cdx_pty* t, float* probe);
 /* The probe back-propagated to the pupil plane, which is what the reference
  * leaves in pupilpatternWave after iterate() (util/ptycho.cpp:705). */
 int cdx_pty_get_pupil(cdx_pty* t, float* pupil);
+/* The probe from a pupil-plane field: probe = angularSpectrumPropagate(pupil)
+ * by dpupil (what readPupilAndObject does with the pupil image,
+ * util/ptycho.cpp:275-287). */
+int cdx_pty_set_pupil(cdx_pty* t, const float* pupil);
 
 /* initObject (util/ptycho.cpp:363-369): the object set to unit modulus with a
  * uniform random phase (a counter-based generator keyed by seed and pixel,

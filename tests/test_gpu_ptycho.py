@@ -143,3 +143,74 @@ def test_argument_checks(PT, cdx):
     assert e.value.code == cdx.CDX_ERR_SIZE
     with pytest.raises(cdx.CdxError):
         PT.Ptycho(32, 32, 64, 64, c["scanx"], c["scany"], lam=0.5, d=2e4, dpupil=1e3, pixelsize=20, pupil_size=40)
+
+
+def test_ptycho_run_program(PT, cdx, tmp_path):
+    """ptycho_run, the config-driven program: a simulation run (object and pupil
+    images, triangle scan, noise-free patterns written as .bin, 30 sweeps) equals
+    the same calls made through the library, and a second run reads the
+    patterns and scan.txt it wrote (readPattern / readScan)."""
+    import subprocess
+    from pathlib import Path
+    from oracle.cdi_oracle import read_bin, write_bin
+    lib = Path(__file__).resolve().parents[1] / "cdixx_gb300" / "_lib"
+    R, RO, step = 32, 64, 12.0
+    rng = np.random.default_rng(5)
+    x = np.linspace(-1, 1, RO)[:, None]
+    y = np.linspace(-1, 1, RO)[None, :]
+    inten = ((0.6 + 0.4 * np.cos(3 * x) * np.sin(2 * y)) ** 2).astype(np.float32)
+    phase = (0.5 + 0.2 * np.sin(2 * x + y)).astype(np.float32)
+    pupil_i = PO.pupil_func(R, R, 16).real.astype(np.float32)
+    write_bin(tmp_path / "obj_i.bin", inten)
+    write_bin(tmp_path / "obj_p.bin", phase)
+    write_bin(tmp_path / "pupil_i.bin", pupil_i)
+    optics = "lambda = 0.5;\n  d = 2e4;\n  dpupil = 1e3;\n  pixelsize = 20.;\n  pupilSize = 16.;\n  exposure = 1.;"
+    (tmp_path / "sim.cfg").write_text(f"""
+InputImages = {{ default = {{ Intensity = "obj_i.bin"; Phase = "obj_p.bin"; Pattern = "pat"; }};
+                 pupil = {{ Intensity = "pupil_i.bin"; }}; }};
+Job = {{
+  {optics}
+  stepSize = {step};
+  nIter = 30;
+  seed = 3;
+  runSim = True;
+  doIteration = True;
+  outputDir = "./";
+}};
+""")
+    r = subprocess.run([str(lib / "ptycho_run"), "sim.cfg"], cwd=tmp_path, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    obj_prog = read_bin(tmp_path / "ptycho_object.bin")
+    assert obj_prog.shape == (RO, RO) and np.isfinite(obj_prog).all()
+    # the same through the library
+    sx, sy = PT.scan_triangle(RO, RO, R, R, step)
+    truth = (np.sqrt(inten) * np.exp(1j * ((phase.astype(np.float64) - 0.5) * 2 * np.pi))).astype(np.complex64)
+    with PT.Ptycho(R, R, RO, RO, sx, sy, lam=0.5, d=2e4, dpupil=1e3, pixelsize=20.0, pupil_size=16.0) as t:
+        t.objectWave = truth
+        t.pupil = np.sqrt(pupil_i).astype(np.complex64)
+        t.createPattern()
+        pats = t.patterns
+        t.initObject(seed=3)
+        t.iterate(30, seed=1)
+        obj_lib = t.objectWave
+    # the program builds the true object in float (cosf/sinf of a float phase), the test in
+    # double: patterns 5e-8 apart, 1.2e-5 after 30 sweeps with momentum (6.6e-8 after one)
+    assert PO.rel_err(obj_prog, obj_lib) < 1e-4
+    saved = read_bin(tmp_path / "pat0.bin")            # centred, times the exposure
+    assert PO.rel_err(np.fft.ifftshift(saved), pats[0]) < 1e-6
+    # readPattern / readScan mode on what the first run wrote
+    (tmp_path / "rec.cfg").write_text(f"""
+InputImages = {{ default = {{ Pattern = "pat"; }}; }};
+Job = {{
+  {optics}
+  nIter = 5;
+  doIteration = True;
+  distFile = "scan.txt";
+  outputDir = "./";
+}};
+""")
+    r = subprocess.run([str(lib / "ptycho_run"), "rec.cfg"], cwd=tmp_path, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "Object image dimension" in r.stdout
+    obj2 = read_bin(tmp_path / "ptycho_object.bin")
+    assert np.isfinite(obj2).all() and obj2.shape[0] % 4 == 0
