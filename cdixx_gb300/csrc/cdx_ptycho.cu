@@ -13,6 +13,7 @@
 // counter that the graph's last node advances.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -374,6 +375,70 @@ __global__ void k_pty_conj_phase(float2* __restrict__ O, long long n, const PtyS
 }
 __global__ void k_pty_next(int* iter) { *iter += 1; }
 
+// FISTA_step (src/post_gpu/FISTA.cc:109-135) of the object, one TV proximal step,
+// fused: o = b * s (s = 0.125/lambda), forward differences p (rows) and q
+// (columns) of o, each component of (p, q) scaled to modulus <= 1 (diffMax),
+// lpq = p + q - p(x-1) - q(y-1) (calcLpq, no wrap), out = b - lambda lpq
+// (src/gpu/cudaConfig.cu:1124-1188).
+__device__ __forceinline__ void pty_tv_pq(const float2* __restrict__ b, int rows, int cols, int x, int y, float s,
+                                          float2& p, float2& q) {
+  const long long i = (long long)x * cols + y;
+  const float2 o = make_float2(b[i].x * s, b[i].y * s);
+  p = o;
+  q = o;
+  if (x != rows - 1) {
+    const float2 d = b[i + cols];
+    p = make_float2(o.x - d.x * s, o.y - d.y * s);
+  }
+  if (y != cols - 1) {
+    const float2 d = b[i + 1];
+    q = make_float2(o.x - d.x * s, o.y - d.y * s);
+  }
+  float m = hypotf(p.x, q.x);
+  if (m > 1) { p.x /= m; q.x /= m; }
+  m = hypotf(p.y, q.y);
+  if (m > 1) { p.y /= m; q.y /= m; }
+}
+__global__ void k_pty_fista(const float2* __restrict__ b, float2* __restrict__ out, int rows, int cols, float s,
+                            float lam) {
+  const long long n = (long long)rows * cols;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(i / cols), y = (int)(i % cols);
+    float2 p, q, l;
+    pty_tv_pq(b, rows, cols, x, y, s, p, q);
+    l = make_float2(p.x + q.x, p.y + q.y);
+    if (x >= 1) {
+      float2 pm, qm;
+      pty_tv_pq(b, rows, cols, x - 1, y, s, pm, qm);
+      l.x -= pm.x;
+      l.y -= pm.y;
+    }
+    if (y >= 1) {
+      float2 pn, qn;
+      pty_tv_pq(b, rows, cols, x, y - 1, s, pn, qn);
+      l.x -= qn.x;
+      l.y -= qn.y;
+    }
+    const float2 v = b[i];
+    out[i] = make_float2(v.x + l.x * -lam, v.y + l.y * -lam);
+  }
+}
+
+// the probe's momentum step on the Zernike sweeps (util/ptycho.cpp:682-686):
+// P_prev <- P - P_prev, then P_prev <- P + c P_prev, and the two swap
+__global__ void k_pty_probe_momentum(float2* __restrict__ P, float2* __restrict__ Pp, long long n, const float* coefz,
+                                     const int* iter) {
+  const float c = coefz[*iter];
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float2 p = P[i], q = Pp[i];
+    float2 d;
+    d.x = p.x + q.x * -1.f;
+    d.y = p.y + q.y * -1.f;
+    P[i] = make_float2(p.x + d.x * c, p.y + d.y * c);
+    Pp[i] = p;
+  }
+}
+
 // Overlap mask (util/ptycho.cpp:470-479): the disk createCircleMask(row>>1, column>>1,
 // pupilSize/2) added at every truncated scan position (addWindow), then bitMap(> 0.5).
 // The sums are small integers, so the atomic order does not matter.
@@ -529,7 +594,11 @@ struct cdx_pty {
   int* derr = nullptr;       // bulk staging timeouts of the column kernel (bit 0)
   int order_cap = 0, coef_cap = 0;
   bool have_scan = false, have_pats = false, have_obj = false, have_probe = false;
-  cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};   // one sweep: object, probe, probe + noise projection
+  // one sweep per kind: phase (object, probe, probe + noise projection) x FISTA x probe momentum
+  cudaGraphExec_t graph[12] = {};
+  float2* Pp = nullptr;       // probe momentum history (Zernike sweeps)
+  float2* fista = nullptr;    // FISTA output before it replaces the object
+  float* coefz = nullptr;     // probe momentum coefficients per sweep
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   float last_ms = 0.f;
   float lam = 0, dist = 0, res = 0;   // propagate_pupil members (float)
@@ -615,7 +684,7 @@ PtyArgs pass_args(cdx_pty* t, int k, bool probe_phase, bool noise_proj = false) 
 }
 
 // One sweep of ptycho::iterate (util/ptycho.cpp:484-690) for the iteration the device counter names.
-int enqueue_sweep(cdx_pty* t, bool probe_phase, bool noise_proj) {
+int enqueue_sweep(cdx_pty* t, bool probe_phase, bool noise_proj, bool fista, bool probe_momentum) {
   cudaStream_t st = t->st;
   const long long n = t->npx, on = t->onpx;
   PTY_CK(cudaMemsetAsync(t->scal->maxb, 0, sizeof(t->scal->maxb), st));
@@ -646,24 +715,38 @@ int enqueue_sweep(cdx_pty* t, bool probe_phase, bool noise_proj) {
     k_pty_far_part<<<kRedBlocks, 256, 0, st>>>(t->tmp, t->p.rows, t->p.cols, t->part, t->scal, t->cnt + 2);
     k_pty_mshift<<<grid1(n), 256, 0, st>>>(t->P, t->p.rows, t->p.cols, t->scal);
   }
+  if (fista) {   // util/ptycho.cpp:665-667: FISTA_step(objectWave, objectWave, 1e-2)
+    const float lam = 1e-2f;
+    k_pty_fista<<<grid1(on), 256, 0, st>>>(t->O, t->fista, t->p.obj_rows, t->p.obj_cols,
+                                            (float)(0.125 / (double)lam), lam);
+    PTY_CK(cudaMemcpyAsync(t->O, t->fista, sizeof(float2) * on, cudaMemcpyDeviceToDevice, st));
+  }
   if (t->p.mpie) {
     k_pty_csum<<<kRedBlocks, 256, 0, st>>>(t->O, t->msum, on, t->part, t->scal, t->cnt + 3, 0);
     k_pty_momentum<<<grid1(on), 256, 0, st>>>(t->O, t->Op, on, t->scal, t->coef, t->iter);
+    if (probe_momentum) k_pty_probe_momentum<<<grid1(n), 256, 0, st>>>(t->P, t->Pp, n, t->coefz, t->iter);
   }
   k_pty_next<<<1, 1, 0, st>>>(t->iter);
   PTY_CK(cudaGetLastError());
   return CDX_OK;
 }
 
-// sweep kind of iteration `it`: 0 object phase, 1 probe phase, 2 probe phase with applyMod
-int sweep_kind(int it) { return it < kUpdateProbeIter ? 0 : (it < kNoiseProjIter ? 1 : 2); }
+// sweep kind of iteration `it`: phase 0 object, 1 probe, 2 probe with applyMod; + 3 with the
+// FISTA object step (it < zernikeIter); + 6 with the probe momentum (a Zernike sweep with mPIE)
+int sweep_kind(const cdx_pty* t, int it) {
+  const int phase = it < kUpdateProbeIter ? 0 : (it < kNoiseProjIter ? 1 : 2);
+  const bool fista = it < t->p.zernike_iter;
+  const bool pmom = fista && t->p.mpie && it % 10 == 0;
+  return phase + (fista ? 3 : 0) + (pmom ? 6 : 0);
+}
 
 int ensure_graph(cdx_pty* t, int kind) {
   cudaGraphExec_t& g = t->graph[kind];
   if (g) return CDX_OK;
   cudaGraph_t graph = nullptr;
   PTY_CK(cudaStreamBeginCapture(t->st, cudaStreamCaptureModeThreadLocal));
-  const int r = enqueue_sweep(t, kind >= 1, kind == 2);
+  const int phase = kind % 3;
+  const int r = enqueue_sweep(t, phase >= 1, phase == 2, (kind / 3) % 2 == 1, kind >= 6);
   const cudaError_t e = cudaStreamEndCapture(t->st, &graph);
   if (r != CDX_OK) {
     if (graph) cudaGraphDestroy(graph);
@@ -709,8 +792,8 @@ int cdx_pty_create(const cdx_pty_params* p, void* stream, cdx_pty** out) {
   if (!p || !out) return set_error(CDX_ERR_ARG, "null argument");
   *out = nullptr;
   if (p->nscan < 1 || p->obj_rows < 1 || p->obj_cols < 1) return set_error(CDX_ERR_ARG, "bad scan count or object size");
-  if (p->noise_level < 0 || !(p->position_uncertainty >= 0))
-    return set_error(CDX_ERR_ARG, "noise_level and position_uncertainty must be >= 0");
+  if (p->noise_level < 0 || !(p->position_uncertainty >= 0) || p->zernike_iter < 0)
+    return set_error(CDX_ERR_ARG, "noise_level, position_uncertainty and zernike_iter must be >= 0");
   if (!(p->lambda > 0) || !(p->pixelsize > 0) || !(p->d > 0) || !(p->exposure > 0))
     return set_error(CDX_ERR_ARG, "lambda, d, pixelsize and exposure must be positive");
   const int pd = (int)p->pupil_size;
@@ -747,7 +830,8 @@ int cdx_pty_create(const cdx_pty_params* p, void* stream, cdx_pty** out) {
       (r = dalloc(&t->pupil, t->npx)) || (r = dalloc(&t->W, t->pat_stride)) ||
       (r = dalloc(&t->pats, t->pat_stride * p->nscan)) || (r = dalloc(&t->bs, t->pat_stride)) ||
       (r = dalloc(&t->win, p->nscan)) || (r = dalloc(&t->tpos, p->nscan)) || (r = dalloc(&t->iter, 1)) ||
-      (r = dalloc(&t->scal, 1)) || (r = dalloc(&t->part, 3 * kRedBlocks)) || (r = dalloc(&t->cnt, 4)) || (r = dalloc(&t->derr, 1)))
+      (r = dalloc(&t->scal, 1)) || (r = dalloc(&t->part, 3 * kRedBlocks)) || (r = dalloc(&t->cnt, 4)) || (r = dalloc(&t->derr, 1)) || (r = dalloc(&t->Pp, t->npx)) ||
+      (r = dalloc(&t->fista, p->zernike_iter > 0 ? t->onpx : 1)))
     return fail(r);
   e = cudaMemsetAsync(t->W, 0, sizeof(float2) * t->pat_stride, t->st);
   if (e == cudaSuccess) e = cudaMemsetAsync(t->pats, 0, sizeof(float) * t->pat_stride * p->nscan, t->st);
@@ -779,7 +863,8 @@ int cdx_pty_destroy(cdx_pty* t) {
   for (auto& g : t->graph)
     if (g) cudaGraphExecDestroy(g);
   void* bufs[] = {t->O, t->Op, t->P, t->step, t->W, t->tmp, t->pupil, t->pats, t->bs, t->msum, t->coef,
-                  t->win, t->tpos, t->order, t->iter, t->scal, t->part, t->cnt, t->derr};
+                  t->win, t->tpos, t->order, t->iter, t->scal, t->part, t->cnt, t->derr, t->Pp, t->fista,
+                  t->coefz};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (t->e0) cudaEventDestroy(t->e0);
@@ -945,6 +1030,10 @@ int cdx_pty_iterate(cdx_pty* t, int first_iter, int n_iter, const int* orders, u
                                   "which is not built: first_iter + n_iter must be <= 500");
   if (!t->have_scan || !t->have_pats || !t->have_obj || !t->have_probe)
     return set_error(CDX_ERR_STATE, "scan positions, patterns, object and probe must be set first");
+  for (int it = std::max(first_iter, kUpdateProbeIter); it < first_iter + n_iter && it < t->p.zernike_iter; ++it)
+    if (it % 10 == 0)
+      return set_error(CDX_ERR_ARG, "from iteration 400 zernikeIter enables the Zernike pupil fit, which is not built "
+                                    "(zernike_iter must be <= 400 or the run must end before the fit)");
   const int ns = t->p.nscan;
   std::vector<int> ord((size_t)std::max(1, n_iter) * ns);
   if (orders) {
@@ -955,11 +1044,12 @@ int cdx_pty_iterate(cdx_pty* t, int first_iter, int n_iter, const int* orders, u
     scan_orders_host(ns, n_iter, seed, ord.data());
   }
   // momentum coefficients (tk - 1)/tk+1 in the reference's float/double mix (util/ptycho.cpp:478, 677-680)
-  std::vector<float> coef(std::max(1, n_iter));
+  std::vector<float> coef(std::max(1, n_iter)), coefz(std::max(1, n_iter));
   float tk = (float)(0.5 + std::sqrt(1.25));
   for (int i = 0; i < n_iter; ++i) {
     const float tkp1 = (float)(0.5 + std::sqrt(0.25 + (double)(tk * tk)));
     coef[i] = (tk - 1) / tkp1;
+    coefz[i] = (float)((double)coef[i] * 0.8);   // (tk-1)/tkp1*0.8 (util/ptycho.cpp:684)
     tk = tkp1;
   }
   if (t->order_cap < (int)ord.size()) {
@@ -973,9 +1063,11 @@ int cdx_pty_iterate(cdx_pty* t, int first_iter, int n_iter, const int* orders, u
   }
   if (t->coef_cap < (int)coef.size()) {
     if (t->coef) cudaFree(t->coef);
-    t->coef = nullptr;
+    if (t->coefz) cudaFree(t->coefz);
+    t->coef = t->coefz = nullptr;
     t->coef_cap = 0;
     PTY_RET(dalloc(&t->coef, coef.size()));
+    PTY_RET(dalloc(&t->coefz, coef.size()));
     t->coef_cap = (int)coef.size();
     for (auto& g : t->graph)
       if (g) { cudaGraphExecDestroy(g); g = nullptr; }
@@ -983,18 +1075,21 @@ int cdx_pty_iterate(cdx_pty* t, int first_iter, int n_iter, const int* orders, u
   cudaStream_t st = t->st;
   PTY_CK(cudaMemcpyAsync(t->order, ord.data(), sizeof(int) * ord.size(), cudaMemcpyHostToDevice, st));
   PTY_CK(cudaMemcpyAsync(t->coef, coef.data(), sizeof(float) * coef.size(), cudaMemcpyHostToDevice, st));
+  PTY_CK(cudaMemcpyAsync(t->coefz, coefz.data(), sizeof(float) * coefz.size(), cudaMemcpyHostToDevice, st));
   // per-call state of iterate(): zero history and probe step, the overlap mask
   PTY_CK(cudaMemsetAsync(t->Op, 0, sizeof(float2) * t->onpx, st));
   PTY_CK(cudaMemsetAsync(t->step, 0, sizeof(float2) * t->npx, st));
+  PTY_CK(cudaMemsetAsync(t->Pp, 0, sizeof(float2) * t->npx, st));
   PTY_CK(cudaMemsetAsync(t->msum, 0, sizeof(float) * t->onpx, st));
   PTY_CK(cudaMemsetAsync(t->iter, 0, sizeof(int), st));
   k_pty_masksum<<<grid1(t->npx * ns), 256, 0, st>>>(t->msum, t->tpos, ns, t->p.rows, t->p.cols, t->p.obj_rows,
                                                      t->p.obj_cols, (float)(t->p.pupil_size / 2));
   k_pty_bitmap<<<grid1(t->onpx), 256, 0, st>>>(t->msum, t->onpx);
   PTY_CK(cudaGetLastError());
-  for (int it = first_iter; it < first_iter + n_iter; ++it) PTY_RET(ensure_graph(t, sweep_kind(it)));
+  for (int it = first_iter; it < first_iter + n_iter; ++it) PTY_RET(ensure_graph(t, sweep_kind(t, it)));
   PTY_CK(cudaEventRecord(t->e0, st));
-  for (int it = first_iter; it < first_iter + n_iter; ++it) PTY_CK(cudaGraphLaunch(t->graph[sweep_kind(it)], st));
+  for (int it = first_iter; it < first_iter + n_iter; ++it)
+    PTY_CK(cudaGraphLaunch(t->graph[sweep_kind(t, it)], st));
   // final global phase of the object (util/ptycho.cpp:731-735)
   k_pty_csum<<<kRedBlocks, 256, 0, st>>>(t->O, nullptr, t->onpx, t->part, t->scal, t->cnt + 3, 1);
   k_pty_conj_phase<<<grid1(t->onpx), 256, 0, st>>>(t->O, t->onpx, t->scal);

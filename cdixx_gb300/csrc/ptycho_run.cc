@@ -117,8 +117,8 @@ int main(int argc, char** argv) {
   }
   readConfig cfg(argv[1]);
   const std::string out = cfg.outputDir ? cfg.outputDir : "./";
-  if (cfg.isFresnel || cfg.zernikeIter > 0) {
-    fprintf(stderr, "Fresnel exit waves and the Zernike/FISTA pupil steps (zernikeIter > 0) are not built\n");
+  if (cfg.isFresnel) {
+    fprintf(stderr, "Fresnel exit waves (isFresnel) are not built\n");
     return 1;
   }
   cdx_pty_params p;
@@ -134,6 +134,7 @@ int main(int argc, char** argv) {
   p.beam_stop_size = cfg.beamStopSize;
   p.noise_level = cfg.noiseLevel;
   p.position_uncertainty = cfg.positionUncertainty;
+  p.zernike_iter = cfg.zernikeIter;
   std::vector<float> sx, sy, obj_truth, pupil, pats;
   if (cfg.runSim) {
     if (!cfg.common.Intensity || !cfg.pupil.Intensity) die("runSim needs InputImages.default.Intensity and .pupil.Intensity");

@@ -42,6 +42,9 @@ typedef struct cdx_pty_params {
   int beam_stop_size;
   int noise_level;         /* noiseLevel: tolerance of the modulus projection from iteration 2000 */
   double position_uncertainty; /* positionUncertainty: > 0 asks for scan-position refinement (not built) */
+  int zernike_iter;        /* zernikeIter: before it the object takes a FISTA (TV) step each sweep and,
+                              every tenth sweep, the probe a momentum step; the Zernike pupil fit it also
+                              enables from iteration 400 is not built (such runs are refused) */
 } cdx_pty_params;
 
 /* Defaults of readConfig (include/readConfig.hpp): mPIE 1, pupilSize 500,

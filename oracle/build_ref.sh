@@ -27,13 +27,15 @@ g++ -o "$OUT/ref_harness" "$OUT"/obj/*.o
 echo "built $OUT/ref_harness"
 
 # Ptychography pin: the reference's ptycho driver (util/ptycho.cpp, compiled
-# into pty_harness.cc), its kernels (src/gpu/ptycho.cu), the propagator and
-# the misc helpers (findMiddle, createCircleMask, shiftWave) it calls.
+# into pty_harness.cc), its kernels (src/gpu/ptycho.cu), the propagator, the
+# FISTA object step and the misc helpers (findMiddle, createCircleMask,
+# shiftWave) it calls.
 PO="$OUT/obj_pty"
 mkdir -p "$PO"
 sed "$LAUNCH" "$REF/src/gpu/ptycho.cu" | $CXX -x c++ - -I"$REF/src/gpu" -c -o "$PO/ptycho.cu.o"
 $CXX -c "$REF/src/post_gpu/propagator.cc" -o "$PO/propagator.cc.o"
-$CXX -DCDXREF_WITH_PROPAGATOR -DCDXREF_WITH_MISC -DCDXREF_WITH_PTYCHO_KERNELS -c "$SHIM/cdxref_stubs.cc" -o "$PO/cdxref_stubs.o"
+$CXX -c "$REF/src/post_gpu/FISTA.cc" -o "$PO/FISTA.cc.o"
+$CXX -DCDXREF_WITH_PROPAGATOR -DCDXREF_WITH_MISC -DCDXREF_WITH_PTYCHO_KERNELS -DCDXREF_WITH_FISTA -c "$SHIM/cdxref_stubs.cc" -o "$PO/cdxref_stubs.o"
 $CXX -c "$SHIM/pty_stubs.cc" -o "$PO/pty_stubs.o"
 $CXX -include "$SHIM/cdxref_ptycho.h" -DCDXREF_PTYCHO_CPP="\"$REF/util/ptycho.cpp\"" -c "$SHIM/pty_harness.cc" \
   -o "$PO/pty_harness.o"

@@ -271,6 +271,39 @@ def angular_spectrum(field, lam, distance, pixelsize, reverse=False):
     return ifft2_u(out)
 
 
+def fista_step(b, lam=0.01):
+    """FISTA_step (src/post_gpu/FISTA.cc:109-135) of the complex object, one TV
+    proximal step: o = b * (0.125 / lambda); p, q = forward differences of o along
+    x and y (partialx / partialy, src/gpu/cudaConfig.cu:1124-1150: the last row /
+    column keeps o itself); each component of (p, q) scaled to modulus <= 1
+    (diffMax, 1158-1170); lpq = p + q - p(x-1) - q(y-1) (no wrap, calcLpq
+    1180-1188); result b - lambda lpq, all in float."""
+    lam = F32(lam)
+    s = F32(0.125 / np.float64(lam))
+    o = (b.astype(C64) * s).astype(C64)
+    ore, oim = o.real.astype(F32), o.imag.astype(F32)
+
+    def parts(a):
+        p = a.copy()
+        p[:-1, :] = (a[:-1, :] - a[1:, :]).astype(F32)
+        q = a.copy()
+        q[:, :-1] = (a[:, :-1] - a[:, 1:]).astype(F32)
+        mod = np.hypot(p, q).astype(F32)
+        big = mod > F32(1)
+        safe = np.where(big, mod, F32(1))
+        p = np.where(big, (p / safe).astype(F32), p)
+        q = np.where(big, (q / safe).astype(F32), q)
+        lpq = (p + q).astype(F32)
+        lpq[1:, :] = (lpq[1:, :] - p[:-1, :]).astype(F32)
+        lpq[:, 1:] = (lpq[:, 1:] - q[:, :-1]).astype(F32)
+        return lpq
+
+    lr, li = parts(ore), parts(oim)
+    out_r = (b.real.astype(F32) + (lr * -lam).astype(F32)).astype(F32)
+    out_i = (b.imag.astype(F32) + (li * -lam).astype(F32)).astype(F32)
+    return (out_r + 1j * out_i).astype(C64)
+
+
 def find_middle(m):
     """findMiddle of a float field (src/post_gpu/misc.cc:27-42) with multiplyx/multiplyy
     (src/gpu/cudaConfig.cu:1427-1437): centroid in units of the size, coordinate
@@ -311,6 +344,7 @@ class PtyParams:
     beam_stop_size: int = 5
     noise_level: int = 0
     position_uncertainty: float = 0.0
+    zernike_iter: int = 0
 
     def resolution(self, rows):
         """resolution = lambda d / pixelsize / row (util/ptycho.cpp:246), stored as float."""
@@ -348,9 +382,13 @@ def iterate(obj0, probe0, patterns, scanx, scany, n_iter, params: PtyParams, ord
     orow, ocol = obj0.shape
     if start_iter + n_iter > POSITION_UPDATE_ITER and params.position_uncertainty > 0:
         raise ValueError("position refinement (iterations >= 500, positionUncertainty > 0) is outside this restatement")
+    for it in range(start_iter, start_iter + n_iter):
+        if it >= UPDATE_PROBE_ITER and it < params.zernike_iter and it % 10 == 0:
+            raise ValueError("the Zernike pupil fit (zernikeIter > 400) is outside this restatement")
     O = obj0.astype(C64).copy()
     Oprev = np.zeros_like(O)
     P = probe0.astype(C64).copy()
+    Pprev = np.zeros_like(P)
     step = np.zeros_like(P)
     nscan = len(scanx)
     norm = F32(1.0 / math.sqrt(rows * cols))
@@ -409,6 +447,8 @@ def iterate(obj0, probe0, patterns, scanx, scany, n_iter, params: PtyParams, ord
             far = convert_fo(fft2_u(P))
             mx, my = find_middle((far.real * far.real + far.imag * far.imag).astype(F32))
             P = multiply_shift(P, F32(np.float64(F32(mx * F32(rows))) - 0.5), F32(np.float64(F32(my * F32(cols))) - 0.5))
+        if it < params.zernike_iter:          # util/ptycho.cpp:665-667
+            O = fista_step(O, 0.01)
         if params.mpie:
             s = (O * msum).astype(C64).astype(np.complex128).sum()
             s = complex(np.complex64(s))
@@ -420,6 +460,11 @@ def iterate(obj0, probe0, patterns, scanx, scany, n_iter, params: PtyParams, ord
             c = F32(F32(tk - F32(1)) / tkp1)
             Oprev = (O + (Oprev * c).astype(C64)).astype(C64)
             O, Oprev = Oprev, O
+            if it < params.zernike_iter and it % 10 == 0:   # dozernike: probe momentum too (682-686)
+                Pprev = (P - Pprev).astype(C64)
+                cz = F32(np.float64(c) * 0.8)
+                Pprev = (P + (Pprev * cz).astype(C64)).astype(C64)
+                P, Pprev = Pprev, P
             tk = tkp1
     pupil = angular_spectrum(P, params.lam, params.dpupil, res, reverse=True)
     s = complex(np.complex64(O.astype(np.complex128).sum()))

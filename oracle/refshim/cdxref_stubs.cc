@@ -92,7 +92,9 @@ complexFormat findMiddle(complexFormat*, int) { return 0; }
 Real* createBeamStop(int, int, int) { abort(); }
 void readComplexWaveFront(const char*, const char*, Real*&, Real*&, int&, int&) { abort(); }
 #endif
+#ifndef CDXREF_WITH_FISTA
 void FISTA(Real*, Real*, Real, int, void (*)(Real*, Real*)) { abort(); }
+#endif
 mnistData::mnistData(const char*) {}
 mnistData::~mnistData() {}
 cuMnist::cuMnist(const char* d, int, int, int, int) : mnistData(d) {}

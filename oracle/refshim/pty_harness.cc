@@ -10,7 +10,9 @@
 // pty_harness <object.bin> <probe.bin> <patterns.bin (nscan stacked, FFT order,
 //             scaled 1/exposure)> <scan.txt ("x y" per line)> <nIter> <mPIE>
 //             <lambda> <d> <dpupil> <pixelsize> <pupilSize> <exposure>
-//             <useBS> <beamStopSize> <rand seed> <out prefix> [noiseLevel]
+//             <useBS> <beamStopSize> <rand seed> <out prefix> [noiseLevel [zernikeIter]]
+// (zernikeIter > 0 runs the FISTA object step; the Zernike pupil fit it also
+// enables from iteration 400 is not linked, so such runs stop before it)
 #define main cdxref_ptycho_main
 #include CDXREF_PTYCHO_CPP
 #undef main
@@ -50,7 +52,7 @@ int main(int argc, char** argv) {
   p.isFresnel = 0;
   p.saveVideoEveryIter = 0;
   p.computeErrorEveryIter = 0;
-  p.zernikeIter = 0;
+  p.zernikeIter = argc > 18 ? atoi(argv[18]) : 0;
   p.positionUncertainty = 0;
   p.nIter = atoi(argv[5]);
   p.mPIE = atoi(argv[6]);

@@ -42,8 +42,11 @@ CASES = [
     ("probe402", 402, 1, 0, 5, 1.0, 40.0, "grid", 7),
     ("refine520", 520, 0, 0, 5, 1.0, 40.0, "grid", 7),
     ("noise2003", 2003, 0, 0, 5, 1.0, 40.0, "grid", 7),
+    ("fista45", 45, 1, 0, 5, 1.0, 40.0, "grid", 7),
+    ("fista405", 405, 0, 0, 5, 1.0, 40.0, "grid", 3),
 ]
 NOISE_LEVEL = {"noise2003": 20}
+ZERNIKE_ITER = {"fista45": 35, "fista405": 300}   # FISTA object step (and the probe momentum every 10)
 OPTICS = dict(lam=0.5, d=2e4, dpupil=1e3, pixelsize=20.0, pupil_size=16.0)
 
 
@@ -93,7 +96,7 @@ def main(ref=None):
             cmd = [str(harness), f"{d}/obj.bin", f"{d}/probe.bin", f"{d}/pats.bin", f"{d}/scan.txt", str(n_iter),
                    str(mpie), str(OPTICS["lam"]), str(OPTICS["d"]), str(OPTICS["dpupil"]), str(OPTICS["pixelsize"]),
                    str(OPTICS["pupil_size"]), str(expo), str(use_bs), str(bss), str(seed), f"{d}/out",
-                   str(NOISE_LEVEL.get(name, 0))]
+                   str(NOISE_LEVEL.get(name, 0)), str(ZERNIKE_ITER.get(name, 0))]
             subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL)
             p = f"{name}/"
             data[p + "obj0"] = obj0
@@ -102,7 +105,8 @@ def main(ref=None):
             data[p + "scanx"] = sx
             data[p + "scany"] = sy
             data[p + "orders"] = PO.scan_orders(len(sx), n_iter, seed)
-            data[p + "cfg"] = np.array([n_iter, mpie, use_bs, bss, seed, NOISE_LEVEL.get(name, 0)], np.int64)
+            data[p + "cfg"] = np.array([n_iter, mpie, use_bs, bss, seed, NOISE_LEVEL.get(name, 0),
+                                        ZERNIKE_ITER.get(name, 0)], np.int64)
             data[p + "exposure"] = np.float64(expo)
             data[p + "ref_object"] = read_bin(f"{d}/out_object.bin").copy()
             data[p + "ref_pupil"] = read_bin(f"{d}/out_pupil.bin").copy()

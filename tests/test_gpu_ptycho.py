@@ -26,7 +26,8 @@ def make(PT, c, prm, rows=None, obj_shape=None):
     t = PT.Ptycho(rows, c["probe0"].shape[1], orow, ocol, c["scanx"], c["scany"], lam=prm.lam, d=prm.d,
                   dpupil=prm.dpupil, pixelsize=prm.pixelsize, pupil_size=prm.pupil_size, exposure=prm.exposure,
                   mpie=prm.mpie, use_bs=prm.use_bs, beam_stop_size=prm.beam_stop_size,
-                  noise_level=prm.noise_level, position_uncertainty=prm.position_uncertainty)
+                  noise_level=prm.noise_level, position_uncertainty=prm.position_uncertainty,
+                  zernike_iter=prm.zernike_iter)
     t.objectWave = c["obj0"]
     t.probe = c["probe0"]
     t.patterns = c["pats"]
@@ -50,7 +51,7 @@ def test_gpu_draws_the_reference_orders_from_the_seed(PT):
         assert np.array_equal(a.objectWave, b.objectWave)
 
 
-@pytest.mark.parametrize("first", [0, 7, 400, 450, 520, 2000])
+@pytest.mark.parametrize("first", [0, 7, 10, 400, 450, 520, 2000])
 @pytest.mark.parametrize("mpie", [False, True])
 def test_one_sweep_matches_oracle(PT, first, mpie):
     """Per-iterate parity: one sweep (object phase, or probe phase from 400) from
@@ -58,6 +59,7 @@ def test_one_sweep_matches_oracle(PT, first, mpie):
     c, prm, _n, _s = load("obj3")
     prm.mpie = mpie
     prm.noise_level = 20   # the noise-tolerant projection from iteration 2000
+    prm.zernike_iter = 400 if first < 400 else 0   # FISTA step (and the probe momentum at 10) in the object phase
     rng = np.random.default_rng(first)
     obj = (c["obj0"] * (0.5 + rng.random(c["obj0"].shape))).astype(np.complex64)
     orders = np.array([rng.permutation(len(c["scanx"]))], np.int32)
@@ -134,6 +136,12 @@ def test_argument_checks(PT, cdx):
     with make(PT, c, prm) as t:
         with pytest.raises(cdx.CdxError):
             t.iterate(10, first_iter=495)          # position refinement from 500 is not built
+    prm.position_uncertainty = 0.0
+    prm.zernike_iter = 1200
+    with make(PT, c, prm) as t:
+        t.iterate(5)                               # FISTA steps in the object phase run
+        with pytest.raises(cdx.CdxError):
+            t.iterate(5, first_iter=400)           # the Zernike pupil fit from 400 is not built
         bad = c["orders"][:2].copy()
         bad[0, 0] = 99
         with pytest.raises(cdx.CdxError):

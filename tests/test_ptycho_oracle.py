@@ -10,7 +10,8 @@ import pytest
 from oracle import ptycho_oracle as PO
 
 GOLD = Path(__file__).resolve().parent / "golden" / "ptycho_cases.npz"
-CASES = ["obj3", "obj20_nompie", "obj30", "beamstop", "saturated", "offedge", "probe402", "refine520", "noise2003"]
+CASES = ["obj3", "obj20_nompie", "obj30", "beamstop", "saturated", "offedge", "probe402", "refine520", "noise2003",
+         "fista45", "fista405"]
 # Relative L2 bounds of oracle (and GPU) against the reference's run.  Short
 # runs agree to float32 rounding; along long runs the rounding differences of
 # two FFTs grow (momentum and the probe phase amplify them): measured oracle
@@ -21,18 +22,21 @@ CASES = ["obj3", "obj20_nompie", "obj30", "beamstop", "saturated", "offedge", "p
 # 520 sweeps across the reference's first position-refinement step (a no-op at
 # positionUncertainty = 0) 2.0e-5 / 1.6e-5; 2003 sweeps, the last three with
 # the noise-tolerant projection (noiseLevel 20), 1.4e-3 / 9.2e-4.
-OBJ_BOUND = {"obj30": 2e-4, "probe402": 3e-3, "refine520": 2e-4, "noise2003": 5e-3}
+# With zernikeIter (FISTA object step each sweep, probe momentum every tenth):
+# 45 sweeps with momentum 1.1e-6, 405 sweeps without 7.4e-7.
+OBJ_BOUND = {"obj30": 2e-4, "probe402": 3e-3, "refine520": 2e-4, "noise2003": 5e-3, "fista45": 1e-5,
+             "fista405": 1e-5}
 PUPIL_BOUND = {"probe402": 1e-4, "refine520": 2e-4, "noise2003": 5e-3}
 
 
 def load(name):
     z = np.load(GOLD)
     p = name + "/"
-    n_iter, mpie, use_bs, bss, seed, noise = [int(v) for v in z[p + "cfg"]]
+    n_iter, mpie, use_bs, bss, seed, noise, zern = [int(v) for v in z[p + "cfg"]]
     opt = z["optics"]
     prm = PO.PtyParams(lam=opt[0], d=opt[1], dpupil=opt[2], pixelsize=opt[3], pupil_size=opt[4],
                        exposure=float(z[p + "exposure"]), mpie=bool(mpie), use_bs=bool(use_bs),
-                       beam_stop_size=bss, noise_level=noise)
+                       beam_stop_size=bss, noise_level=noise, zernike_iter=zern)
     case = {k: z[p + k] for k in ("obj0", "probe0", "pats", "scanx", "scany", "orders", "ref_object", "ref_pupil")}
     return case, prm, n_iter, seed
 
