@@ -260,7 +260,9 @@ void CDI::prepareIter() {   // cdi.cc:160-230
   check(cdx_random_start(ctx_, seed_++), "prepareIter");
 }
 
-void CDI::checkAutoCorrelation() {   // cdi.cc:231-239: |IFFT(I)|/sqrt(N) written as .bin
+// cdi.cc:231-239: the forward transform of the pattern (R2C filled to the full
+// Hermitian spectrum) times 1/sqrt(N), the buffer the reference plots, written as .bin
+void CDI::checkAutoCorrelation() {
   const size_t n = (size_t)row * column;
   std::vector<float> pat(n), buf(2 * n, 0.f);
   cudaMemcpy(pat.data(), patternData, n * sizeof(float), cudaMemcpyDeviceToHost);
@@ -269,7 +271,6 @@ void CDI::checkAutoCorrelation() {   // cdi.cc:231-239: |IFFT(I)|/sqrt(N) writte
     check(CDX_ERR_NOMEM, "checkAutoCorrelation");
   cudaMemcpy(autoCorrelation, buf.data(), buf.size() * sizeof(float), cudaMemcpyHostToDevice);
   check(cdx_fft2(autoCorrelation, autoCorrelation, row, column, 1, 0, nullptr), "checkAutoCorrelation");
-  check(cdx_convert_fo(autoCorrelation, autoCorrelation, row, column, 1, 1, nullptr), "checkAutoCorrelation");
   cudaMemcpy(buf.data(), autoCorrelation, buf.size() * sizeof(float), cudaMemcpyDeviceToHost);
   const float s = (float)(1.0 / std::sqrt((double)n));
   for (float& v : buf) v *= s;

@@ -1,4 +1,4 @@
-// Host stand-in for the cuFFT C2C plans the reference uses (cudaConfig.cu:137-180):
+// Host stand-in for the cuFFT C2C (and R2C) plans the reference uses (cudaConfig.cu:137-180):
 // the published unnormalised DFT, evaluated in double (radix-2 for powers of
 // two, direct sums otherwise) and rounded once to float.
 #pragma once
@@ -77,5 +77,15 @@ inline cufftResult cufftExecC2C(cufftHandle h, cufftComplex* in, cufftComplex* o
   for (size_t i = 0; i < a.size(); ++i) out[i] = {(float)a[i].real(), (float)a[i].imag()};
   return 0;
 }
-inline cufftResult cufftExecR2C(cufftHandle, cufftReal*, cufftComplex*) { abort(); }
+// R2C: the C2C transform of the real input, columns 0 .. cols/2 of each row kept
+inline cufftResult cufftExecR2C(cufftHandle h, cufftReal* in, cufftComplex* out) {
+  const cdxref_plan p = cdxref_plans().at(h);
+  const int R = p.rows, C = p.cols, H = C / 2 + 1;
+  std::vector<cufftComplex> full((size_t)R * C);
+  for (size_t i = 0; i < full.size(); ++i) full[i] = {in[i], 0.f};
+  cufftExecC2C(h, full.data(), full.data(), CUFFT_FORWARD);
+  for (int r = 0; r < R; ++r)
+    for (int c = 0; c < H; ++c) out[(size_t)r * H + c] = full[(size_t)r * C + c];
+  return 0;
+}
 inline cufftResult cufftExecC2R(cufftHandle, cufftComplex*, cufftReal*) { abort(); }

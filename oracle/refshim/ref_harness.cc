@@ -79,6 +79,16 @@ int main(int argc, char** argv) {
   if (argc > 11 && atoi(argv[11])) {
     writeComplexImage((pre + "_rho_before_save.bin").c_str(), c.objectWave, c.row, c.column);
     c.saveState();
+    // checkAutoCorrelation (cdi.cc:231-239) takes rows*cols floats from the pool and has
+    // the R2C write rows*(cols/2+1) complex into them, rows*8 bytes past the end; the
+    // pool is handed a block of the half spectrum's size under that request's size
+    {
+      const size_t asked = (size_t)c.row * c.column * sizeof(Real);
+      void* half = malloc((size_t)c.row * (c.column / 2 + 1) * sizeof(complexFormat));
+      memMngr.registerMem(half, asked);
+      memMngr.returnCache(half);
+    }
+    c.checkAutoCorrelation();   // util/cdi.cpp:47: plotted as "autocorrelation"
   }
   writeComplexImage((pre + "_rho.bin").c_str(), c.objectWave, c.row, c.column);
   writeComplexImage((pre + "_psi.bin").c_str(), c.patternWave, c.row, c.column);

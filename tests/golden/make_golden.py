@@ -98,6 +98,7 @@ def main(ref=None):
         data["savestate/support"] = O.read_bin(plots / "support.bin")   # after bitMap
         data["savestate/wave"] = O.read_bin(plots / "recon_wave.bin")   # object cropped about mid
         data["savestate/autocorrelation"] = O.read_bin(plots / "autocorrelation_recon.bin")
+        data["savestate/check_autocorrelation"] = O.read_bin(plots / "autocorrelation.bin")   # checkAutoCorrelation
         # the noise-free runSim simulation (readObjectWave + prepareIter, cdi.cc:62-82, 161-200)
         rng = np.random.default_rng(11)
         m = 32

@@ -148,6 +148,9 @@ def test_oracle_savestate_matches_reference():
     assert np.array_equal(O.crop_about(rho, wave.shape[0], wave.shape[1], mid[0], mid[1]), wave)
     ac = np.fft.fft2(np.abs(psi.astype(np.complex128)) ** 2)
     assert rel(Z["savestate/autocorrelation"], ac) <= 1e-6
+    # checkAutoCorrelation: R2C of the pattern, filled to the Hermitian spectrum, / sqrt(N)
+    I = Z["intensity"].astype(np.float64)
+    assert rel(Z["savestate/check_autocorrelation"], np.fft.fft2(I) / np.sqrt(I.size)) <= 1e-6
     alg = str(Z["savestate/algorithm"])
     st, tol = trajectory_bound(Z["psi0"], Z["intensity"], alg, oversampling_spt=2.0, shrink_threshold=0.1)
     assert rel(st.rho, rho) <= tol
@@ -190,6 +193,8 @@ Job = {{
         assert rel(wave, Z["savestate/wave"]) <= tol
     ac = O.read_bin(tmp_path / "autocorrelation_recon.bin")
     assert rel(ac, Z["savestate/autocorrelation"]) <= 2 * tol
+    ac = O.read_bin(tmp_path / "autocorrelation.bin")          # checkAutoCorrelation
+    assert rel(ac, Z["savestate/check_autocorrelation"]) <= 1e-5
 
 
 # ------------------------------------------------------------------ runSim
