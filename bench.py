@@ -287,15 +287,17 @@ def batched_section():
 # Ptychography: the reference's own configuration (html/default/ptycho.cfg optics,
 # 512^2 probe, row_O = column_O = 1280, initScan_triangle with stepSize 250).
 PTY_R, PTY_RO, PTY_STEP = 512, 1280, 250.0
-PTY_OPTICS = dict(lam=0.6328, d=125e3, dpupil=6.8e3, pixelsize=13.0, pupil_size=335.0083, exposure=0.01)
+PTY_OPTICS = dict(lam=0.6328, d=125e3, dpupil=6.8e3, pixelsize=13.0, pupil_size=335.0083, exposure=0.01,
+                  zernike_iter=1200)
 PTY_SWEEPS = 100
 
 
 def ptycho_section(cpu=True):
-    """rPIE + mPIE sweeps (ptycho::iterate, object phase) on the reference's
-    configuration with noise-free simulated patterns of a smooth synthetic object:
-    sweeps/s from CUDA events around cdx_pty_iterate, a probe-phase sweep time,
-    the roofline of a sweep and the oracle on one sweep as the CPU baseline."""
+    """rPIE + mPIE sweeps (ptycho::iterate, object phase with the FISTA object step of
+    zernikeIter 1200) on the reference's configuration with noise-free simulated
+    patterns of a smooth synthetic object: sweeps/s from CUDA events around
+    cdx_pty_iterate, probe-phase sweep times (with and without the Zernike pupil
+    fit), the roofline of a sweep and the oracle on one sweep as the CPU baseline."""
     from cdixx_gb300 import ptycho as PT
     sx, sy = PT.scan_triangle(PTY_RO, PTY_RO, PTY_R, PTY_R, PTY_STEP)
     t = PT.Ptycho(PTY_R, PTY_R, PTY_RO, PTY_RO, sx, sy, **PTY_OPTICS)
@@ -313,12 +315,17 @@ def ptycho_section(cpu=True):
     ms = t.iterate(PTY_SWEEPS, seed=1)
     sweeps_s = PTY_SWEEPS / (ms / 1000.0)
     t.probe = probe0
-    ms_probe = t.iterate(20, first_iter=400, seed=2)
+    ms_probe = t.iterate(20, first_iter=400, seed=2)      # two of them with the Zernike pupil fit
+    t.probe = probe0
+    ms_zk = t.iterate(1, first_iter=400, seed=3)
+    t.probe = probe0
+    ms_nozk = t.iterate(1, first_iter=401, seed=3)
     n, on, ns = PTY_R * PTY_R, PTY_RO * PTY_RO, len(sx)
     # algorithmic bytes of a sweep: per position the object window read and written,
-    # the probe and the pattern read (8 + 8 + 8 + 4 B/px); the momentum step reads the
-    # object, its history and the overlap mask and writes both (36 B/px of the object)
-    alg = ns * 28 * n + 36 * on
+    # the probe and the pattern read (8 + 8 + 8 + 4 B/px); the FISTA step reads and
+    # writes the object (16 B/px); the momentum step reads the object, its history and
+    # the overlap mask and writes both (36 B/px of the object)
+    alg = ns * 28 * n + (16 + 36) * on
     achieved = alg / (ms / PTY_SWEEPS / 1000.0) / 1e9
     peak, peak_kind = peaks()
     out = {"metric": "ptycho sweeps/s", "value": sweeps_s, "positions_per_s": sweeps_s * ns,
@@ -326,14 +333,15 @@ def ptycho_section(cpu=True):
                       "optics": PTY_OPTICS, "sweeps": PTY_SWEEPS, "mPIE": True,
                       "data": "noise-free patterns of a synthetic smooth object (createPattern)"},
            "ms_per_sweep": ms / PTY_SWEEPS, "ms_per_probe_phase_sweep": ms_probe / 20,
+           "ms_zernike_sweep": ms_zk, "ms_probe_sweep_without_zernike": ms_nozk,
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                         "alg_bytes_per_sweep": alg, "peak_kind": peak_kind},
-           "gpu_launches_per_sweep": 3 * ns + 4}
+           "gpu_launches_per_sweep": 3 * ns + 5 + 0.1}   # + the probe momentum every tenth sweep
     if cpu:
         from oracle import ptycho_oracle as PO
         prm = PO.PtyParams(lam=PTY_OPTICS["lam"], d=PTY_OPTICS["d"], dpupil=PTY_OPTICS["dpupil"],
                            pixelsize=PTY_OPTICS["pixelsize"], pupil_size=PTY_OPTICS["pupil_size"],
-                           exposure=PTY_OPTICS["exposure"], mpie=True)
+                           exposure=PTY_OPTICS["exposure"], mpie=True, zernike_iter=PTY_OPTICS["zernike_iter"])
         pats = t.patterns
         orders = PO.scan_orders(ns, 1, 1)
         t0 = time.perf_counter()

@@ -24,7 +24,7 @@ GENCODE = "arch=compute_103a,code=sm_103a"
 
 CU_UNITS = ["cdx_api.cu", "cdx_misc.cu", "cdx_dispatch.cu", "cdx_sizes_a.cu", "cdx_sizes_b.cu",
             "cdx_sizes_c.cu", "cdx_sizes_d.cu", "cdx_noalloc.cu", "cdx_unet.cu", "cdx_fwdmodel.cu", "cdx_umma.cu",
-            "cdx_ptycho.cu", "cdx_pty_sizes_a.cu", "cdx_pty_sizes_b.cu"]
+            "cdx_ptycho.cu", "cdx_pty_sizes_a.cu", "cdx_pty_sizes_b.cu", "cdx_pty_zernike.cu"]
 CC_UNITS = ["cdx_host.cc", "cdx_config.cc", "cdi_shim.cc"]
 
 

@@ -1,0 +1,294 @@
+// The Zernike pupil fit of the ptychographic probe phase (util/ptycho.cpp:617-626,
+// src/gpu/beamDecomposition.cu:11-608): on a Zernike sweep the pd x pd crop of the
+// back-propagated probe is projected on the real Zernike basis up to radial order
+// 40 (861 modes), the coefficients are soft-thresholded and the crop is replaced
+// by their sum, instead of being cut with the pupil disk.
+//
+// Device layout: a per-pixel table of the crop (covered fraction of the pixel in
+// the disk of radius pd/2, the radius and angle of the covered part's centroid)
+// built once per context; per sweep three launches:
+//   k_zk_project   one pixel per thread, per mode a warp reduction, the CTA's
+//                  four warps summed into one partial row [CTA][mode]
+//   k_zk_finish    per mode the partial rows summed in double, scaled by
+//                  1/(pi (pd/2)^2) and soft-thresholded
+//   k_zk_rebuild   the probe rewritten: the coefficients' sum inside the crop on
+//                  the pixels the disk touches, zero elsewhere (crop, pad)
+#include <cuda_runtime.h>
+
+#include "cdx_pty_zernike.cuh"
+
+namespace cdx {
+namespace {
+
+constexpr int kZkThreads = 128;
+constexpr int kZkWarps = kZkThreads / 32;
+
+struct Cover {
+  float a, cx, cy;
+};
+
+// compute_pixel (beamDecomposition.cu:11-104): area of the unit pixel centred at
+// (px, py) inside the circle of radius r about the origin, and the centroid of
+// that area.  Far pixels count 0 or 1; a pixel with all corners in (out) counts
+// 1 (0); otherwise the polygon of the inside corners and the edge crossings,
+// ordered by angle about the pixel centre, plus the circular segment beyond the
+// chord when the circle crosses the pixel twice.
+__device__ Cover pixel_cover(float px, float py, float r) {
+  const float r2 = r * r;
+  const float d2 = px * px + py * py;
+  const float s2 = sqrtf(2.f);
+  if (d2 > (r + s2) * (r + s2)) return {0.f, px, py};
+  if (d2 < (r - s2) * (r - s2)) return {1.f, px, py};
+  const float x0 = px - 0.5f, x1 = px + 0.5f, y0 = py - 0.5f, y1 = py + 0.5f;
+  const float qx[4] = {x0, x1, x1, x0}, qy[4] = {y0, y0, y1, y1};
+  bool in[4];
+  int n_in = 0;
+  for (int k = 0; k < 4; ++k) {
+    in[k] = qx[k] * qx[k] + qy[k] * qy[k] < r2;
+    n_in += in[k];
+  }
+  if (n_in == 4) return {1.f, px, py};
+  if (n_in == 0) return {0.f, px, py};
+  const float eps = 1e-5f;
+  float ix[8], iy[8];
+  int ni = 0;
+  auto known = [&](float x, float y) {
+    for (int k = 0; k < ni; ++k)
+      if (fabsf(ix[k] - x) < eps && fabsf(iy[k] - y) < eps) return true;
+    return false;
+  };
+  for (int e = 0; e < 2; ++e) {   // vertical edges x = x0, x1
+    const float x = e ? x1 : x0;
+    float val = (r - x) * (r + x);
+    if (val >= -eps) {
+      const float y = sqrtf(fmaxf(val, 0.f));
+      if (y >= y0 - eps && y <= y1 + eps && !known(x, y)) { ix[ni] = x; iy[ni] = y; ++ni; }
+      if (ni < 8 && y > eps && -y >= y0 - eps && -y <= y1 + eps && !known(x, -y)) { ix[ni] = x; iy[ni] = -y; ++ni; }
+    }
+  }
+  for (int e = 0; e < 2; ++e) {   // horizontal edges y = y0, y1
+    const float y = e ? y1 : y0;
+    float val = (r - y) * (r + y);
+    if (val >= -eps) {
+      const float x = sqrtf(fmaxf(val, 0.f));
+      if (x >= x0 - eps && x <= x1 + eps && !known(x, y)) { ix[ni] = x; iy[ni] = y; ++ni; }
+      if (ni < 8 && x > eps && -x >= x0 - eps && -x <= x1 + eps && !known(-x, y)) { ix[ni] = -x; iy[ni] = y; ++ni; }
+    }
+  }
+  float vx[12], vy[12], ang[12];
+  int nv = 0;
+  for (int k = 0; k < 4; ++k)
+    if (in[k]) { vx[nv] = qx[k]; vy[nv] = qy[k]; ++nv; }
+  for (int k = 0; k < ni; ++k) { vx[nv] = ix[k]; vy[nv] = iy[k]; ++nv; }
+  if (nv < 3) return {n_in > 0 ? 1.f : 0.f, px, py};
+  int idx[12];
+  for (int k = 0; k < nv; ++k) {
+    idx[k] = k;
+    ang[k] = atan2f(vy[k] - py, vx[k] - px);
+  }
+  for (int i = 0; i < nv - 1; ++i)   // the reference's exchange sort by angle
+    for (int j = i + 1; j < nv; ++j)
+      if (ang[idx[i]] > ang[idx[j]]) { const int s = idx[i]; idx[i] = idx[j]; idx[j] = s; }
+  float A = 0.f, Mx = 0.f, My = 0.f;
+  for (int i = 0; i < nv; ++i) {
+    const int a = idx[i], b = idx[(i + 1) % nv];
+    const double cross = (double)vx[a] * vy[b] - (double)vx[b] * vy[a];
+    A = (float)(A + cross);
+    Mx = (float)(Mx + (vx[a] + vx[b]) * cross);
+    My = (float)(My + (vy[a] + vy[b]) * cross);
+  }
+  A *= 0.5f;
+  Mx /= 6.f;
+  My /= 6.f;
+  if (A < 0.f) { A = -A; Mx = -Mx; My = -My; }
+  if (ni == 2) {   // circular segment between the chord and the arc
+    const float mx = (ix[0] + ix[1]) * 0.5f, my = (iy[0] + iy[1]) * 0.5f;
+    const float cx = ix[0] - ix[1], cy = iy[0] - iy[1];
+    const float L = sqrtf(cx * cx + cy * cy);
+    const float h = sqrtf(mx * mx + my * my);
+    const float th = 2.f * atan2f(0.5f * L, h);
+    float tms, shc;
+    if (th < 1e-4f) {   // theta - sin(theta) and sin^3(theta/2) by their series
+      const float t2 = th * th, t3 = t2 * th, t5 = t3 * t2;
+      tms = t3 / 6.f - t5 / 120.f;
+      const float sh = 0.5f * th;
+      shc = sh * sh * sh;
+    } else {
+      tms = th - sinf(th);
+      shc = powf(sinf(0.5f * th), 3.f);
+    }
+    const float As = 0.5f * r2 * tms;
+    const float ds = tms > 1e-10f ? (4.f * r * shc) / (3.f * tms) : r;
+    const float nrm = h > 1e-9f ? h : 1.f;
+    A += As;
+    Mx += As * ds * (mx / nrm);
+    My += As * ds * (my / nrm);
+  }
+  if (A > 1e-9f) return {A, Mx / A, My / A};
+  return {A, px, py};
+}
+
+// the crop's pixel table: x = column, y = row about ((pd-1)/2, (pd-1)/2), radius pd/2
+__global__ void k_zk_table(float4* __restrict__ tab, int pd) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= pd * pd) return;
+  const float c = (float)(pd - 1) / 2, rad = (float)pd / 2;
+  const Cover cv = pixel_cover((float)(g % pd) - c, (float)(g / pd) - c, rad);
+  float rho = 1.f, th = 0.f;
+  if (cv.a > 2e-20f) {
+    rho = fminf(sqrtf(cv.cx * cv.cx + cv.cy * cv.cy) / rad, 1.f);
+    th = atan2f(cv.cy, cv.cx);
+  }
+  // x: projection weight (zero for pixels the disk misses), w: rebuilt (1) or zeroed (0)
+  tab[g] = make_float4(cv.a > 2e-20f ? cv.a : 0.f, rho, th, cv.a < 2e-20f ? 0.f : 1.f);
+}
+
+// Visits the 861 modes in the reference's order (m = 0 .. 40; n = m, m+2 .. 40;
+// cos then sin for m > 0) with the radial polynomial R_n^m(rho) * weight from
+// the three-term recurrence in n, normalised by sqrt(n+1) (m = 0) or
+// sqrt(2 (n+1)); f(mode, value) receives the basis value at the pixel.
+template <class F>
+__device__ __forceinline__ void zk_modes(float rho, float th, float weight, F&& f) {
+  int mode = 0;
+  float rp = weight;   // weight * rho^m
+  for (int m = 0; m <= kZkMaxN; ++m) {
+    float cm = 1.f, sm = 0.f;
+    if (m > 0) sincosf(m * th, &sm, &cm);
+    float r2 = 0.f, r4 = 0.f;
+    for (int n = m; n <= kZkMaxN; n += 2) {
+      float cur;
+      if (n == m) {
+        cur = rp;
+      } else if (n == m + 2) {
+        cur = r2 * ((m + 2) * rho * rho - (m + 1));
+      } else {
+        const float k1 = 0.5f * (n + m) * (n - m) * (n - 2.f);
+        const float k2 = 2.f * n * (n - 1.f) * (n - 2.f);
+        const float k3 = -m * m * (n - 1.f) - n * (n - 1.f) * (n - 2.f);
+        const float k4 = -0.5f * n * (n + m - 2.f) * (n - m - 2.f);
+        cur = ((k2 * rho * rho + k3) * r2 + k4 * r4) / k1;
+      }
+      r4 = r2;
+      r2 = cur;
+      const float z = cur * (m == 0 ? sqrtf(n + 1.f) : sqrtf(2.f * (n + 1.f)));
+      if (m == 0) {
+        f(mode++, z);
+      } else {
+        f(mode++, z * cm);
+        f(mode++, z * sm);
+      }
+    }
+    rp *= rho;
+  }
+}
+
+__global__ void __launch_bounds__(kZkThreads) k_zk_project(const float2* __restrict__ P, int cols, int r0, int c0,
+                                                            int pd, const float4* __restrict__ tab,
+                                                            float2* __restrict__ part) {
+  __shared__ float2 acc[kZkWarps][kZkModes];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int g = blockIdx.x * kZkThreads + threadIdx.x;
+  float4 e = make_float4(0.f, 1.f, 0.f, 0.f);
+  float2 v = make_float2(0.f, 0.f);
+  if (g < pd * pd) {
+    e = tab[g];
+    if (e.x > 0.f) v = P[(long long)(r0 + g / pd) * cols + c0 + g % pd];
+  }
+  zk_modes(e.y, e.z, e.x, [&](int k, float z) {
+    float re = v.x * z, im = v.y * z;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      re += __shfl_xor_sync(0xffffffffu, re, o);
+      im += __shfl_xor_sync(0xffffffffu, im, o);
+    }
+    if (lane == 0) acc[warp][k] = make_float2(re, im);
+  });
+  __syncthreads();
+  for (int k = threadIdx.x; k < kZkModes; k += kZkThreads) {
+    float2 s = acc[0][k];
+#pragma unroll
+    for (int w = 1; w < kZkWarps; ++w) {
+      s.x += acc[w][k].x;
+      s.y += acc[w][k].y;
+    }
+    part[(long long)blockIdx.x * kZkModes + k] = s;
+  }
+}
+
+// reduce_coefficients (norm 1/(pi r^2)) and regularize_zernike_coefficients as
+// zernike_compute launches them (beamDecomposition.cu:460-513, 568-591): the
+// launch passes the mode count (861) as the order bound, so mode k <= 430 is
+// thresholded as (p, m) = (2k, 0) and mode k > 430 as (1 + 2 ((k - 431) / 2), 1);
+// c *= max(0, 1 - (5e-5 p^2 + 5e-8 m^2) / |c|), zero for |c| <= 1e-9.
+__global__ void k_zk_finish(const float2* __restrict__ part, int nblk, double norm, float2* __restrict__ coef) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= kZkModes) return;
+  double sx = 0, sy = 0;
+  for (int b = 0; b < nblk; ++b) {
+    const float2 p = part[(long long)b * kZkModes + k];
+    sx += p.x;
+    sy += p.y;
+  }
+  const float cx = (float)(sx * norm), cy = (float)(sy * norm);
+  const int half = kZkModes >> 1;
+  int p, m;
+  if (k <= half) {
+    p = 2 * k;
+    m = 0;
+  } else {
+    m = 1;
+    p = 1 + (((k - half - 1) >> 1) << 1);
+  }
+  const float factor = 5e-5f * p * p + 5e-8f * m * m;
+  const float mag = hypotf(cx, cy);
+  const float s = mag > 1e-9f ? fmaxf(0.f, 1.f - factor / mag) : 0.f;
+  coef[k] = make_float2(cx * s, cy * s);
+}
+
+// zernike_reconstruct into the crop, then pad back: the whole probe is written
+__global__ void k_zk_rebuild(float2* __restrict__ P, int rows, int cols, int r0, int c0, int pd,
+                             const float4* __restrict__ tab, const float2* __restrict__ coef) {
+  __shared__ float2 cs[kZkModes];
+  for (int k = threadIdx.x; k < kZkModes; k += blockDim.x) cs[k] = coef[k];
+  __syncthreads();
+  const long long n = (long long)rows * cols;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(i / cols) - r0, y = (int)(i % cols) - c0;
+    float2 out = make_float2(0.f, 0.f);
+    if (x >= 0 && x < pd && y >= 0 && y < pd) {
+      const float4 e = tab[x * pd + y];
+      if (e.w > 0.f) {
+        const float th = e.y > 2e-20f ? e.z : 0.f;
+        zk_modes(e.y, th, 1.f, [&](int k, float z) {
+          out.x += cs[k].x * z;
+          out.y += cs[k].y * z;
+        });
+      }
+    }
+    P[i] = out;
+  }
+}
+
+}  // namespace
+
+int zk_blocks(int pd) { return (pd * pd + kZkThreads - 1) / kZkThreads; }
+
+cudaError_t zk_table(float4* tab, int pd, cudaStream_t st) {
+  k_zk_table<<<(pd * pd + 127) / 128, 128, 0, st>>>(tab, pd);
+  return cudaGetLastError();
+}
+
+cudaError_t zk_fit(float2* P, int rows, int cols, int pd, const float4* tab, float2* part, float2* coef,
+                   cudaStream_t st) {
+  const int r0 = (rows - pd) / 2, c0 = (cols - pd) / 2;
+  const int nblk = zk_blocks(pd);
+  k_zk_project<<<nblk, kZkThreads, 0, st>>>(P, cols, r0, c0, pd, tab, part);
+  const float rad = (float)pd / 2;
+  k_zk_finish<<<(kZkModes + 127) / 128, 128, 0, st>>>(part, nblk, 1. / (M_PI * rad * rad), coef);
+  const long long n = (long long)rows * cols;
+  const int grid = (int)((n + 255) / 256 < 1216 ? (n + 255) / 256 : 1216);
+  k_zk_rebuild<<<grid, 256, 0, st>>>(P, rows, cols, r0, c0, pd, tab, coef);
+  return cudaGetLastError();
+}
+
+}  // namespace cdx

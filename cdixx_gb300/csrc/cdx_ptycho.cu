@@ -24,6 +24,7 @@
 #include "cdx_fft.cuh"
 #include "cdx_host.h"
 #include "cdx_ptycho.cuh"
+#include "cdx_pty_zernike.cuh"
 #include "cdx_types.h"
 
 using namespace cdx;
@@ -165,13 +166,17 @@ __global__ void k_pty_obj_balance(float2* __restrict__ O, float2* __restrict__ O
   }
 }
 
-__global__ void k_pty_scale(float2* __restrict__ x, long long n, const float* f) {
+// applyNorm(pupilpatternWave, 1/sf) and applyNorm(probe_prev, 1/sf) (util/ptycho.cpp:506-507)
+__global__ void k_pty_scale(float2* __restrict__ x, float2* __restrict__ y, long long n, const float* f) {
   const float s = *f;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    float2 v = x[i];
+    float2 v = x[i], w = y[i];
     v.x *= s;
     v.y *= s;
+    w.x *= s;
+    w.y *= s;
     x[i] = v;
+    y[i] = w;
   }
 }
 
@@ -595,10 +600,14 @@ struct cdx_pty {
   int order_cap = 0, coef_cap = 0;
   bool have_scan = false, have_pats = false, have_obj = false, have_probe = false;
   // one sweep per kind: phase (object, probe, probe + noise projection) x FISTA x probe momentum
-  cudaGraphExec_t graph[12] = {};
+  // x Zernike pupil fit
+  cudaGraphExec_t graph[24] = {};
   float2* Pp = nullptr;       // probe momentum history (Zernike sweeps)
   float2* fista = nullptr;    // FISTA output before it replaces the object
   float* coefz = nullptr;     // probe momentum coefficients per sweep
+  float4* zk_tab = nullptr;   // Zernike fit: pixel table of the pupil crop
+  float2* zk_part = nullptr;  // Zernike fit: partial coefficients per projection CTA
+  float2* zk_coef = nullptr;  // Zernike fit: the thresholded coefficients
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   float last_ms = 0.f;
   float lam = 0, dist = 0, res = 0;   // propagate_pupil members (float)
@@ -684,7 +693,7 @@ PtyArgs pass_args(cdx_pty* t, int k, bool probe_phase, bool noise_proj = false) 
 }
 
 // One sweep of ptycho::iterate (util/ptycho.cpp:484-690) for the iteration the device counter names.
-int enqueue_sweep(cdx_pty* t, bool probe_phase, bool noise_proj, bool fista, bool probe_momentum) {
+int enqueue_sweep(cdx_pty* t, bool probe_phase, bool noise_proj, bool fista, bool probe_momentum, bool zernike) {
   cudaStream_t st = t->st;
   const long long n = t->npx, on = t->onpx;
   PTY_CK(cudaMemsetAsync(t->scal->maxb, 0, sizeof(t->scal->maxb), st));
@@ -694,7 +703,7 @@ int enqueue_sweep(cdx_pty* t, bool probe_phase, bool noise_proj, bool fista, boo
     k_pty_max_mod2<<<grid1(on), 256, 0, st>>>(t->O, t->msum, on, &t->scal->maxb[1], t->scal, t->cnt + 1, 1);
   if (probe_phase) {
     k_pty_obj_balance<<<grid1(on), 256, 0, st>>>(t->O, t->Op, on, t->scal);
-    k_pty_scale<<<grid1(n), 256, 0, st>>>(t->P, n, &t->scal->isf);
+    k_pty_scale<<<grid1(n), 256, 0, st>>>(t->P, t->Pp, n, &t->scal->isf);
   }
   PTY_CK(cudaGetLastError());
   for (int k = 0; k < t->p.nscan; ++k) {
@@ -709,7 +718,10 @@ int enqueue_sweep(cdx_pty* t, bool probe_phase, bool noise_proj, bool fista, boo
   if (probe_phase) {
     k_pty_add_step<<<grid1(n), 256, 0, st>>>(t->P, t->step, n);
     PTY_RET(angular_spectrum(t, t->P, true));
-    k_pty_pupil_mask<<<grid1(n), 256, 0, st>>>(t->P, t->p.rows, t->p.cols, (int)t->p.pupil_size);
+    if (zernike)   // util/ptycho.cpp:619-621: zernike_compute + zernike_reconstruct on the crop
+      PTY_CK(zk_fit(t->P, t->p.rows, t->p.cols, (int)t->p.pupil_size, t->zk_tab, t->zk_part, t->zk_coef, st));
+    else
+      k_pty_pupil_mask<<<grid1(n), 256, 0, st>>>(t->P, t->p.rows, t->p.cols, (int)t->p.pupil_size);
     PTY_RET(angular_spectrum(t, t->P, false));
     PTY_RET(fft2(t, t->P, t->tmp, false));
     k_pty_far_part<<<kRedBlocks, 256, 0, st>>>(t->tmp, t->p.rows, t->p.cols, t->part, t->scal, t->cnt + 2);
@@ -732,12 +744,14 @@ int enqueue_sweep(cdx_pty* t, bool probe_phase, bool noise_proj, bool fista, boo
 }
 
 // sweep kind of iteration `it`: phase 0 object, 1 probe, 2 probe with applyMod; + 3 with the
-// FISTA object step (it < zernikeIter); + 6 with the probe momentum (a Zernike sweep with mPIE)
+// FISTA object step (it < zernikeIter); + 6 with the probe momentum (dozernike with mPIE);
+// + 12 with the Zernike pupil fit (dozernike in the probe phase)
 int sweep_kind(const cdx_pty* t, int it) {
   const int phase = it < kUpdateProbeIter ? 0 : (it < kNoiseProjIter ? 1 : 2);
   const bool fista = it < t->p.zernike_iter;
-  const bool pmom = fista && t->p.mpie && it % 10 == 0;
-  return phase + (fista ? 3 : 0) + (pmom ? 6 : 0);
+  const bool dozernike = fista && it % 10 == 0;
+  const bool pmom = dozernike && t->p.mpie;
+  return phase + (fista ? 3 : 0) + (pmom ? 6 : 0) + (dozernike && phase > 0 ? 12 : 0);
 }
 
 int ensure_graph(cdx_pty* t, int kind) {
@@ -746,7 +760,7 @@ int ensure_graph(cdx_pty* t, int kind) {
   cudaGraph_t graph = nullptr;
   PTY_CK(cudaStreamBeginCapture(t->st, cudaStreamCaptureModeThreadLocal));
   const int phase = kind % 3;
-  const int r = enqueue_sweep(t, phase >= 1, phase == 2, (kind / 3) % 2 == 1, kind >= 6);
+  const int r = enqueue_sweep(t, phase >= 1, phase == 2, (kind / 3) % 2 == 1, (kind / 6) % 2 == 1, kind >= 12);
   const cudaError_t e = cudaStreamEndCapture(t->st, &graph);
   if (r != CDX_OK) {
     if (graph) cudaGraphDestroy(graph);
@@ -833,6 +847,13 @@ int cdx_pty_create(const cdx_pty_params* p, void* stream, cdx_pty** out) {
       (r = dalloc(&t->scal, 1)) || (r = dalloc(&t->part, 3 * kRedBlocks)) || (r = dalloc(&t->cnt, 4)) || (r = dalloc(&t->derr, 1)) || (r = dalloc(&t->Pp, t->npx)) ||
       (r = dalloc(&t->fista, p->zernike_iter > 0 ? t->onpx : 1)))
     return fail(r);
+  if (p->zernike_iter > kUpdateProbeIter) {   // Zernike sweeps are possible: the fit's buffers and pixel table
+    if ((r = dalloc(&t->zk_tab, (size_t)pd * pd)) || (r = dalloc(&t->zk_part, (size_t)zk_blocks(pd) * kZkModes)) ||
+        (r = dalloc(&t->zk_coef, kZkModes)))
+      return fail(r);
+    if ((e = zk_table(t->zk_tab, pd, t->st)) != cudaSuccess)
+      return fail(set_error(CDX_ERR_CUDA, std::string("Zernike table: ") + cudaGetErrorString(e)));
+  }
   e = cudaMemsetAsync(t->W, 0, sizeof(float2) * t->pat_stride, t->st);
   if (e == cudaSuccess) e = cudaMemsetAsync(t->pats, 0, sizeof(float) * t->pat_stride * p->nscan, t->st);
   if (e == cudaSuccess) e = cudaMemsetAsync(t->bs, 0, sizeof(float) * t->pat_stride, t->st);
@@ -864,7 +885,7 @@ int cdx_pty_destroy(cdx_pty* t) {
     if (g) cudaGraphExecDestroy(g);
   void* bufs[] = {t->O, t->Op, t->P, t->step, t->W, t->tmp, t->pupil, t->pats, t->bs, t->msum, t->coef,
                   t->win, t->tpos, t->order, t->iter, t->scal, t->part, t->cnt, t->derr, t->Pp, t->fista,
-                  t->coefz};
+                  t->coefz, t->zk_tab, t->zk_part, t->zk_coef};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (t->e0) cudaEventDestroy(t->e0);
@@ -1030,10 +1051,6 @@ int cdx_pty_iterate(cdx_pty* t, int first_iter, int n_iter, const int* orders, u
                                   "which is not built: first_iter + n_iter must be <= 500");
   if (!t->have_scan || !t->have_pats || !t->have_obj || !t->have_probe)
     return set_error(CDX_ERR_STATE, "scan positions, patterns, object and probe must be set first");
-  for (int it = std::max(first_iter, kUpdateProbeIter); it < first_iter + n_iter && it < t->p.zernike_iter; ++it)
-    if (it % 10 == 0)
-      return set_error(CDX_ERR_ARG, "from iteration 400 zernikeIter enables the Zernike pupil fit, which is not built "
-                                    "(zernike_iter must be <= 400 or the run must end before the fit)");
   const int ns = t->p.nscan;
   std::vector<int> ord((size_t)std::max(1, n_iter) * ns);
   if (orders) {

@@ -43,8 +43,9 @@ typedef struct cdx_pty_params {
   int noise_level;         /* noiseLevel: tolerance of the modulus projection from iteration 2000 */
   double position_uncertainty; /* positionUncertainty: > 0 asks for scan-position refinement (not built) */
   int zernike_iter;        /* zernikeIter: before it the object takes a FISTA (TV) step each sweep and,
-                              every tenth sweep, the probe a momentum step; the Zernike pupil fit it also
-                              enables from iteration 400 is not built (such runs are refused) */
+                              every tenth sweep, the probe a momentum step (with mPIE) and, from
+                              iteration 400, the Zernike pupil fit (861 modes up to order 40) in place of
+                              the pupil disk (util/ptycho.cpp:484, 617-626, 665-671) */
 } cdx_pty_params;
 
 /* Defaults of readConfig (include/readConfig.hpp): mPIE 1, pupilSize 500,

@@ -28,17 +28,21 @@ echo "built $OUT/ref_harness"
 
 # Ptychography pin: the reference's ptycho driver (util/ptycho.cpp, compiled
 # into pty_harness.cc), its kernels (src/gpu/ptycho.cu), the propagator, the
-# FISTA object step and the misc helpers (findMiddle, createCircleMask,
-# shiftWave) it calls.
+# FISTA object step, the Zernike pupil fit (src/gpu/beamDecomposition.cu) and
+# the misc helpers (findMiddle, createCircleMask, shiftWave) it calls.
 PO="$OUT/obj_pty"
 mkdir -p "$PO"
 sed "$LAUNCH" "$REF/src/gpu/ptycho.cu" | $CXX -x c++ - -I"$REF/src/gpu" -c -o "$PO/ptycho.cu.o"
+# the Zernike pupil fit synchronises its blocks: its launches go through
+# cdxref::coop (a generic lambda calls the kernel by name, default arguments kept)
+COOP='s/\([A-Za-z_][A-Za-z0-9_]*\(<[A-Za-z0-9_ ,:]*>\)\{0,1\}\)[ ]*<<<\(.*\)>>>/cdxref::coop(\3, [](auto... cdxref_a_) { \1(cdxref_a_...); })/g'
+sed "$COOP" "$REF/src/gpu/beamDecomposition.cu" | $CXX -x c++ - -I"$REF/src/gpu" -c -o "$PO/beamDecomposition.cu.o"
 $CXX -c "$REF/src/post_gpu/propagator.cc" -o "$PO/propagator.cc.o"
 $CXX -c "$REF/src/post_gpu/FISTA.cc" -o "$PO/FISTA.cc.o"
 $CXX -DCDXREF_WITH_PROPAGATOR -DCDXREF_WITH_MISC -DCDXREF_WITH_PTYCHO_KERNELS -DCDXREF_WITH_FISTA -c "$SHIM/cdxref_stubs.cc" -o "$PO/cdxref_stubs.o"
 $CXX -c "$SHIM/pty_stubs.cc" -o "$PO/pty_stubs.o"
 $CXX -include "$SHIM/cdxref_ptycho.h" -DCDXREF_PTYCHO_CPP="\"$REF/util/ptycho.cpp\"" -c "$SHIM/pty_harness.cc" \
   -o "$PO/pty_harness.o"
-g++ -o "$OUT/pty_harness" "$PO"/*.o "$OUT/obj/cudaConfig.cu.o" "$OUT/obj/cdi.cu.o" "$OUT/obj/cub_wrap.cu.o" \
+g++ -pthread -o "$OUT/pty_harness" "$PO"/*.o "$OUT/obj/cudaConfig.cu.o" "$OUT/obj/cdi.cu.o" "$OUT/obj/cub_wrap.cu.o" \
   "$OUT/obj/misc.cc.o" "$OUT/obj/memManager.cc.o" "$OUT/obj/readConfig.cc.o"
 echo "built $OUT/pty_harness"

@@ -12,8 +12,8 @@ the reference's scalar types (float parameters; the double literals and double
 config fields where the reference has them).  The FFT is the unnormalised DFT
 via NumPy (cuFFT's published transform), reductions accumulate in float64.
 
-Scope: the iteration without Fresnel propagation, Zernike/FISTA pupil steps and
-scan-position refinement.  From iteration 500 the reference refines the
+Scope: the iteration with the FISTA object step and the Zernike pupil fit,
+without Fresnel propagation and scan-position refinement.  From iteration 500 the reference refines the
 positions every 20 sweeps; with positionUncertainty = 0 (its default) that
 leaves every shift at zero and the object changed only by the rounding of an
 FFT round trip, which is not repeated here; runs with positionUncertainty > 0
@@ -329,6 +329,200 @@ def multiply_shift(wave, shiftx, shifty):
     return (wave * (np.cos(ph) + 1j * np.sin(ph)).astype(C64)).astype(C64)
 
 
+# ------------------------------------------------------- Zernike pupil fit
+ZERNIKE_MAX_N = 40                      # util/ptycho.cpp:439
+ZERNIKE_REG_L, ZERNIKE_REG_M = F32(5e-5), F32(5e-8)   # beamDecomposition.cu:585-588
+
+
+def pixel_coverage(px, py, r):
+    """compute_pixel (src/gpu/beamDecomposition.cu:11-104): the area of the unit
+    pixel centred at (px, py) inside the circle of radius r about the origin and
+    that area's centroid.  Pixels further than r + sqrt(2) are out, nearer than
+    r - sqrt(2) in; a pixel with all four corners in (or out) counts whole (or
+    not at all); otherwise the polygon of its inside corners and the circle's
+    crossings of its edges (sorted by angle about the pixel centre, shoelace
+    area and first moments), plus the circular segment beyond the chord when
+    there are two crossings.  Float arithmetic as the reference's."""
+    f = F32
+    px, py, r = f(px), f(py), f(r)
+    r2 = f(r * r)
+    d2 = f(f(px * px) + f(py * py))
+    s2 = f(math.sqrt(2.0))
+    if d2 > f(f(r + s2) * f(r + s2)):
+        return f(0), px, py
+    if d2 < f(f(r - s2) * f(r - s2)):
+        return f(1), px, py
+    x0, x1, y0, y1 = f(px - f(0.5)), f(px + f(0.5)), f(py - f(0.5)), f(py + f(0.5))
+    inside = [f(f(x0 * x0) + f(y0 * y0)) < r2, f(f(x1 * x1) + f(y0 * y0)) < r2,
+              f(f(x1 * x1) + f(y1 * y1)) < r2, f(f(x0 * x0) + f(y1 * y1)) < r2]
+    n_in = sum(inside)
+    if n_in == 4:
+        return f(1), px, py
+    if n_in == 0:
+        return f(0), px, py
+    eps = f(1e-5)
+    ints = []
+
+    def dup(x, y):
+        return any(abs(f(a - x)) < eps and abs(f(b - y)) < eps for a, b in ints)
+
+    for x in (x0, x1):                   # crossings of the vertical edges
+        val = f(f(r - x) * f(r + x))
+        if val >= -eps:
+            y = f(math.sqrt(max(val, f(0))))
+            if f(y0 - eps) <= y <= f(y1 + eps) and not dup(x, y):
+                ints.append((x, y))
+            if len(ints) < 8 and y > eps and f(y0 - eps) <= -y <= f(y1 + eps) and not dup(x, -y):
+                ints.append((x, -y))
+    for y in (y0, y1):                   # crossings of the horizontal edges
+        val = f(f(r - y) * f(r + y))
+        if val >= -eps:
+            x = f(math.sqrt(max(val, f(0))))
+            if f(x0 - eps) <= x <= f(x1 + eps) and not dup(x, y):
+                ints.append((x, y))
+            if len(ints) < 8 and x > eps and f(x0 - eps) <= -x <= f(x1 + eps) and not dup(-x, y):
+                ints.append((-x, y))
+    corners = [(x0, y0), (x1, y0), (x1, y1), (x0, y1)]
+    verts = [c for c, k in zip(corners, inside) if k] + ints
+    nc = len(verts)
+    if nc < 3:
+        return f(1 if n_in > 0 else 0), px, py
+    idx = list(range(nc))
+    ang = [f(math.atan2(f(v[1] - py), f(v[0] - px))) for v in verts]
+    for i in range(nc - 1):              # the reference's exchange sort by angle
+        for j in range(i + 1, nc):
+            if ang[idx[i]] > ang[idx[j]]:
+                idx[i], idx[j] = idx[j], idx[i]
+    A = Mx = My = f(0)
+    for i in range(nc):
+        p1, p2 = verts[idx[i]], verts[idx[(i + 1) % nc]]
+        cross = float(p1[0]) * float(p2[1]) - float(p2[0]) * float(p1[1])
+        A = f(float(A) + cross)
+        Mx = f(float(Mx) + float(f(p1[0] + p2[0])) * cross)
+        My = f(float(My) + float(f(p1[1] + p2[1])) * cross)
+    A, Mx, My = f(A * f(0.5)), f(Mx / f(6)), f(My / f(6))
+    if A < 0:
+        A, Mx, My = -A, -Mx, -My
+    if len(ints) == 2:                   # the circular segment beyond the chord
+        mx, my = f(f(ints[0][0] + ints[1][0]) * f(0.5)), f(f(ints[0][1] + ints[1][1]) * f(0.5))
+        dxc, dyc = f(ints[0][0] - ints[1][0]), f(ints[0][1] - ints[1][1])
+        L = f(math.sqrt(f(f(dxc * dxc) + f(dyc * dyc))))
+        h = f(math.sqrt(f(f(mx * mx) + f(my * my))))
+        th = f(f(2) * f(math.atan2(f(f(0.5) * L), h)))
+        if th < f(1e-4):
+            t2 = f(th * th)
+            t3 = f(t2 * th)
+            t5 = f(t3 * t2)
+            tms = f(f(t3 / f(6)) - f(t5 / f(120)))
+            sh = f(f(0.5) * th)
+            shc = f(f(sh * sh) * sh)
+        else:
+            tms = f(th - f(math.sin(th)))
+            shc = f(f(math.sin(f(f(0.5) * th))) ** 3)
+        As = f(f(f(0.5) * r2) * tms)
+        ds = f(f(f(f(4) * r) * shc) / f(f(3) * tms)) if tms > f(1e-10) else r
+        nrm = h if h > f(1e-9) else f(1)
+        ux, uy = f(mx / nrm), f(my / nrm)
+        A, Mx, My = f(A + As), f(Mx + f(f(As * ds) * ux)), f(My + f(f(As * ds) * uy))
+    if A > f(1e-9):
+        return A, f(Mx / A), f(My / A)
+    return A, px, py
+
+
+def zernike_table(pd):
+    """Per pixel of the pd x pd crop (x the fast index, y the slow one): the
+    covered fraction of the pixel in the disk of radius pd/2 about ((pd-1)/2,
+    (pd-1)/2), the centroid's radius over pd/2 (clamped to 1) and its angle
+    atan2(dy, dx) (beamDecomposition.cu:356-368, 521-530)."""
+    c = F32((pd - 1) / 2)
+    rad = F32(pd / 2)
+    frac = np.zeros((pd, pd), F32)
+    rho = np.ones((pd, pd), F32)
+    th = np.zeros((pd, pd), F32)
+    for y in range(pd):
+        for x in range(pd):
+            a, cx, cy = pixel_coverage(F32(x - c), F32(y - c), rad)
+            frac[y, x] = a
+            if a > F32(2e-20):
+                rho[y, x] = min(F32(F32(math.sqrt(F32(F32(cx * cx) + F32(cy * cy)))) / rad), F32(1))
+                th[y, x] = F32(math.atan2(cy, cx))
+    return frac, rho, th
+
+
+def zernike_modes(rho, th, weight):
+    """The real Zernike basis in the reference's mode order (m = 0 .. maxN, n = m,
+    m+2, .. maxN; cos then sin for m > 0): the radial polynomials by the
+    three-term recurrence from weight * rho^m, normalised by sqrt(n+1) (m = 0)
+    or sqrt(2(n+1)).  Returns an array [nmodes, ...] (float64)."""
+    rho = rho.astype(np.float64)
+    out = []
+    rp = weight.astype(np.float64)
+    for m in range(ZERNIKE_MAX_N + 1):
+        cm, sm = np.cos(m * th.astype(np.float64)), np.sin(m * th.astype(np.float64))
+        r2 = r4 = None
+        for n in range(m, ZERNIKE_MAX_N + 1, 2):
+            if n == m:
+                cur = rp
+            elif n == m + 2:
+                cur = r2 * ((m + 2) * rho * rho - (m + 1))
+            else:
+                k1 = 0.5 * (n + m) * (n - m) * (n - 2.0)
+                k2 = 2.0 * n * (n - 1.0) * (n - 2.0)
+                k3 = -m * m * (n - 1.0) - n * (n - 1.0) * (n - 2.0)
+                k4 = -0.5 * n * (n + m - 2.0) * (n - m - 2.0)
+                cur = ((k2 * rho * rho + k3) * r2 + k4 * r4) / k1
+            r4, r2 = r2, cur
+            nz = cur * (math.sqrt(n + 1.0) if m == 0 else math.sqrt(2.0 * (n + 1.0)))
+            if m == 0:
+                out.append(nz)
+            else:
+                out.append(nz * cm)
+                out.append(nz * sm)
+        rp = rp * rho
+    return np.stack(out)
+
+
+def zernike_regularize(coef):
+    """regularize_zernike_coefficients (beamDecomposition.cu:480-513) as zernike_compute
+    launches it, with max_l = the number of modes (861): modes 0..430 get p = 2 * mode,
+    m = 0, modes 431..860 m = 1, p = 1 + 2 ((mode - 431) // 2); each coefficient is
+    soft-thresholded by 5e-5 p^2 + 5e-8 m^2 (zero below 1e-9 in modulus)."""
+    nm = coef.shape[0]
+    out = np.zeros(nm, C64)
+    half = nm >> 1
+    for mode in range(nm):
+        if mode <= half:
+            p, m = 2 * mode, 0
+        elif nm % 2 == 1 and mode < (nm + 1) * 3 // 2:
+            m, p = 1, 1 + (((mode - half - 1) >> 1) << 1)
+        else:
+            raise ValueError("mode outside the two branches the launch reaches")
+        factor = F32(F32(F32(ZERNIKE_REG_L * F32(p)) * F32(p)) + F32(F32(ZERNIKE_REG_M * F32(m)) * F32(m)))
+        c = np.complex64(coef[mode])
+        mag = F32(abs(c))
+        sc = max(F32(0), F32(F32(1) - F32(factor / mag))) if mag > F32(1e-9) else F32(0)
+        out[mode] = np.complex64(complex(F32(c.real * sc), F32(c.imag * sc)))
+    return out
+
+
+def zernike_fit(crop):
+    """zernike_compute + zernike_reconstruct of util/ptycho.cpp:619-622 on the pd x pd
+    crop: coefficients = sum over pixels of crop * coverage * Z_k (at the coverage
+    centroid) / (pi (pd/2)^2), regularised, and the crop replaced by sum_k c_k Z_k
+    on the pixels the disk touches (zero elsewhere; beamDecomposition.cu:339-608)."""
+    pd = crop.shape[0]
+    frac, rho, th = zernike_table(pd)
+    live = frac > F32(2e-20)
+    Z = zernike_modes(np.where(live, rho, 1), th, np.where(live, frac, 0))
+    rad = np.float64(F32(pd / 2))
+    coef = (Z.reshape(Z.shape[0], -1) @ crop.astype(np.complex128).reshape(-1)) / (math.pi * rad * rad)
+    coef = zernike_regularize(coef.astype(C64))
+    th0 = np.where(rho > F32(2e-20), th, F32(0))
+    B = zernike_modes(rho, th0, np.ones_like(rho))
+    rec = np.tensordot(coef.astype(np.complex128), B, axes=1)
+    return np.where(frac >= F32(2e-20), rec, 0).astype(C64)
+
+
 # ------------------------------------------------- ptycho::iterate and set-up
 @dataclass
 class PtyParams:
@@ -382,9 +576,6 @@ def iterate(obj0, probe0, patterns, scanx, scany, n_iter, params: PtyParams, ord
     orow, ocol = obj0.shape
     if start_iter + n_iter > POSITION_UPDATE_ITER and params.position_uncertainty > 0:
         raise ValueError("position refinement (iterations >= 500, positionUncertainty > 0) is outside this restatement")
-    for it in range(start_iter, start_iter + n_iter):
-        if it >= UPDATE_PROBE_ITER and it < params.zernike_iter and it % 10 == 0:
-            raise ValueError("the Zernike pupil fit (zernikeIter > 400) is outside this restatement")
     O = obj0.astype(C64).copy()
     Oprev = np.zeros_like(O)
     P = probe0.astype(C64).copy()
@@ -417,6 +608,7 @@ def iterate(obj0, probe0, patterns, scanx, scany, n_iter, params: PtyParams, ord
             O = (O * sf).astype(C64)
             Oprev = (Oprev * sf).astype(C64)
             P = (P * F32(1.0 / np.float64(sf))).astype(C64)
+            Pprev = (Pprev * F32(1.0 / np.float64(sf))).astype(C64)     # util/ptycho.cpp:507
             obj_max = probe_max = F32(math.sqrt(np.float64(F32(obj_max * probe_max))))
         for i in orders[it - start_iter]:
             sx, sy = wins[i]
@@ -440,7 +632,10 @@ def iterate(obj0, probe0, patterns, scanx, scany, n_iter, params: PtyParams, ord
             step = (step * F32(0)).astype(C64)
             P = angular_spectrum(P, params.lam, params.dpupil, res, reverse=True)
             r0, c0 = (rows - pd) // 2, (cols - pd) // 2
-            crop = P[r0:r0 + pd, c0:c0 + pd] * (pupil_support > F32(0.5))
+            if it < params.zernike_iter and it % 10 == 0:    # dozernike (util/ptycho.cpp:619-621)
+                crop = zernike_fit(P[r0:r0 + pd, c0:c0 + pd])
+            else:
+                crop = P[r0:r0 + pd, c0:c0 + pd] * (pupil_support > F32(0.5))
             P = np.zeros_like(P)
             P[r0:r0 + pd, c0:c0 + pd] = crop
             P = angular_spectrum(P, params.lam, params.dpupil, res, reverse=False)

@@ -2,9 +2,15 @@
 // hot-path sources as plain C++ (test infrastructure: the oracle pin).
 // Kernels become host functions; a launch runs the body once per thread of
 // the grid, with blockIdx/threadIdx/blockDim/gridDim as thread-local globals.
-// Only element-wise kernels (no __syncthreads) are ever executed this way.
+// Element-wise kernels run this way; kernels that synchronise their block
+// (__syncthreads over extern shared memory) are launched through
+// cdxref::coop, which runs each block's threads as OS threads, blocks in turn.
 #pragma once
 #include <algorithm>
+#include <condition_variable>
+#include <mutex>
+#include <thread>
+#include <vector>
 #include <cmath>
 #include <cstddef>
 #include <cstdint>
@@ -51,12 +57,63 @@ struct Launch {
     return true;
   }
 };
+// __syncthreads of a cooperative block: a generation-counted barrier; a thread
+// that returns leaves the count
+struct BlockBarrier {
+  std::mutex m;
+  std::condition_variable cv;
+  int expected = 0, arrived = 0;
+  long gen = 0;
+  void wait() {
+    std::unique_lock<std::mutex> l(m);
+    const long g = gen;
+    if (++arrived == expected) { arrived = 0; ++gen; cv.notify_all(); return; }
+    cv.wait(l, [&] { return gen != g; });
+  }
+  void drop() {
+    std::unique_lock<std::mutex> l(m);
+    if (--expected > 0 && arrived == expected) { arrived = 0; ++gen; cv.notify_all(); }
+  }
+};
+extern thread_local BlockBarrier* tl_block_barrier;
+template <class F> struct Coop {
+  dim3 g, b;
+  F f;
+  template <class... A> void operator()(A... a) const {
+    const unsigned nt = b.x * b.y * b.z;
+    for (unsigned bz = 0; bz < g.z; ++bz)
+      for (unsigned by = 0; by < g.y; ++by)
+        for (unsigned bx = 0; bx < g.x; ++bx) {
+          BlockBarrier bar;
+          bar.expected = (int)nt;
+          std::vector<std::thread> th;
+          th.reserve(nt);
+          for (unsigned t = 0; t < nt; ++t)
+            th.emplace_back([&, t] {
+              gridDim = g;
+              blockDim = b;
+              blockIdx = {bx, by, bz};
+              threadIdx = {t % b.x, (t / b.x) % b.y, t / (b.x * b.y)};
+              tl_block_barrier = &bar;
+              f(a...);
+              tl_block_barrier = nullptr;
+              bar.drop();
+            });
+          for (auto& x : th) x.join();
+        }
+  }
+};
+template <class F> Coop<F> coop(dim3 g, dim3 b, F f) { return {g, b, f}; }
+template <class F> Coop<F> coop(dim3 g, dim3 b, size_t, F f) { return {g, b, f}; }
 }  // namespace cdxref
 
-inline void __syncthreads() {}
+inline void __syncthreads() {
+  if (cdxref::tl_block_barrier) cdxref::tl_block_barrier->wait();
+}
 template <class A, class B> inline auto max(A a, B b) -> decltype(a + b) { return a > b ? a : b; }
 template <class A, class B> inline auto min(A a, B b) -> decltype(a + b) { return a < b ? a : b; }
 inline float __fdividef(float a, float b) { return a / b; }
+inline float __fmaf_rn(float a, float b, float c) { return std::fma(a, b, c); }
 inline float __expf(float a) { return std::exp(a); }
 inline float __logf(float a) { return std::log(a); }
 inline float __sinf(float a) { return std::sin(a); }

@@ -18,6 +18,7 @@
 
 thread_local uint3_t blockIdx, threadIdx;
 thread_local dim3 blockDim, gridDim;
+thread_local cdxref::BlockBarrier* cdxref::tl_block_barrier = nullptr;
 std::map<int, cdxref_plan>& cdxref_plans() { static std::map<int, cdxref_plan> m; return m; }
 float tile[1];   // the extern __shared__ tile of applyConvolution (never launched here)
 

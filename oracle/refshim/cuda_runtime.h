@@ -8,7 +8,10 @@ enum cudaMemcpyKind { cudaMemcpyHostToHost, cudaMemcpyHostToDevice, cudaMemcpyDe
                       cudaMemcpyDefault };
 typedef void* cudaStream_t;
 inline const char* cudaGetErrorString(int) { return "cuda error (host emulation)"; }
-inline cudaError_t cudaMalloc(void** p, size_t n) { *p = calloc(n ? n : 1, 1); return *p ? 0 : 2; }
+// sizes rounded up to 512 bytes like the device allocator's blocks: the reference's
+// regularize_zernike_coefficients (beamDecomposition.cu:480-513) touches its whole
+// last thread block of modes, past the coefficients' end but inside that rounding
+inline cudaError_t cudaMalloc(void** p, size_t n) { *p = calloc((n + 511) / 512 * 512 + (n ? 0 : 512), 1); return *p ? 0 : 2; }
 template <class T> inline cudaError_t cudaMalloc(T** p, size_t n) { return cudaMalloc((void**)p, n); }
 inline cudaError_t cudaFree(void* p) { free(p); return 0; }
 inline cudaError_t cudaMemset(void* p, int v, size_t n) { memset(p, v, n); return 0; }

@@ -1,7 +1,8 @@
 """Generate the golden fixtures of the ptychography path from the reference's own code.
 
 Builds the reference's ptychography driver (util/ptycho.cpp with
-src/gpu/ptycho.cu, cudaConfig.cu, cdi.cu, src/post_gpu/propagator.cc, misc.cc)
+src/gpu/ptycho.cu, beamDecomposition.cu, cudaConfig.cu, cdi.cu,
+src/post_gpu/propagator.cc, FISTA.cc, misc.cc)
 as host code with oracle/build_ref.sh, runs ptycho::iterate on seeded
 synthetic 32x32-probe / 64x64-object cases (inputs made by the oracle's
 restatement of pupilFunc, the angular-spectrum propagator and the noise-free
@@ -44,9 +45,12 @@ CASES = [
     ("noise2003", 2003, 0, 0, 5, 1.0, 40.0, "grid", 7),
     ("fista45", 45, 1, 0, 5, 1.0, 40.0, "grid", 7),
     ("fista405", 405, 0, 0, 5, 1.0, 40.0, "grid", 3),
+    ("zernike412", 412, 0, 0, 5, 1.0, 40.0, "grid", 3),
+    ("zernike412_mpie", 412, 1, 0, 5, 1.0, 40.0, "grid", 7),
 ]
 NOISE_LEVEL = {"noise2003": 20}
-ZERNIKE_ITER = {"fista45": 35, "fista405": 300}   # FISTA object step (and the probe momentum every 10)
+# FISTA object step (and the probe momentum every 10); from 400 the Zernike pupil fit every 10
+ZERNIKE_ITER = {"fista45": 35, "fista405": 300, "zernike412": 1200, "zernike412_mpie": 1200}
 OPTICS = dict(lam=0.5, d=2e4, dpupil=1e3, pixelsize=20.0, pupil_size=16.0)
 
 

@@ -51,15 +51,21 @@ def test_gpu_draws_the_reference_orders_from_the_seed(PT):
         assert np.array_equal(a.objectWave, b.objectWave)
 
 
-@pytest.mark.parametrize("first", [0, 7, 10, 400, 450, 520, 2000])
+# (first iteration, zernikeIter): FISTA step (and the probe momentum at 10) in the
+# object phase; from 400 the pupil disk, or the Zernike pupil fit at 400, 410, 2010
+SWEEPS = [(0, 400), (7, 400), (10, 400), (400, 0), (400, 1200), (410, 1200), (411, 1200), (450, 0), (520, 0),
+          (2000, 0), (2010, 2100)]
+
+
+@pytest.mark.parametrize("first,zernike_iter", SWEEPS)
 @pytest.mark.parametrize("mpie", [False, True])
-def test_one_sweep_matches_oracle(PT, first, mpie):
+def test_one_sweep_matches_oracle(PT, first, zernike_iter, mpie):
     """Per-iterate parity: one sweep (object phase, or probe phase from 400) from
     the same object and probe as the oracle."""
     c, prm, _n, _s = load("obj3")
     prm.mpie = mpie
     prm.noise_level = 20   # the noise-tolerant projection from iteration 2000
-    prm.zernike_iter = 400 if first < 400 else 0   # FISTA step (and the probe momentum at 10) in the object phase
+    prm.zernike_iter = zernike_iter
     rng = np.random.default_rng(first)
     obj = (c["obj0"] * (0.5 + rng.random(c["obj0"].shape))).astype(np.complex64)
     orders = np.array([rng.permutation(len(c["scanx"]))], np.int32)
@@ -105,6 +111,36 @@ def test_large_sweep_matches_oracle_and_reconstructs(PT):
         assert e1 < 0.5 * e0, (e0, e1)
 
 
+def test_zernike_sweep_at_the_reference_pupil_ratio(PT):
+    """One Zernike sweep (iteration 410, zernikeIter 1200, mPIE) on a 128^2 probe with
+    an 84-pixel pupil (about the reference configuration's 335 of 512) against the
+    oracle, and the fitted pupil differs from the disk-cut one."""
+    R, RO = 128, 256
+    prm = PO.PtyParams(lam=0.5, d=5e4, dpupil=1e3, pixelsize=20.0, pupil_size=84.0, exposure=1.0, mpie=True,
+                       zernike_iter=1200)
+    res = prm.resolution(R)
+    rng = np.random.default_rng(8)
+    x = np.linspace(-1, 1, RO)[:, None]
+    y = np.linspace(-1, 1, RO)[None, :]
+    truth = ((0.7 + 0.3 * np.cos(4 * x) * np.sin(3 * y)) * np.exp(1j * np.sin(3 * x + y))).astype(np.complex64)
+    probe = PO.angular_spectrum(PO.pupil_func(R, R, prm.pupil_size), prm.lam, prm.dpupil, res)
+    sx = np.array([30 + 40 * i + 0.4 * j for i in range(3) for j in range(3)], np.float32)
+    sy = np.array([30 + 40 * j + 0.7 * i for i in range(3) for j in range(3)], np.float32)
+    pats = PO.simulate_patterns(truth, probe, sx, sy)
+    pats = (pats / pats.max() * 0.9).astype(np.float32)
+    obj0 = (truth * np.exp(0.3j * rng.random((RO, RO)))).astype(np.complex64)
+    c = {"obj0": obj0, "probe0": probe, "pats": pats, "scanx": sx, "scany": sy}
+    orders = PO.scan_orders(9, 1, 4)
+    with make(PT, c, prm) as t:
+        t.iterate(1, first_iter=410, orders=orders)
+        O, pupil, P = PO.iterate(obj0, probe, pats, sx, sy, 1, prm, orders, start_iter=410)
+        assert PO.rel_err(t.objectWave, O) < STEP_BOUND
+        assert PO.rel_err(t.probe, P) < STEP_BOUND
+        prm.zernike_iter = 0
+        _O, _pu, Pdisk = PO.iterate(obj0, probe, pats, sx, sy, 1, prm, orders, start_iter=410)
+        assert PO.rel_err(t.probe, Pdisk) > 100 * STEP_BOUND
+
+
 def test_simulate_matches_oracle(PT):
     c, prm, _n, _s = load("offedge")
     with make(PT, c, prm) as t:
@@ -139,9 +175,8 @@ def test_argument_checks(PT, cdx):
     prm.position_uncertainty = 0.0
     prm.zernike_iter = 1200
     with make(PT, c, prm) as t:
-        t.iterate(5)                               # FISTA steps in the object phase run
-        with pytest.raises(cdx.CdxError):
-            t.iterate(5, first_iter=400)           # the Zernike pupil fit from 400 is not built
+        t.iterate(5)                               # FISTA steps in the object phase
+        t.iterate(5, first_iter=400)               # the Zernike pupil fit at 400
         bad = c["orders"][:2].copy()
         bad[0, 0] = 99
         with pytest.raises(cdx.CdxError):

@@ -11,7 +11,7 @@ from oracle import ptycho_oracle as PO
 
 GOLD = Path(__file__).resolve().parent / "golden" / "ptycho_cases.npz"
 CASES = ["obj3", "obj20_nompie", "obj30", "beamstop", "saturated", "offedge", "probe402", "refine520", "noise2003",
-         "fista45", "fista405"]
+         "fista45", "fista405", "zernike412", "zernike412_mpie"]
 # Relative L2 bounds of oracle (and GPU) against the reference's run.  Short
 # runs agree to float32 rounding; along long runs the rounding differences of
 # two FFTs grow (momentum and the probe phase amplify them): measured oracle
@@ -23,7 +23,8 @@ CASES = ["obj3", "obj20_nompie", "obj30", "beamstop", "saturated", "offedge", "p
 # positionUncertainty = 0) 2.0e-5 / 1.6e-5; 2003 sweeps, the last three with
 # the noise-tolerant projection (noiseLevel 20), 1.4e-3 / 9.2e-4.
 # With zernikeIter (FISTA object step each sweep, probe momentum every tenth):
-# 45 sweeps with momentum 1.1e-6, 405 sweeps without 7.4e-7.
+# 45 sweeps with momentum 1.1e-6, 405 sweeps without 7.4e-7; 412 sweeps, the Zernike
+# pupil fit at 400 and 410, without momentum 4.1e-7 / 6.7e-7, with it 2.1e-6 / 8.2e-7.
 OBJ_BOUND = {"obj30": 2e-4, "probe402": 3e-3, "refine520": 2e-4, "noise2003": 5e-3, "fista45": 1e-5,
              "fista405": 1e-5}
 PUPIL_BOUND = {"probe402": 1e-4, "refine520": 2e-4, "noise2003": 5e-3}
