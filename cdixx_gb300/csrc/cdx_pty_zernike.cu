@@ -6,14 +6,18 @@
 //
 // Device layout: a per-pixel table of the crop (covered fraction of the pixel in
 // the disk of radius pd/2, the radius and angle of the covered part's centroid)
-// built once per context; per sweep three launches:
-//   k_zk_project   one pixel per thread, per mode a warp reduction, the CTA's
-//                  four warps summed into one partial row [CTA][mode]
-//   k_zk_finish    per mode the partial rows summed in double, scaled by
-//                  1/(pi (pd/2)^2) and soft-thresholded
+// built once per context, and the recurrence coefficients of the 441 radial
+// polynomials in constant memory; per sweep three launches:
+//   k_zk_project   four pixels per thread, per mode a warp reduction, the CTA's
+//                  four warps summed into one partial per (mode, CTA)
+//   k_zk_finish    one warp per mode sums its CTAs' partials in double, scales
+//                  by 1/(pi (pd/2)^2) and soft-thresholds
 //   k_zk_rebuild   the probe rewritten: the coefficients' sum inside the crop on
 //                  the pixels the disk touches, zero elsewhere (crop, pad)
 #include <cuda_runtime.h>
+
+#include <cmath>
+#include <vector>
 
 #include "cdx_pty_zernike.cuh"
 
@@ -22,6 +26,15 @@ namespace {
 
 constexpr int kZkThreads = 128;
 constexpr int kZkWarps = kZkThreads / 32;
+constexpr int kZkPix = 4;                                      // pixels per projection thread
+constexpr int kZkRadial = (kZkMaxN / 2 + 1) * (kZkMaxN / 2 + 2) - (kZkMaxN / 2 + 1);   // 441 (m, n) pairs
+
+// radial step (m, n) in mode order: R_n^m = (a rho^2 + b) R_{n-2}^m + c R_{n-4}^m, basis
+// value R_n^m * nrm (nrm = sqrt(n+1) for m = 0, sqrt(2 (n+1)) otherwise)
+struct ZkStep {
+  float a, b, c, nrm;
+};
+__constant__ ZkStep c_zk[kZkRadial];
 
 struct Cover {
   float a, cx, cy;
@@ -144,41 +157,44 @@ __global__ void k_zk_table(float4* __restrict__ tab, int pd) {
 }
 
 // Visits the 861 modes in the reference's order (m = 0 .. 40; n = m, m+2 .. 40;
-// cos then sin for m > 0) with the radial polynomial R_n^m(rho) * weight from
-// the three-term recurrence in n, normalised by sqrt(n+1) (m = 0) or
-// sqrt(2 (n+1)); f(mode, value) receives the basis value at the pixel.
-template <class F>
-__device__ __forceinline__ void zk_modes(float rho, float th, float weight, F&& f) {
-  int mode = 0;
-  float rp = weight;   // weight * rho^m
+// cos then sin for m > 0) for P pixels at once: the radial polynomial times the
+// pixel's weight from weight * rho^m by the three-term recurrence in n, times the
+// normalisation; f(mode, z[P]) receives the basis values.
+template <int P, class F>
+__device__ __forceinline__ void zk_walk(const float (&rho)[P], const float (&th)[P], const float (&wt)[P], F&& f) {
+  float rp[P], rr[P];
+#pragma unroll
+  for (int p = 0; p < P; ++p) {
+    rp[p] = wt[p];
+    rr[p] = rho[p] * rho[p];
+  }
+  int mode = 0, j = 0;
   for (int m = 0; m <= kZkMaxN; ++m) {
-    float cm = 1.f, sm = 0.f;
-    if (m > 0) sincosf(m * th, &sm, &cm);
-    float r2 = 0.f, r4 = 0.f;
-    for (int n = m; n <= kZkMaxN; n += 2) {
-      float cur;
-      if (n == m) {
-        cur = rp;
-      } else if (n == m + 2) {
-        cur = r2 * ((m + 2) * rho * rho - (m + 1));
-      } else {
-        const float k1 = 0.5f * (n + m) * (n - m) * (n - 2.f);
-        const float k2 = 2.f * n * (n - 1.f) * (n - 2.f);
-        const float k3 = -m * m * (n - 1.f) - n * (n - 1.f) * (n - 2.f);
-        const float k4 = -0.5f * n * (n + m - 2.f) * (n - m - 2.f);
-        cur = ((k2 * rho * rho + k3) * r2 + k4 * r4) / k1;
-      }
-      r4 = r2;
-      r2 = cur;
-      const float z = cur * (m == 0 ? sqrtf(n + 1.f) : sqrtf(2.f * (n + 1.f)));
-      if (m == 0) {
-        f(mode++, z);
-      } else {
-        f(mode++, z * cm);
-        f(mode++, z * sm);
-      }
+    float cm[P], sm[P], r2[P], r4[P];
+#pragma unroll
+    for (int p = 0; p < P; ++p) {
+      cm[p] = 1.f;
+      sm[p] = 0.f;
+      if (m > 0) sincosf(m * th[p], &sm[p], &cm[p]);
+      r2[p] = r4[p] = 0.f;
     }
-    rp *= rho;
+    for (int n = m; n <= kZkMaxN; n += 2, ++j) {
+      const ZkStep s = c_zk[j];
+      float zc[P], zs[P];
+#pragma unroll
+      for (int p = 0; p < P; ++p) {
+        const float cur = n == m ? rp[p] : fmaf(fmaf(s.a, rr[p], s.b), r2[p], s.c * r4[p]);
+        r4[p] = r2[p];
+        r2[p] = cur;
+        const float z = cur * s.nrm;
+        zc[p] = z * cm[p];
+        zs[p] = z * sm[p];
+      }
+      f(mode++, zc);
+      if (m > 0) f(mode++, zs);
+    }
+#pragma unroll
+    for (int p = 0; p < P; ++p) rp[p] *= rho[p];
   }
 }
 
@@ -187,15 +203,28 @@ __global__ void __launch_bounds__(kZkThreads) k_zk_project(const float2* __restr
                                                             float2* __restrict__ part) {
   __shared__ float2 acc[kZkWarps][kZkModes];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int g = blockIdx.x * kZkThreads + threadIdx.x;
-  float4 e = make_float4(0.f, 1.f, 0.f, 0.f);
-  float2 v = make_float2(0.f, 0.f);
-  if (g < pd * pd) {
-    e = tab[g];
-    if (e.x > 0.f) v = P[(long long)(r0 + g / pd) * cols + c0 + g % pd];
+  float rho[kZkPix], th[kZkPix], wt[kZkPix];
+  float2 v[kZkPix];
+#pragma unroll
+  for (int p = 0; p < kZkPix; ++p) {
+    const int g = (blockIdx.x * kZkPix + p) * kZkThreads + threadIdx.x;
+    float4 e = make_float4(0.f, 1.f, 0.f, 0.f);
+    v[p] = make_float2(0.f, 0.f);
+    if (g < pd * pd) {
+      e = tab[g];
+      if (e.x > 0.f) v[p] = P[(long long)(r0 + g / pd) * cols + c0 + g % pd];
+    }
+    wt[p] = e.x;
+    rho[p] = e.y;
+    th[p] = e.z;
   }
-  zk_modes(e.y, e.z, e.x, [&](int k, float z) {
-    float re = v.x * z, im = v.y * z;
+  zk_walk<kZkPix>(rho, th, wt, [&](int k, const float (&z)[kZkPix]) {
+    float re = 0.f, im = 0.f;
+#pragma unroll
+    for (int p = 0; p < kZkPix; ++p) {
+      re = fmaf(v[p].x, z[p], re);
+      im = fmaf(v[p].y, z[p], im);
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       re += __shfl_xor_sync(0xffffffffu, re, o);
@@ -211,7 +240,7 @@ __global__ void __launch_bounds__(kZkThreads) k_zk_project(const float2* __restr
       s.x += acc[w][k].x;
       s.y += acc[w][k].y;
     }
-    part[(long long)blockIdx.x * kZkModes + k] = s;
+    part[(long long)k * gridDim.x + blockIdx.x] = s;
   }
 }
 
@@ -221,14 +250,20 @@ __global__ void __launch_bounds__(kZkThreads) k_zk_project(const float2* __restr
 // thresholded as (p, m) = (2k, 0) and mode k > 430 as (1 + 2 ((k - 431) / 2), 1);
 // c *= max(0, 1 - (5e-5 p^2 + 5e-8 m^2) / |c|), zero for |c| <= 1e-9.
 __global__ void k_zk_finish(const float2* __restrict__ part, int nblk, double norm, float2* __restrict__ coef) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (k >= kZkModes) return;
   double sx = 0, sy = 0;
-  for (int b = 0; b < nblk; ++b) {
-    const float2 p = part[(long long)b * kZkModes + k];
+  for (int b = lane; b < nblk; b += 32) {
+    const float2 p = part[(long long)k * nblk + b];
     sx += p.x;
     sy += p.y;
   }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    sx += __shfl_xor_sync(0xffffffffu, sx, o);
+    sy += __shfl_xor_sync(0xffffffffu, sy, o);
+  }
+  if (lane) return;
   const float cx = (float)(sx * norm), cy = (float)(sy * norm);
   const int half = kZkModes >> 1;
   int p, m;
@@ -258,10 +293,10 @@ __global__ void k_zk_rebuild(float2* __restrict__ P, int rows, int cols, int r0,
     if (x >= 0 && x < pd && y >= 0 && y < pd) {
       const float4 e = tab[x * pd + y];
       if (e.w > 0.f) {
-        const float th = e.y > 2e-20f ? e.z : 0.f;
-        zk_modes(e.y, th, 1.f, [&](int k, float z) {
-          out.x += cs[k].x * z;
-          out.y += cs[k].y * z;
+        const float rho[1] = {e.y}, th[1] = {e.y > 2e-20f ? e.z : 0.f}, one[1] = {1.f};
+        zk_walk<1>(rho, th, one, [&](int k, const float (&z)[1]) {
+          out.x = fmaf(cs[k].x, z[0], out.x);
+          out.y = fmaf(cs[k].y, z[0], out.y);
         });
       }
     }
@@ -271,9 +306,34 @@ __global__ void k_zk_rebuild(float2* __restrict__ P, int rows, int cols, int r0,
 
 }  // namespace
 
-int zk_blocks(int pd) { return (pd * pd + kZkThreads - 1) / kZkThreads; }
+int zk_blocks(int pd) { return (pd * pd + kZkThreads * kZkPix - 1) / (kZkThreads * kZkPix); }
 
 cudaError_t zk_table(float4* tab, int pd, cudaStream_t st) {
+  // the recurrence of R_n^m in n (k1 R_n = (k2 rho^2 + k3) R_{n-2} + k4 R_{n-4}, the
+  // coefficients of beamDecomposition.cu:162-176) divided through by k1, in double
+  static const std::vector<ZkStep> steps = [] {
+    std::vector<ZkStep> v;
+    for (int m = 0; m <= kZkMaxN; ++m)
+      for (int n = m; n <= kZkMaxN; n += 2) {
+        ZkStep s{0.f, 0.f, 0.f, (float)std::sqrt(m == 0 ? n + 1.0 : 2.0 * (n + 1))};
+        if (n == m + 2) {
+          s.a = (float)(m + 2);
+          s.b = (float)(-(m + 1));
+        } else if (n > m + 2) {
+          const double k1 = 0.5 * (n + m) * (n - m) * (n - 2.0), k2 = 2.0 * n * (n - 1.0) * (n - 2.0);
+          const double k3 = -double(m) * m * (n - 1.0) - n * (n - 1.0) * (n - 2.0);
+          const double k4 = -0.5 * n * (n + m - 2.0) * (n - m - 2.0);
+          s.a = (float)(k2 / k1);
+          s.b = (float)(k3 / k1);
+          s.c = (float)(k4 / k1);
+        }
+        v.push_back(s);
+      }
+    return v;
+  }();
+  cudaError_t e = cudaMemcpyToSymbolAsync(c_zk, steps.data(), sizeof(ZkStep) * steps.size(), 0,
+                                          cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return e;
   k_zk_table<<<(pd * pd + 127) / 128, 128, 0, st>>>(tab, pd);
   return cudaGetLastError();
 }
@@ -284,7 +344,7 @@ cudaError_t zk_fit(float2* P, int rows, int cols, int pd, const float4* tab, flo
   const int nblk = zk_blocks(pd);
   k_zk_project<<<nblk, kZkThreads, 0, st>>>(P, cols, r0, c0, pd, tab, part);
   const float rad = (float)pd / 2;
-  k_zk_finish<<<(kZkModes + 127) / 128, 128, 0, st>>>(part, nblk, 1. / (M_PI * rad * rad), coef);
+  k_zk_finish<<<(kZkModes + 7) / 8, 256, 0, st>>>(part, nblk, 1. / (M_PI * rad * rad), coef);
   const long long n = (long long)rows * cols;
   const int grid = (int)((n + 255) / 256 < 1216 ? (n + 255) / 256 : 1216);
   k_zk_rebuild<<<grid, 256, 0, st>>>(P, rows, cols, r0, c0, pd, tab, coef);
