@@ -153,15 +153,22 @@ using RFirst = RPass<N, PLAN, 0>;
 template <int N, int PLAN>
 using RLast = RPass<N, PLAN, plan_len(N) - 1>;
 
+struct NoHook {
+  __device__ __forceinline__ void operator()() const {}
+};
+
 // The whole transform of the CTA's L lines: `in` holds pass 0's inputs
 // (element j + r*N/R0 of line l for butterfly (l, j)), `out` receives the
 // last pass's outputs (element j + r*NS_last).  The shared lines must be free
 // on entry (callers synchronise); on return other threads may still be
-// reading them, so callers synchronise before the next write.
-template <int N, int PLAN, bool INV>
+// reading them, so callers synchronise before the next write.  `hook` runs
+// after every thread's last read of the shared lines has been issued and before
+// the last pass's arithmetic (a caller that synchronises there may refill the
+// lines while the last pass computes).
+template <int N, int PLAN, bool INV, class H = NoHook>
 __device__ __forceinline__ void rfft(float2 (&in)[RFirst<N, PLAN>::B][RFirst<N, PLAN>::R],
                                      float2 (&out)[RLast<N, PLAN>::B][RLast<N, PLAN>::R], float2* buf,
-                                     const float2* tw, int cb) {
+                                     const float2* tw, int cb, H&& hook = H{}) {
   constexpr int M = plan_len(N);
   rpass_compute_all<N, PLAN, 0, INV>(in, cb, tw);
   if constexpr (M == 1) {
@@ -169,11 +176,13 @@ __device__ __forceinline__ void rfft(float2 (&in)[RFirst<N, PLAN>::B][RFirst<N, 
     for (int b = 0; b < RFirst<N, PLAN>::B; ++b)
 #pragma unroll
       for (int r = 0; r < RFirst<N, PLAN>::R; ++r) out[b][r] = in[b][r];
+    hook();
   } else {
     rpass_store<N, PLAN, 0>(buf, in, cb);
     __syncthreads();
     rfft_middle<N, PLAN, 1, INV>(buf, tw, cb);
     rpass_load<N, PLAN, M - 1>(buf, out, cb);
+    hook();
     rpass_compute_all<N, PLAN, M - 1, INV>(out, cb, tw);
   }
 }
@@ -190,12 +199,22 @@ __device__ __forceinline__ void rfft(float2 (&in)[RFirst<N, PLAN>::B][RFirst<N, 
 #ifndef CDX_RK_MINB_ROW
 #define CDX_RK_MINB_ROW 0
 #endif
+// RHO_IN_BUF: the iterating row pass stages its rho rows in the FFT line buffer
+// itself, copied in after the inverse transform's last shared-memory read (the
+// copy overlaps the last pass's arithmetic), so the CTA needs one line buffer
+// instead of two and four CTAs fit per SM instead of three.
+#ifndef CDX_RHO_IN_BUF
+#define CDX_RHO_IN_BUF 1
+#endif
 template <int N>
 struct RGeom {
   using G = Geom<N>;
-  static constexpr int SMEM_ROW_ITER = G::SMEM_LINES + G::L * G::LD * (int)sizeof(float2) + G::L * ((N + 31) >> 5) * 4;
+  static constexpr bool RHO_IN_BUF = CDX_RHO_IN_BUF && G::T == 256 && plan_len(N) > 1;
+  static constexpr int SMEM_ROW_ITER =
+      G::SMEM_LINES + (RHO_IN_BUF ? 0 : G::L * G::LD * (int)sizeof(float2)) + G::L * ((N + 31) >> 5) * 4;
   static constexpr int MINB_COL = (CDX_RK_MINB_COL > 0 && G::T == 256) ? CDX_RK_MINB_COL : G::MINB;
-  static constexpr int MINB_ROW = (CDX_RK_MINB_ROW > 0 && G::T == 256) ? CDX_RK_MINB_ROW : G::MINB;
+  static constexpr int MINB_ROW =
+      (CDX_RK_MINB_ROW > 0 && G::T == 256) ? CDX_RK_MINB_ROW : (RHO_IN_BUF ? 4 : G::MINB);
 };
 
 // ------------------------------------------------------------- real-space updates
@@ -400,10 +419,12 @@ __device__ __forceinline__ void row_pass_body(const RowArgs& a) {
                                 : (tiled ? min(tl, rfft_cb_max<N>()) : rfft_cb_max<N>());
 
   // rho rows and support words of the CTA (ROW_ITER), landing during the inverse FFT
+  // (RHO_IN_BUF: the rho rows land in the line buffer during its last pass)
   constexpr int RS = G::LD;                 // rho line stride in shared memory
   constexpr int WPR = (N + 31) >> 5;
-  float2* rho_s = smem + L * G::LD;
-  uint32_t* mask_s = reinterpret_cast<uint32_t*>(rho_s + L * RS);
+  constexpr bool rho_in_buf = RGeom<N>::RHO_IN_BUF;
+  float2* rho_s = rho_in_buf ? smem : smem + L * G::LD;
+  uint32_t* mask_s = reinterpret_cast<uint32_t*>(smem + L * G::LD + (rho_in_buf ? 0 : L * RS));
   float2* rho = a.rho + (long long)blockIdx.y * a.rho_stride + (long long)row0 * N;
   // with an even line stride each rho row is one bulk copy (16-byte aligned)
   constexpr bool bulk_rho = bulk_staging<N>() && RS % 2 == 0;
@@ -411,20 +432,25 @@ __device__ __forceinline__ void row_pass_body(const RowArgs& a) {
   if constexpr (iter && bulk_rho) {
     if (threadIdx.x == 0) bulk_bar_init(&rho_bar);
     __syncthreads();
-    if (threadIdx.x == 0) {
-      bulk_expect(&rho_bar, (unsigned)nrows * N * (unsigned)sizeof(float2));
-      for (int l = 0; l < nrows; ++l) bulk_g2s(rho_s + l * RS, rho + (long long)l * N, N * (unsigned)sizeof(float2), &rho_bar);
-    }
   }
-  if constexpr (iter) {
-    if constexpr (!bulk_rho && RS % 2 == 0) {
+  // the rho rows: one bulk copy per row, or 16- / 8-byte cp.async pieces
+  auto stage_rho = [&]() {
+    if constexpr (bulk_rho) {
+      if (threadIdx.x == 0) {
+        // the lines were last read through the generic proxy: order that before the bulk writes
+        if constexpr (rho_in_buf) asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        bulk_expect(&rho_bar, (unsigned)nrows * N * (unsigned)sizeof(float2));
+        for (int l = 0; l < nrows; ++l)
+          bulk_g2s(rho_s + l * RS, rho + (long long)l * N, N * (unsigned)sizeof(float2), &rho_bar);
+      }
+    } else if constexpr (RS % 2 == 0) {
 #pragma unroll 4
       for (int e = threadIdx.x; e < L * N / 2; e += T) {
         const int l = (2 * e) / N, c = 2 * e - l * N;
         const bool ok = l < nrows;
         cp_async16(rho_s + l * RS + c, ok ? rho + 2 * e : rho, ok);
       }
-    } else if constexpr (!bulk_rho) {
+    } else {
 #pragma unroll 4
       for (int e = threadIdx.x; e < L * N; e += T) {
         const int l = e / N, c = e - l * N;
@@ -432,6 +458,9 @@ __device__ __forceinline__ void row_pass_body(const RowArgs& a) {
         cp_async8(rho_s + l * RS + c, ok ? rho + e : rho, ok);
       }
     }
+  };
+  if constexpr (iter) {
+    if constexpr (!rho_in_buf) stage_rho();
     const uint32_t* mask = a.mask + (long long)blockIdx.y * a.mask_stride + (long long)row0 * WPR;
     for (int w = threadIdx.x; w < L * WPR; w += T) {
       const bool ok = w / WPR < nrows;
@@ -456,8 +485,17 @@ __device__ __forceinline__ void row_pass_body(const RowArgs& a) {
       for (int r = 0; r < F0::R; ++r)
         v0[b][r] = l < nrows ? __ldcg(in + goff(a.in_tiled, l, j + r * F0::NR)) : make_float2(0.f, 0.f);
     }
-    if (iter || a.inv) rfft<N, 0, true>(v0, v, buf, tw, cb);
-    else rfft<N, 0, false>(v0, v, buf, tw, cb);
+    if constexpr (iter && rho_in_buf) {
+      rfft<N, 0, true>(v0, v, buf, tw, cb, [&]() {
+        __syncthreads();   // every thread's last read of the lines is done
+        stage_rho();
+        cp_commit();
+      });
+    } else if (iter || a.inv) {
+      rfft<N, 0, true>(v0, v, buf, tw, cb);
+    } else {
+      rfft<N, 0, false>(v0, v, buf, tw, cb);
+    }
   }
   float2* out = a.out + (long long)blockIdx.y * a.out_stride;
   const float s = a.scale;
@@ -500,6 +538,7 @@ __device__ __forceinline__ void row_pass_body(const RowArgs& a) {
       }
     }
     float2 o[IL::B][IL::R];
+    if constexpr (rho_in_buf) __syncthreads();   // the rho rows are read before the lines are reused
     rfft<N, 1, false>(v, o, buf, tw, cb);
 #pragma unroll
     for (int b = 0; b < IL::B; ++b) {
