@@ -200,6 +200,10 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
                "l"(src), "r"(bytes), "r"(smem_addr(bar))
                : "memory");
 }
+// warm L2 with `bytes` (a multiple of 16) from a 16-byte aligned global address; no completion
+__device__ __forceinline__ void bulk_prefetch_l2(const void* src, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(src), "r"(bytes) : "memory");
+}
 __device__ __forceinline__ void bulk_wait(uint64_t* bar, int* err) {
   const unsigned b = smem_addr(bar);
   for (unsigned i = 0; i < kBulkSpinLimit; ++i) {

@@ -461,6 +461,8 @@ __device__ __forceinline__ void row_pass_body(const RowArgs& a) {
   };
   if constexpr (iter) {
     if constexpr (!rho_in_buf) stage_rho();
+    // rows copied in late: start them towards L2 now
+    if constexpr (rho_in_buf) if (threadIdx.x < nrows) bulk_prefetch_l2(rho + (long long)threadIdx.x * N, N * (unsigned)sizeof(float2));
     const uint32_t* mask = a.mask + (long long)blockIdx.y * a.mask_stride + (long long)row0 * WPR;
     for (int w = threadIdx.x; w < L * WPR; w += T) {
       const bool ok = w / WPR < nrows;
