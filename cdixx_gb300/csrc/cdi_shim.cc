@@ -125,13 +125,17 @@ void CDI::readObjectWave() {
       obj[o] = mod * std::cos(ph);
       obj[o + 1] = mod * std::sin(ph);
     }
-  // pattern = |FFT(obj)|^2 / N on the device (myFFT + convertFOPhase(1/sqrt N) + getMod2)
-  void* d = nullptr;
-  if (cudaMalloc(&d, obj.size() * sizeof(float)) != cudaSuccess) check(CDX_ERR_NOMEM, "readObjectWave");
-  cudaMemcpy(d, obj.data(), obj.size() * sizeof(float), cudaMemcpyHostToDevice);
-  check(cdx_fft2(d, d, row, column, 1, 0, nullptr), "readObjectWave");
-  cudaMemcpy(obj.data(), d, obj.size() * sizeof(float), cudaMemcpyDeviceToHost);
-  cudaFree(d);
+  // pattern = |FFT(obj)|^2 / N on the device (myFFT + convertFOPhase(1/sqrt N) + getMod2),
+  // the object first multiplied by the Fresnel phase with isFresnel (cdi.cc:174)
+  void* dev = nullptr;
+  if (cudaMalloc(&dev, obj.size() * sizeof(float)) != cudaSuccess) check(CDX_ERR_NOMEM, "readObjectWave");
+  cudaMemcpy(dev, obj.data(), obj.size() * sizeof(float), cudaMemcpyHostToDevice);
+  if (isFresnel)
+    check(cdx_fresnel_phase(dev, row, column, 1, cdx_fresnel_factor(lambda, d, pixelsize, row, 0), nullptr),
+          "readObjectWave");
+  check(cdx_fft2(dev, dev, row, column, 1, 0, nullptr), "readObjectWave");
+  cudaMemcpy(obj.data(), dev, obj.size() * sizeof(float), cudaMemcpyDeviceToHost);
+  cudaFree(dev);
   std::vector<float> pat((size_t)row * column);
   const double n = (double)row * column;
   for (size_t i = 0; i < pat.size(); ++i)
@@ -311,6 +315,20 @@ void CDI::saveState() {   // cdi.cc:255-294: restart file of Psi plus .bin dumps
   cdx_write_bin(out_path(outputDir, "recon_object" + save_suffix + ".bin").c_str(), rho.data(), row, column, 1);
   for (float& v : spt) v = v > stats_.threshold ? 1.f : 0.f;   // bitMap(support, support)
   cdx_write_bin(out_path(outputDir, "support" + save_suffix + ".bin").c_str(), spt.data(), row, column, 0);
+  if (isFresnel) {   // cdi.cc:285-288: the object's phase with the Fresnel phase removed
+    std::vector<float> rf(rho);
+    void* dev = nullptr;
+    if (cudaMalloc(&dev, rf.size() * sizeof(float)) != cudaSuccess) check(CDX_ERR_NOMEM, "saveState");
+    cudaMemcpy(dev, rf.data(), rf.size() * sizeof(float), cudaMemcpyHostToDevice);
+    check(cdx_fresnel_phase(dev, row, column, 1, cdx_fresnel_factor(lambda, d, pixelsize, row, 1), nullptr),
+          "saveState");
+    cudaMemcpy(rf.data(), dev, rf.size() * sizeof(float), cudaMemcpyDeviceToHost);
+    cudaFree(dev);
+    std::vector<float> ph(n);
+    for (size_t i = 0; i < n; ++i) ph[i] = std::atan2(rf[2 * i + 1], rf[2 * i]);
+    cdx_write_bin(out_path(outputDir, "recon_phase_fresnelRemoved" + save_suffix + ".bin").c_str(), ph.data(), row,
+                  column, 0);
+  }
 
   // findMiddle (misc.cc:27-42): centroid of the support bitmap in units of the
   // field, coordinates (x + 0.5)/row - 0.5 (multiplyx/multiplyy, cudaConfig.cu:1427-1437)

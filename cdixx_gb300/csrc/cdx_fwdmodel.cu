@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <string>
 
 #include "cdx.h"
@@ -220,5 +221,37 @@ extern "C" int cdx_ccd_noise(float* pattern, long long count, float noise_level,
                                                     seed);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return set_error(CDX_ERR_CUDA, std::string("ccd noise: ") + cudaGetErrorString(e));
+  return CDX_OK;
+}
+
+// multiplyFresnelPhase_Device (cudaConfig.cu:1095-1101): a <- a exp(i f ((x - rows/2)^2 + (y - cols/2)^2))
+// on the entries that are not zero, the squared distance in integers and the phase in float
+__global__ void k_fresnel_phase(float2* __restrict__ a, int rows, int cols, long long n, float f) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const long long k = i % ((long long)rows * cols);
+    const int dx = (int)(k / cols) - (rows >> 1), dy = (int)(k % cols) - (cols >> 1);
+    const float ph = f * (float)(dx * dx + dy * dy);
+    float s, c;
+    sincosf(ph, &s, &c);
+    const float2 v = a[i];
+    if (v.x != 0.f || v.y != 0.f) a[i] = make_float2(v.x * c - v.y * s, v.x * s + v.y * c);
+  }
+}
+
+extern "C" float cdx_fresnel_factor(double lambda, double distance, double pixelsize, int rows, int remove) {
+  // propagator members are float (propagator.hpp:9-13); pi lambda d / (pixelsize row)^2 in double
+  const float lam = (float)lambda, dist = (float)distance, px = (float)pixelsize;
+  const float side = px * (float)rows;
+  const double f = M_PI * (double)lam * (double)dist / (double)(side * side);
+  return (float)(remove ? -f : f);
+}
+
+extern "C" int cdx_fresnel_phase(void* field, int rows, int cols, int batch, float factor, void* stream) {
+  if (!field || rows < 1 || cols < 1 || batch < 1) return set_error(CDX_ERR_ARG, "bad Fresnel-phase argument");
+  const long long n = (long long)rows * cols * batch;
+  const int g = (int)std::min<long long>((n + 255) / 256, 152 * 32);
+  k_fresnel_phase<<<g, 256, 0, (cudaStream_t)stream>>>((float2*)field, rows, cols, n, factor);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return set_error(CDX_ERR_CUDA, std::string("Fresnel phase: ") + cudaGetErrorString(e));
   return CDX_OK;
 }

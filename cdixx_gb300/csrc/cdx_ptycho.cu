@@ -20,6 +20,7 @@
 #include <string>
 #include <vector>
 
+#include "../../include/cdx.h"
 #include "../../include/cdx_ptycho.h"
 #include "cdx_fft.cuh"
 #include "cdx_host.h"
@@ -611,6 +612,7 @@ struct cdx_pty {
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   float last_ms = 0.f;
   float lam = 0, dist = 0, res = 0;   // propagate_pupil members (float)
+  float fresnel = 0.f;                // propagate_esw's Fresnel phase factor (isFresnel), else 0
 };
 
 namespace {
@@ -689,6 +691,7 @@ PtyArgs pass_args(cdx_pty* t, int k, bool probe_phase, bool noise_proj = false) 
   a.ccd_scale = (float)(1. / t->p.exposure);
   a.rcolor = kRcolor;
   a.err = t->derr;
+  a.fresnel = t->fresnel;
   return a;
 }
 
@@ -874,6 +877,8 @@ int cdx_pty_create(const cdx_pty_params* p, void* stream, cdx_pty** out) {
   t->lam = (float)p->lambda;
   t->dist = (float)p->dpupil;
   t->res = (float)(p->lambda * p->d / p->pixelsize / p->rows);
+  // propagate_esw: lambda, distance d, pixelsize, row (util/ptycho.cpp:74-76, 232)
+  t->fresnel = p->is_fresnel ? cdx_fresnel_factor(p->lambda, p->d, p->pixelsize, p->rows, 0) : 0.f;
   *out = t;
   return CDX_OK;
 }

@@ -37,7 +37,17 @@ struct PtyArgs {
   float ccd_scale;         // vars.scale = 1/exposure
   float rcolor;            // vars.rcolor
   int* err;                // bit 0: a bulk staging copy timed out
+  float fresnel;           // isFresnel: the exit wave's Fresnel phase factor (0: off)
 };
+
+// multiplyFresnelPhase_Device at (row, col) of the rows x cols frame (cudaConfig.cu:1095-1101):
+// v exp(i f ((row - rows/2)^2 + (col - cols/2)^2)) unless v is zero
+__device__ __forceinline__ float2 pty_fresnel(float2 v, int row, int col, int rows, int cols, float f) {
+  const int dx = row - (rows >> 1), dy = col - (cols >> 1);
+  float s, c;
+  sincosf(f * (float)(dx * dx + dy * dy), &s, &c);
+  return (v.x != 0.f || v.y != 0.f) ? make_float2(v.x * c - v.y * s, v.x * s + v.y * c) : v;
+}
 
 constexpr float kPtyAlpha = 0.1f;   // ALPHA, src/gpu/ptycho.cu:5
 constexpr float kPtyBeta = 0.5f;    // BETA, src/gpu/ptycho.cu:6
@@ -153,6 +163,7 @@ __global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_ROW) pty_fwd_rk(Pty
     for (int r = 0; r < F0::R; ++r) {
       const int t = l * SN + j + r * F0::NR;   // multiply(esw, probe, window): zero outside the object
       v0[b][r] = cmul(p_s[t], o_s[t]);
+      if (a.fresnel != 0.f) v0[b][r] = pty_fresnel(v0[b][r], row0 + l, j + r * F0::NR, a.rows, a.cols, a.fresnel);
     }
   }
   float2 v[FL::B][FL::R];
@@ -290,8 +301,10 @@ __global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_ROW) pty_upd_rk(Pty
       const long long pi = (long long)row * N + c;
       const float2 p = p_s[l * SN + c];
       float2 d = cmul(p, o);                     // esw = P * O_window, then esw += Fn * (-1)
+      if (a.fresnel != 0.f) d = pty_fresnel(d, row, c, a.rows, a.cols, a.fresnel);
       d.x -= pp.x;
       d.y -= pp.y;
+      if (a.fresnel != 0.f) d = pty_fresnel(d, row, c, a.rows, a.cols, -a.fresnel);   // removeFresnelPhase
       o = pty_rpie(o, p, d, pmax, kPtyAlpha, a.obj_step);
       if (a.probe_phase) {
         const float2 st = pty_rpie_step(o, d, omax, kPtyBeta);

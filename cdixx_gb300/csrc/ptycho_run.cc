@@ -117,10 +117,6 @@ int main(int argc, char** argv) {
   }
   readConfig cfg(argv[1]);
   const std::string out = cfg.outputDir ? cfg.outputDir : "./";
-  if (cfg.isFresnel) {
-    fprintf(stderr, "Fresnel exit waves (isFresnel) are not built\n");
-    return 1;
-  }
   cdx_pty_params p;
   cdx_pty_params_default(&p);
   p.lambda = cfg.lambda;
@@ -135,6 +131,7 @@ int main(int argc, char** argv) {
   p.noise_level = cfg.noiseLevel;
   p.position_uncertainty = cfg.positionUncertainty;
   p.zernike_iter = cfg.zernikeIter;
+  p.is_fresnel = cfg.isFresnel;
   std::vector<float> sx, sy, obj_truth, pupil, pats;
   if (cfg.runSim) {
     if (!cfg.common.Intensity || !cfg.pupil.Intensity) die("runSim needs InputImages.default.Intensity and .pupil.Intensity");

@@ -86,6 +86,8 @@ _SIGS = {
     "cdx_fft2": [_P, _P, _I, _I, _I, _I, _P],
     "cdx_fft2_ex": [_P, _P, _I, _I, _I, _I, _I, _P],
     "cdx_ccd_noise": [_P, _LL, _F, _F, _I, ctypes.c_ulonglong, _P],
+    "cdx_fresnel_factor": [ctypes.c_double, ctypes.c_double, ctypes.c_double, _I, _I],
+    "cdx_fresnel_phase": [_P, _I, _I, _I, _F, _P],
     "cdx_apply_mod_abs": [_P, _P, _LL, _P],
     "cdx_apply_mod": [_P, _P, _P, _I, _F, _I, _LL, _P],
     "cdx_apply_support": [_P, _P, _P, _F, _F, _I, _LL, _P],
@@ -132,7 +134,7 @@ _SIGS = {
     "cdx_pty_scan_orders": [_I, _I, ctypes.c_uint, _P],
 }
 _RESTYPE = {"cdx_last_error": ctypes.c_char_p, "cdx_version": ctypes.c_char_p, "cdx_unet_destroy": None,
-            "cdx_unet_param_count": ctypes.c_longlong}
+            "cdx_unet_param_count": ctypes.c_longlong, "cdx_fresnel_factor": ctypes.c_float}
 
 _lib = None
 
@@ -373,6 +375,19 @@ def ccd_noise(pattern, noise_level, exposure=1.0, rcolor=65535, seed=0, stream=N
     check(lib().cdx_ccd_noise(ctypes.c_void_p(pattern.data_ptr()), pattern.numel(), noise_level, exposure, rcolor,
                               ctypes.c_ulonglong(seed), _stream_ptr(stream)))
     return pattern
+
+
+def fresnel_factor(lam, distance, pixelsize, rows, remove=False):
+    """propagator's Fresnel phase factor pi lambda d / (pixelsize rows)^2 (float members)."""
+    return float(lib().cdx_fresnel_factor(lam, distance, pixelsize, rows, int(remove)))
+
+
+def fresnel_phase(field, factor, stream=None):
+    """multiplyFresnelPhase_Device on a device complex64 tensor [..., rows, cols], in place."""
+    rows, cols = field.shape[-2:]
+    batch = int(np.prod(field.shape[:-2])) if field.dim() > 2 else 1
+    check(lib().cdx_fresnel_phase(ctypes.c_void_p(field.data_ptr()), rows, cols, batch, factor, _stream_ptr(stream)))
+    return field
 
 
 def apply_mod_abs(psi, intensity, stream=None):

@@ -23,7 +23,8 @@ class PtyParams(ctypes.Structure):
                 ("d", ctypes.c_double), ("dpupil", ctypes.c_double), ("pixelsize", ctypes.c_double),
                 ("pupil_size", ctypes.c_double), ("exposure", ctypes.c_double), ("mpie", ctypes.c_int),
                 ("use_bs", ctypes.c_int), ("beam_stop_size", ctypes.c_int), ("noise_level", ctypes.c_int),
-                ("position_uncertainty", ctypes.c_double), ("zernike_iter", ctypes.c_int)]
+                ("position_uncertainty", ctypes.c_double), ("zernike_iter", ctypes.c_int),
+                ("is_fresnel", ctypes.c_int)]
 
 
 def _c64(a, shape):
@@ -72,7 +73,7 @@ class Ptycho:
 
     def __init__(self, rows, cols, obj_rows, obj_cols, scanposx, scanposy, *, lam, d, dpupil, pixelsize,
                  pupil_size=500.0, exposure=1.0, mpie=True, use_bs=False, beam_stop_size=5, noise_level=0,
-                 position_uncertainty=0.0, zernike_iter=0, stream=None):
+                 position_uncertainty=0.0, zernike_iter=0, is_fresnel=False, stream=None):
         p = PtyParams()
         check(lib().cdx_pty_params_default(ctypes.byref(p)))
         p.rows, p.cols, p.obj_rows, p.obj_cols = rows, cols, obj_rows, obj_cols
@@ -86,6 +87,7 @@ class Ptycho:
         p.use_bs, p.beam_stop_size = int(bool(use_bs)), beam_stop_size
         p.noise_level, p.position_uncertainty = noise_level, position_uncertainty
         p.zernike_iter = zernike_iter
+        p.is_fresnel = int(is_fresnel)
         self.params = p
         self.row, self.column, self.row_O, self.column_O, self.nscan = rows, cols, obj_rows, obj_cols, p.nscan
         self._h = ctypes.c_void_p()

@@ -185,6 +185,13 @@ int cdx_fft2(const void* in, void* out, int rows, int cols, int batch, int inver
  * pixel index), not the reference's curand MRG32k3a states. */
 int cdx_ccd_noise(float* pattern, long long count, float noise_level, float exposure, int rcolor,
                   unsigned long long seed, void* stream);
+/* propagator::multiplyFresnelPhase / removeFresnelPhase (src/post_gpu/propagator.cc:15-20):
+ * the phase factor pi lambda d / (pixelsize rows)^2 of the propagator's float members
+ * (negated when `remove`), and multiplyFresnelPhase_Device (cudaConfig.cu:1095-1101) on a
+ * DEVICE field of `batch` rows x cols complex images: a <- a exp(i factor ((x - rows/2)^2 +
+ * (y - cols/2)^2)) on the entries that are not zero. */
+float cdx_fresnel_factor(double lambda, double distance, double pixelsize, int rows, int remove);
+int cdx_fresnel_phase(void* field, int rows, int cols, int batch, float factor, void* stream);
 /* cdx_fft2 with the FFT arithmetic chosen by fft_mode (CDX_FFT_*). */
 int cdx_fft2_ex(const void* in, void* out, int rows, int cols, int batch, int inverse, int fft_mode, void* stream);
 /* applyModAbs(source, target) with state NULL (cudaConfig.cu:827-841). */

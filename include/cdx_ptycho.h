@@ -46,6 +46,9 @@ typedef struct cdx_pty_params {
                               every tenth sweep, the probe a momentum step (with mPIE) and, from
                               iteration 400, the Zernike pupil fit (861 modes up to order 40) in place of
                               the pupil disk (util/ptycho.cpp:484, 617-626, 665-671) */
+  int is_fresnel;          /* isFresnel: the exit wave times the Fresnel phase of distance d before
+                              its transform, the difference of exit waves times its inverse after
+                              (util/ptycho.cpp:323-326, 526-528, 551; propagator.cc:15-20) */
 } cdx_pty_params;
 
 /* Defaults of readConfig (include/readConfig.hpp): mPIE 1, pupilSize 500,

@@ -1,6 +1,6 @@
 #!/bin/sh
 # Builds the reference's hot-path sources (src/gpu/cdi.cu, cudaConfig.cu,
-# cub_wrap.cu, src/post_gpu/cdi.cc, misc.cc, src/independant/readConfig.cc,
+# cub_wrap.cu, src/post_gpu/cdi.cc, misc.cc, propagator.cc, src/independant/readConfig.cc,
 # memManager.cc) as HOST code from where they lie in the reference checkout,
 # through the emulation headers in oracle/refshim, into oracle/_ref/ref_harness.
 # The kernels' explicit "<<<grid, block>>>" launches are rewritten on the way
@@ -18,10 +18,10 @@ for f in src/gpu/cdi.cu src/gpu/cudaConfig.cu src/gpu/cub_wrap.cu; do
   o="$OUT/obj/$(basename "$f").o"
   sed "$LAUNCH" "$REF/$f" | $CXX -x c++ - -I"$REF/$(dirname "$f")" -c -o "$o"
 done
-for f in src/post_gpu/cdi.cc src/post_gpu/misc.cc src/independant/readConfig.cc src/independant/memManager.cc; do
+for f in src/post_gpu/cdi.cc src/post_gpu/misc.cc src/post_gpu/propagator.cc src/independant/readConfig.cc src/independant/memManager.cc; do
   $CXX -c "$REF/$f" -o "$OUT/obj/$(basename "$f").o"
 done
-$CXX -DCDXREF_WITH_MISC -c "$SHIM/cdxref_stubs.cc" -o "$OUT/obj/cdxref_stubs.o"
+$CXX -DCDXREF_WITH_MISC -DCDXREF_WITH_PROPAGATOR -c "$SHIM/cdxref_stubs.cc" -o "$OUT/obj/cdxref_stubs.o"
 $CXX -c "$SHIM/ref_harness.cc" -o "$OUT/obj/ref_harness.o"
 g++ -o "$OUT/ref_harness" "$OUT"/obj/*.o
 echo "built $OUT/ref_harness"

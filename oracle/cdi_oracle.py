@@ -568,16 +568,23 @@ def crop_about(src, out_rows, out_cols, midx, midy):
     return src.reshape(-1)[(x * cols + y)]
 
 
-def sim_pattern(intensity, phase, oversampling, phase_modulation):
+def sim_pattern(intensity, phase, oversampling, phase_modulation, fresnel=0.0):
     """The noise-free runSim pattern: readObjectWave (src/post_gpu/cdi.cc:62-82) places
     sqrt(I) exp(i (phaseModulation * phase - 0.5) 2 pi) at the centre of a field
     `oversampling` times larger (createWaveFront, src/gpu/cudaConfig.cu:688-708);
-    prepareIter (cdi.cc:181-200) stores |FFT(object)|^2 / (rows cols) in FFT order."""
+    prepareIter (cdi.cc:181-200) stores |FFT(object)|^2 / (rows cols) in FFT order; with
+    isFresnel (fresnel = propagator's phase factor) the object takes the Fresnel phase
+    first (cdi.cc:174, cudaConfig.cu:1095-1101)."""
     r, c = intensity.shape
     rows, cols = int(r * oversampling), int(c * oversampling)
     obj = np.zeros((rows, cols), np.complex128)
     ph = (np.float64(phase_modulation) * phase.astype(np.float64) - 0.5) * 2 * math.pi if phase is not None else 0.0
     x0, y0 = (rows - r) // 2, (cols - c) // 2
     obj[x0:x0 + r, y0:y0 + c] = np.sqrt(np.maximum(intensity.astype(np.float64), 0)) * np.exp(1j * ph)
+    if fresnel:
+        dx = (np.arange(rows) - (rows >> 1))[:, None]
+        dy = (np.arange(cols) - (cols >> 1))[None, :]
+        fph = (np.float32(fresnel) * (dx * dx + dy * dy).astype(np.float32)).astype(np.float32).astype(np.float64)
+        obj = np.where(obj != 0, obj * np.exp(1j * fph), obj)
     F = np.fft.fft2(obj)
     return (np.abs(F) ** 2 / (rows * cols)).astype(np.float32)

@@ -12,8 +12,8 @@ the reference's scalar types (float parameters; the double literals and double
 config fields where the reference has them).  The FFT is the unnormalised DFT
 via NumPy (cuFFT's published transform), reductions accumulate in float64.
 
-Scope: the iteration with the FISTA object step and the Zernike pupil fit,
-without Fresnel propagation and scan-position refinement.  From iteration 500 the reference refines the
+Scope: the iteration with the FISTA object step, the Zernike pupil fit and the
+Fresnel exit-wave phase, without scan-position refinement.  From iteration 500 the reference refines the
 positions every 20 sweeps; with positionUncertainty = 0 (its default) that
 leaves every shift at zero and the object changed only by the rounding of an
 FFT round trip, which is not repeated here; runs with positionUncertainty > 0
@@ -329,6 +329,27 @@ def multiply_shift(wave, shiftx, shifty):
     return (wave * (np.cos(ph) + 1j * np.sin(ph)).astype(C64)).astype(C64)
 
 
+def fresnel_factor(lam, distance, pixelsize, rows, remove=False):
+    """propagator::multiplyFresnelPhase / removeFresnelPhase (src/post_gpu/propagator.cc:15-20):
+    pi lambda distance / (pixelsize rows)^2 of the propagator's float members, in double,
+    passed on as float."""
+    side = F32(F32(pixelsize) * F32(rows))
+    f = math.pi * float(F32(lam)) * float(F32(distance)) / float(F32(side * side))
+    return F32(-f if remove else f)
+
+
+def fresnel_phase(a, factor):
+    """multiplyFresnelPhase_Device (src/gpu/cudaConfig.cu:1095-1101): a exp(i factor ((x - rows/2)^2
+    + (y - cols/2)^2)) on the entries that are not zero, the squared distance in integers and
+    the phase in float."""
+    rows, cols = a.shape
+    dx = (np.arange(rows) - (rows >> 1))[:, None]
+    dy = (np.arange(cols) - (cols >> 1))[None, :]
+    ph = (F32(factor) * (dx * dx + dy * dy).astype(F32)).astype(F32).astype(np.float64)
+    p = (np.cos(ph) + 1j * np.sin(ph)).astype(C64)
+    return np.where(a != 0, (a * p).astype(C64), a).astype(C64)
+
+
 # ------------------------------------------------------- Zernike pupil fit
 ZERNIKE_MAX_N = 40                      # util/ptycho.cpp:439
 ZERNIKE_REG_L, ZERNIKE_REG_M = F32(5e-5), F32(5e-8)   # beamDecomposition.cu:585-588
@@ -539,20 +560,25 @@ class PtyParams:
     noise_level: int = 0
     position_uncertainty: float = 0.0
     zernike_iter: int = 0
+    is_fresnel: bool = False
 
     def resolution(self, rows):
         """resolution = lambda d / pixelsize / row (util/ptycho.cpp:246), stored as float."""
         return F32(self.lam * self.d / self.pixelsize / rows)
 
 
-def simulate_patterns(obj, probe, scanx, scany, exposure=1.0):
+def simulate_patterns(obj, probe, scanx, scany, exposure=1.0, fresnel=0.0):
     """The noise-free part of ptycho::createPattern (util/ptycho.cpp:310-359):
-    I_i = |FFT(P O_window)|^2 / (rows cols), times exposure then times float(1/exposure)."""
+    I_i = |FFT(P O_window)|^2 / (rows cols), times exposure then times float(1/exposure);
+    with isFresnel (fresnel = the factor) the exit wave takes the Fresnel phase first."""
     rows, cols = probe.shape
     out = []
     for px, py in zip(scanx, scany):
         w = get_window(obj, c_round(px), c_round(py), rows, cols)
-        F = fft2_u((probe * w).astype(C64))
+        esw = (probe * w).astype(C64)
+        if fresnel:
+            esw = fresnel_phase(esw, fresnel)
+        F = fft2_u(esw)
         I = ((F.real * F.real + F.imag * F.imag).astype(F32) * F32(1.0 / (rows * cols))).astype(F32)
         I = (I * F32(exposure)).astype(F32)
         I = (I * F32(1.0 / exposure)).astype(F32)
@@ -592,6 +618,7 @@ def iterate(obj0, probe0, patterns, scanx, scany, n_iter, params: PtyParams, ord
     bs = circle_mask(rows, cols, rows >> 1, cols >> 1, params.beam_stop_size, True) if params.use_bs else None
     tk = F32(0.5 + math.sqrt(1.25))
     wins = [(c_round(F32(x)), c_round(F32(y))) for x, y in zip(scanx, scany)]
+    fres = fresnel_factor(params.lam, params.d, params.pixelsize, rows) if params.is_fresnel else None
     for it in range(start_iter, start_iter + n_iter):
         probe_max = F32(np.max((P.real * P.real + P.imag * P.imag).astype(F32)))
         obj_max = F32(0)
@@ -614,6 +641,8 @@ def iterate(obj0, probe0, patterns, scanx, scany, n_iter, params: PtyParams, ord
             sx, sy = wins[i]
             w = get_window(O, sx, sy, rows, cols)
             esw = (P * w).astype(C64)
+            if fres is not None:                  # util/ptycho.cpp:526-528
+                esw = fresnel_phase(esw, fres)
             F = fft2_u(esw)
             if it < NOISE_PROJ_ITER:
                 F = apply_mod_accurate(F, patterns[i], norm, scale, bs)
@@ -621,6 +650,8 @@ def iterate(obj0, probe0, patterns, scanx, scany, n_iter, params: PtyParams, ord
                 F = apply_mod_noise(F, patterns[i], norm, scale, params.noise_level, bs)
             F = (ifft2_u(F) * norm).astype(C64)
             diff = (esw - F).astype(C64)
+            if fres is not None:                  # removeFresnelPhase (util/ptycho.cpp:551)
+                diff = fresnel_phase(diff, -fres)
             if it < UPDATE_PROBE_ITER:
                 w = rpie(w, P, diff, probe_max, ALPHA, 1.0)
             else:

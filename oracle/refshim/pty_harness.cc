@@ -10,9 +10,9 @@
 // pty_harness <object.bin> <probe.bin> <patterns.bin (nscan stacked, FFT order,
 //             scaled 1/exposure)> <scan.txt ("x y" per line)> <nIter> <mPIE>
 //             <lambda> <d> <dpupil> <pixelsize> <pupilSize> <exposure>
-//             <useBS> <beamStopSize> <rand seed> <out prefix> [noiseLevel [zernikeIter]]
-// (zernikeIter > 0 runs the FISTA object step; the Zernike pupil fit it also
-// enables from iteration 400 is not linked, so such runs stop before it)
+//             <useBS> <beamStopSize> <rand seed> <out prefix> [noiseLevel [zernikeIter [isFresnel]]]
+// (zernikeIter > 0 runs the FISTA object step, the probe momentum and, from
+// iteration 400, the Zernike pupil fit; isFresnel the exit wave's Fresnel phase)
 #define main cdxref_ptycho_main
 #include CDXREF_PTYCHO_CPP
 #undef main
@@ -49,7 +49,7 @@ int main(int argc, char** argv) {
   ptycho p("none.cfg");
   p.verbose = 0;
   p.runSim = 0;
-  p.isFresnel = 0;
+  p.isFresnel = argc > 19 ? atoi(argv[19]) : 0;
   p.saveVideoEveryIter = 0;
   p.computeErrorEveryIter = 0;
   p.zernikeIter = argc > 18 ? atoi(argv[18]) : 0;

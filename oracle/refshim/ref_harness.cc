@@ -28,8 +28,11 @@ extern cudaVars vars;
 extern "C" void writeFloatImage(const char* name, void* data, int row, int column);
 
 // ref_harness --sim <intensity.bin> <phase.bin or -> <oversampling> <phaseModulation> <exposure> <out.bin>
+//                   [<lambda> <pixelsize> <beamspotsize> <oversampling_spt> <isFresnel>]
 // runs the noise-free simulation of readFiles/prepareIter (runSim, cdi.cc:62-82,
-// 161-200) and writes the simulated patternData.
+// 161-200) and writes the simulated patternData.  The optics set the distance as
+// the constructor does for runSim (cdi.cc:39) and, with isFresnel, the Fresnel
+// phase of the object (cdi.cc:174).
 static int run_sim(int argc, char** argv) {
   if (argc < 8) return 2;
   CDI c("none.cfg");
@@ -44,6 +47,14 @@ static int run_sim(int argc, char** argv) {
   c.restart = 0;
   c.useBS = 0;
   c.verbose = 0;
+  if (argc > 12) {
+    c.lambda = atof(argv[8]);
+    c.pixelsize = atof(argv[9]);
+    c.beamspotsize = atof(argv[10]);
+    c.oversampling_spt = atof(argv[11]);
+    c.isFresnel = atoi(argv[12]);
+    c.d = c.oversampling_spt * c.pixelsize * c.beamspotsize / c.lambda;
+  }
   c.readFiles();
   c.init();
   c.prepareIter();

@@ -44,6 +44,7 @@ CASES = [(f"hio_{k}", f"{k}*HIO", 2.0, 0.1, 1.0, 0, 0) for k in range(1, 11)] + 
 PRTF_CASES = [("prtf_er", "30*ER", 10), ("prtf_hio", "12*HIO+10*ER", 6)]
 SAVE_ALGO = "2*(10*HIO+1*shrinkWrap)+4*ER"
 SIM_OVERSAMPLING, SIM_PHASEMOD, SIM_EXPOSURE = 2.0, 0.7, 0.5
+SIM_FRESNEL_OPTICS = (0.6328, 13.0, 300.0, 2.0)   # lambda, pixelsize, beamspotsize, oversampling_spt
 
 
 def main(ref=None):
@@ -114,6 +115,12 @@ def main(ref=None):
         data["sim/phase"] = phase.astype(np.float32)
         data["sim/params"] = np.array([SIM_OVERSAMPLING, SIM_PHASEMOD, SIM_EXPOSURE])
         data["sim/pattern"] = O.read_bin(td / "sim_out.bin")
+        # the same with isFresnel: the distance of runSim (cdi.cc:39) and the object's Fresnel phase
+        subprocess.run([str(exe), "--sim", "sim_i.bin", "sim_p.bin", str(SIM_OVERSAMPLING), str(SIM_PHASEMOD),
+                        str(SIM_EXPOSURE), "simf_out.bin", *[str(v) for v in SIM_FRESNEL_OPTICS], "1"],
+                       cwd=td, check=True, capture_output=True)
+        data["simf/optics"] = np.array(SIM_FRESNEL_OPTICS)
+        data["simf/pattern"] = O.read_bin(td / "simf_out.bin")
         # one step from the reference's own state after k-1 HIO steps: restart from
         # its Psi_{k-1} (prepareIter recomputes rho_{k-1} = IFFT(Psi_{k-1})/N)
         prev = psi0

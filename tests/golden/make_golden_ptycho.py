@@ -47,10 +47,13 @@ CASES = [
     ("fista405", 405, 0, 0, 5, 1.0, 40.0, "grid", 3),
     ("zernike412", 412, 0, 0, 5, 1.0, 40.0, "grid", 3),
     ("zernike412_mpie", 412, 1, 0, 5, 1.0, 40.0, "grid", 7),
+    ("fresnel30", 30, 1, 0, 5, 1.0, 40.0, "grid", 5),
+    ("fresnel405", 405, 0, 0, 5, 1.0, 40.0, "grid", 3),
 ]
 NOISE_LEVEL = {"noise2003": 20}
 # FISTA object step (and the probe momentum every 10); from 400 the Zernike pupil fit every 10
 ZERNIKE_ITER = {"fista45": 35, "fista405": 300, "zernike412": 1200, "zernike412_mpie": 1200}
+FRESNEL = {"fresnel30", "fresnel405"}   # isFresnel: the exit waves take the Fresnel phase of distance d
 OPTICS = dict(lam=0.5, d=2e4, dpupil=1e3, pixelsize=20.0, pupil_size=16.0)
 
 
@@ -86,7 +89,8 @@ def main(ref=None):
             sx, sy = scan(layout)
             probe_t = PO.angular_spectrum(PO.pupil_func(R, R, OPTICS["pupil_size"]), OPTICS["lam"],
                                           OPTICS["dpupil"], res)
-            pats = PO.simulate_patterns(truth_object(rng), probe_t, sx, sy, 1.0)
+            fres = PO.fresnel_factor(OPTICS["lam"], OPTICS["d"], OPTICS["pixelsize"], R) if name in FRESNEL else 0.0
+            pats = PO.simulate_patterns(truth_object(rng), probe_t, sx, sy, 1.0, fresnel=fres)
             pats = (pats / pats.max() * np.float32(pscale / expo)).astype(np.float32)
             obj0 = np.exp(2j * np.pi * rng.random((RO, RO))).astype(np.complex64)
             probe0 = PO.angular_spectrum(PO.pupil_func(R, R, OPTICS["pupil_size"]), OPTICS["lam"],
@@ -100,7 +104,7 @@ def main(ref=None):
             cmd = [str(harness), f"{d}/obj.bin", f"{d}/probe.bin", f"{d}/pats.bin", f"{d}/scan.txt", str(n_iter),
                    str(mpie), str(OPTICS["lam"]), str(OPTICS["d"]), str(OPTICS["dpupil"]), str(OPTICS["pixelsize"]),
                    str(OPTICS["pupil_size"]), str(expo), str(use_bs), str(bss), str(seed), f"{d}/out",
-                   str(NOISE_LEVEL.get(name, 0)), str(ZERNIKE_ITER.get(name, 0))]
+                   str(NOISE_LEVEL.get(name, 0)), str(ZERNIKE_ITER.get(name, 0)), str(int(name in FRESNEL))]
             subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL)
             p = f"{name}/"
             data[p + "obj0"] = obj0
@@ -110,7 +114,7 @@ def main(ref=None):
             data[p + "scany"] = sy
             data[p + "orders"] = PO.scan_orders(len(sx), n_iter, seed)
             data[p + "cfg"] = np.array([n_iter, mpie, use_bs, bss, seed, NOISE_LEVEL.get(name, 0),
-                                        ZERNIKE_ITER.get(name, 0)], np.int64)
+                                        ZERNIKE_ITER.get(name, 0), int(name in FRESNEL)], np.int64)
             data[p + "exposure"] = np.float64(expo)
             data[p + "ref_object"] = read_bin(f"{d}/out_object.bin").copy()
             data[p + "ref_pupil"] = read_bin(f"{d}/out_pupil.bin").copy()

@@ -19,12 +19,13 @@ import numpy as np
 import pytest
 
 from oracle import cdi_oracle as O
+from oracle import ptycho_oracle as PO
 from tests._bounds import STEP_TOL, rel_l2 as rel, trajectory_bound
 
 GOLDEN = Path(__file__).resolve().parent / "golden" / "reference_cases.npz"
 Z = np.load(GOLDEN)
 CASES = sorted({k.split("/")[0] for k in Z.files
-                if "/" in k and not k.startswith(("step_", "prtf_", "savestate", "sim/"))})
+                if "/" in k and not k.startswith(("step_", "prtf_", "savestate", "sim/", "simf/"))})
 PRTF_CASES = sorted({k.split("/")[0] for k in Z.files if k.startswith("prtf_")})
 STEPS = list(range(1, 11))
 
@@ -197,17 +198,62 @@ Job = {{
     assert rel(ac, Z["savestate/check_autocorrelation"]) <= 1e-5
 
 
+@pytest.mark.gpu
+def test_cdi_run_savestate_fresnel_removed_phase(cdx, tmp_path):
+    """With isFresnel, saveState also dumps the object's phase with the Fresnel phase
+    removed (cdi.cc:285-288): the phase of recon_object times the inverse Fresnel phase."""
+    import subprocess
+    lib = Path(__file__).resolve().parents[1] / "cdixx_gb300" / "_lib"
+    I = Z["intensity"]
+    O.write_bin(tmp_path / "pattern.bin", np.fft.fftshift(I))
+    O.write_bin(tmp_path / "restart.bin", Z["psi0"])
+    (tmp_path / "cdi.cfg").write_text("""
+InputImages = { default = { Pattern = "pattern.bin"; restart = "restart.bin"; }; };
+Job = {
+  algorithm = "20*HIO+5*ER";
+  oversampling_spt = 2.;
+  exposure = 1.;
+  nIter = 0;
+  doIteration = True;
+  restart = True;
+  isFresnel = True;
+  lambda = 0.6328;
+  d = 2e4;
+  pixelsize = 13.;
+  outputDir = "./";
+};
+""")
+    r = subprocess.run([str(lib / "cdi_run"), "cdi.cfg"], cwd=tmp_path, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    rho = O.read_bin(tmp_path / "recon_object.bin")
+    ph = O.read_bin(tmp_path / "recon_phase_fresnelRemoved.bin")
+    f = PO.fresnel_factor(0.6328, 2e4, 13.0, I.shape[0], remove=True)
+    want = np.angle(PO.fresnel_phase(rho.astype(np.complex64), f))
+    live = np.abs(rho) > 1e-3 * np.abs(rho).max()
+    d = np.angle(np.exp(1j * (ph[live] - want[live])))
+    assert np.max(np.abs(d)) < 1e-4
+
+
 # ------------------------------------------------------------------ runSim
 def test_oracle_sim_pattern_matches_reference():
     """The noise-free runSim pattern of the reference (readObjectWave + prepareIter)."""
     os_, pm, _ex = Z["sim/params"]
     got = O.sim_pattern(Z["sim/intensity"], Z["sim/phase"], float(os_), float(pm))
     assert rel(got, Z["sim/pattern"]) <= 1e-6
+    # isFresnel: the object takes the Fresnel phase of the runSim distance first
+    lam, px, bss, ospt = Z["simf/optics"]
+    rows = int(Z["sim/intensity"].shape[0] * os_)
+    f = PO.fresnel_factor(lam, ospt * px * bss / lam, px, rows)
+    got = O.sim_pattern(Z["sim/intensity"], Z["sim/phase"], float(os_), float(pm), fresnel=f)
+    assert rel(got, Z["simf/pattern"]) <= 1e-6
+    assert rel(Z["sim/pattern"], Z["simf/pattern"]) > 0.1
 
 
 @pytest.mark.gpu
-def test_cpp_runsim_pattern_matches_reference(cdx, tmp_path):
-    """The C++ CDI layer's runSim set-up (cdi_shim readObjectWave) on the same images."""
+@pytest.mark.parametrize("fresnel", [False, True])
+def test_cpp_runsim_pattern_matches_reference(cdx, tmp_path, fresnel):
+    """The C++ CDI layer's runSim set-up (cdi_shim readObjectWave) on the same images,
+    with and without isFresnel."""
     import subprocess
     root = Path(__file__).resolve().parents[1]
     lib = root / "cdixx_gb300" / "_lib"
@@ -218,6 +264,9 @@ def test_cpp_runsim_pattern_matches_reference(cdx, tmp_path):
     O.write_bin(tmp_path / "i.bin", Z["sim/intensity"])
     O.write_bin(tmp_path / "p.bin", Z["sim/phase"])
     os_, pm, ex = Z["sim/params"]
+    lam, px, bss, ospt = Z["simf/optics"]
+    optics = (f"lambda = {lam!r}; pixelsize = {px!r}; beamspotsize = {bss!r}; isFresnel = True;"
+              if fresnel else "")
     (tmp_path / "sim.cfg").write_text(f"""
 InputImages = {{ default = {{ Intensity = "i.bin"; Phase = "p.bin"; }}; }};
 Job = {{
@@ -225,12 +274,14 @@ Job = {{
   oversampling = {float(os_)};
   phaseModulation = {float(pm)};
   exposure = {float(ex)};
-  oversampling_spt = 2.;
+  oversampling_spt = {float(ospt)};
+  {optics}
   outputDir = "./";
 }};
 """)
     r = subprocess.run([str(exe), "sim.cfg", "sim_out.bin"], cwd=tmp_path, capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stdout + r.stderr
     got = O.read_bin(tmp_path / "sim_out.bin")
-    assert got.shape == Z["sim/pattern"].shape
-    assert rel(got, Z["sim/pattern"]) <= 2e-6
+    ref = Z["simf/pattern" if fresnel else "sim/pattern"]
+    assert got.shape == ref.shape
+    assert rel(got, ref) <= 2e-6

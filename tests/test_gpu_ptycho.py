@@ -27,7 +27,7 @@ def make(PT, c, prm, rows=None, obj_shape=None):
                   dpupil=prm.dpupil, pixelsize=prm.pixelsize, pupil_size=prm.pupil_size, exposure=prm.exposure,
                   mpie=prm.mpie, use_bs=prm.use_bs, beam_stop_size=prm.beam_stop_size,
                   noise_level=prm.noise_level, position_uncertainty=prm.position_uncertainty,
-                  zernike_iter=prm.zernike_iter)
+                  zernike_iter=prm.zernike_iter, is_fresnel=prm.is_fresnel)
     t.objectWave = c["obj0"]
     t.probe = c["probe0"]
     t.patterns = c["pats"]
@@ -139,6 +139,30 @@ def test_zernike_sweep_at_the_reference_pupil_ratio(PT):
         prm.zernike_iter = 0
         _O, _pu, Pdisk = PO.iterate(obj0, probe, pats, sx, sy, 1, prm, orders, start_iter=410)
         assert PO.rel_err(t.probe, Pdisk) > 100 * STEP_BOUND
+
+
+@pytest.mark.parametrize("first", [0, 400])
+@pytest.mark.parametrize("mpie", [False, True])
+def test_one_fresnel_sweep_matches_oracle(PT, first, mpie):
+    """isFresnel: one sweep with the exit waves' Fresnel phase (object phase, probe
+    phase) against the oracle, and createPattern with it."""
+    c, prm, _n, _s = load("fresnel30")
+    prm.mpie = mpie
+    rng = np.random.default_rng(first + 1)
+    obj = (c["obj0"] * (0.5 + rng.random(c["obj0"].shape))).astype(np.complex64)
+    orders = np.array([rng.permutation(len(c["scanx"]))], np.int32)
+    with make(PT, c, prm) as t:
+        t.objectWave = obj
+        t.iterate(1, first_iter=first, orders=orders)
+        O, pupil, P = PO.iterate(obj, c["probe0"], c["pats"], c["scanx"], c["scany"], 1, prm, orders, start_iter=first)
+        assert PO.rel_err(t.objectWave, O) < STEP_BOUND
+        assert PO.rel_err(t.probe, P) < STEP_BOUND
+        t.objectWave = obj
+        t.probe = c["probe0"]
+        t.createPattern()
+        fres = PO.fresnel_factor(prm.lam, prm.d, prm.pixelsize, c["probe0"].shape[0])
+        ref = PO.simulate_patterns(obj, c["probe0"], c["scanx"], c["scany"], prm.exposure, fresnel=fres)
+        assert np.linalg.norm(t.patterns - ref) / np.linalg.norm(ref) < 2e-6
 
 
 def test_simulate_matches_oracle(PT):

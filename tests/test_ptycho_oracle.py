@@ -11,7 +11,7 @@ from oracle import ptycho_oracle as PO
 
 GOLD = Path(__file__).resolve().parent / "golden" / "ptycho_cases.npz"
 CASES = ["obj3", "obj20_nompie", "obj30", "beamstop", "saturated", "offedge", "probe402", "refine520", "noise2003",
-         "fista45", "fista405", "zernike412", "zernike412_mpie"]
+         "fista45", "fista405", "zernike412", "zernike412_mpie", "fresnel30", "fresnel405"]
 # Relative L2 bounds of oracle (and GPU) against the reference's run.  Short
 # runs agree to float32 rounding; along long runs the rounding differences of
 # two FFTs grow (momentum and the probe phase amplify them): measured oracle
@@ -25,19 +25,23 @@ CASES = ["obj3", "obj20_nompie", "obj30", "beamstop", "saturated", "offedge", "p
 # With zernikeIter (FISTA object step each sweep, probe momentum every tenth):
 # 45 sweeps with momentum 1.1e-6, 405 sweeps without 7.4e-7; 412 sweeps, the Zernike
 # pupil fit at 400 and 410, without momentum 4.1e-7 / 6.7e-7, with it 2.1e-6 / 8.2e-7.
+# With isFresnel (phases up to 39 rad on the 32^2 frame): one sweep 7.6e-7, then the
+# rounding of the phase factors grows along the run without momentum (1.6e-6 after
+# 10 sweeps, 8.6e-6 after 50, 1.3e-4 after 200, 2.9e-3 / 5.6e-4 after 405), and
+# 1.1e-4 after 30 sweeps with momentum.
 OBJ_BOUND = {"obj30": 2e-4, "probe402": 3e-3, "refine520": 2e-4, "noise2003": 5e-3, "fista45": 1e-5,
-             "fista405": 1e-5}
-PUPIL_BOUND = {"probe402": 1e-4, "refine520": 2e-4, "noise2003": 5e-3}
+             "fista405": 1e-5, "fresnel30": 2e-4, "fresnel405": 5e-3}
+PUPIL_BOUND = {"probe402": 1e-4, "refine520": 2e-4, "noise2003": 5e-3, "fresnel405": 1e-3}
 
 
 def load(name):
     z = np.load(GOLD)
     p = name + "/"
-    n_iter, mpie, use_bs, bss, seed, noise, zern = [int(v) for v in z[p + "cfg"]]
+    n_iter, mpie, use_bs, bss, seed, noise, zern, fres = [int(v) for v in z[p + "cfg"]]
     opt = z["optics"]
     prm = PO.PtyParams(lam=opt[0], d=opt[1], dpupil=opt[2], pixelsize=opt[3], pupil_size=opt[4],
                        exposure=float(z[p + "exposure"]), mpie=bool(mpie), use_bs=bool(use_bs),
-                       beam_stop_size=bss, noise_level=noise, zernike_iter=zern)
+                       beam_stop_size=bss, noise_level=noise, zernike_iter=zern, is_fresnel=bool(fres))
     case = {k: z[p + k] for k in ("obj0", "probe0", "pats", "scanx", "scany", "orders", "ref_object", "ref_pupil")}
     return case, prm, n_iter, seed
 
