@@ -265,7 +265,7 @@ def test_cpp_runsim_pattern_matches_reference(cdx, tmp_path, fresnel):
     O.write_bin(tmp_path / "p.bin", Z["sim/phase"])
     os_, pm, ex = Z["sim/params"]
     lam, px, bss, ospt = Z["simf/optics"]
-    optics = (f"lambda = {lam!r}; pixelsize = {px!r}; beamspotsize = {bss!r}; isFresnel = True;"
+    optics = (f"lambda = {float(lam)!r}; pixelsize = {float(px)!r}; beamspotsize = {float(bss)!r}; isFresnel = True;"
               if fresnel else "")
     (tmp_path / "sim.cfg").write_text(f"""
 InputImages = {{ default = {{ Intensity = "i.bin"; Phase = "p.bin"; }}; }};
