@@ -381,6 +381,146 @@ __global__ void k_pty_conj_phase(float2* __restrict__ O, long long n, const PtyS
 }
 __global__ void k_pty_next(int* iter) { *iter += 1; }
 
+// ------------------------------------------------------------ scan-position refinement
+// (positionUncertainty > 0: every 20 sweeps from 500, util/ptycho.cpp:511-585)
+
+// getWindow of the position visited k-th (zero outside the object), row-major rows x cols
+__global__ void k_pty_pos_window(const float2* __restrict__ O, int obj_rows, int obj_cols, const int2* __restrict__ win,
+                                 const int* order, const int* iter, int nscan, int k, float2* __restrict__ gw,
+                                 int rows, int cols) {
+  const int2 w = win[order[*iter * nscan + k]];
+  const long long n = (long long)rows * cols;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int ox = w.x + (int)(i / cols), oy = w.y + (int)(i % cols);
+    gw[i] = ox >= 0 && ox < obj_rows && oy >= 0 && oy < obj_cols ? O[(long long)ox * obj_cols + oy] : make_float2(0.f, 0.f);
+  }
+}
+
+// updatePosition's spectral derivatives (util/ptycho.cpp:366-371): the window's spectrum
+// (FFT order) centred and scaled by s1 = sqrt(1/n), times (x/rows - 0.5) (frame D) and
+// (y/cols - 0.5) (frame D + n) at the centred coordinates, back to FFT order times 1/n
+__global__ void k_pty_pos_deriv(float2* __restrict__ D, int rows, int cols, float s1, float nrm) {
+  const long long n = (long long)rows * cols;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(i / cols), c = (int)(i % cols);
+    const int xc = (r + (rows >> 1)) % rows, yc = (c + (cols >> 1)) % cols;
+    const float sx = (float)xc * (1.0f / (float)rows) - 0.5f, sy = (float)yc * (1.0f / (float)cols) - 0.5f;
+    float2 v = D[i];
+    v.x *= s1;
+    v.y *= s1;
+    D[i] = make_float2(v.x * sx * nrm, v.y * sx * nrm);
+    D[i + n] = make_float2(v.x * sy * nrm, v.y * sy * nrm);
+  }
+}
+
+// multiply(cache, cache, probe) on both frames
+__global__ void k_pty_pos_probe(float2* __restrict__ D, const float2* __restrict__ P, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float2 p = P[i];
+    D[i] = cmul(D[i], p);
+    D[i + n] = cmul(D[i + n], p);
+  }
+}
+
+// calcPartial (src/gpu/ptycho.cu:156-169) on both frames against Fn * norm, summed (findSum):
+// (Fn.x d.y - Fn.y d.x)(1 - sqrt(max(I + 1e-3, 0) / (|Fn|^2 + 1e-3))); beamstop pixels add
+// nothing.  Per-CTA double sums, the last CTA writes grad[si] and grad[si + nscan].
+__global__ void k_pty_pos_partial(const float2* __restrict__ Fn, const float2* __restrict__ D, const float* __restrict__ pats,
+                                  long long pat_stride, const float* __restrict__ bs, int rows, int cols, int tl, float norm,
+                                  const int* order, const int* iter, int nscan, int k, double* part, unsigned* count,
+                                  float* grad) {
+  __shared__ double red[2][8];
+  const int si = order[*iter * nscan + k];
+  const float* pat = pats + (long long)si * pat_stride;
+  const long long n = (long long)rows * cols;
+  double ax = 0, ay = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(i / cols), c = (int)(i % cols);
+    const long long ti = pty_tiled(r, c, rows, tl);
+    if (bs && bs[ti] > 0.5f) continue;
+    float2 f = Fn[i];
+    f.x *= norm;
+    f.y *= norm;
+    const float fm2 = f.x * f.x + f.y * f.y;
+    float fact = pat[ti] + 1e-3f;
+    if (fact < 0.f) fact = 0.f;
+    const float kf = 1.f - sqrtf(fact / (fm2 + 1e-3f));
+    const float2 dx = D[i], dy = D[i + n];
+    ax += (double)((f.x * dx.y - f.y * dx.x) * kf);
+    ay += (double)((f.x * dy.y - f.y * dy.x) * kf);
+  }
+  for (int o = 16; o; o >>= 1) {
+    ax += __shfl_xor_sync(0xffffffffu, ax, o);
+    ay += __shfl_xor_sync(0xffffffffu, ay, o);
+  }
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) { red[0][w] = ax; red[1][w] = ay; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0, b = 0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) { a += red[0][q]; b += red[1][q]; }
+    part[2 * blockIdx.x] = a;
+    part[2 * blockIdx.x + 1] = b;
+  }
+  if (!pty_last_block(count)) return;
+  __shared__ double fin[8];
+  double a = 0, b = 0;
+  for (int q = threadIdx.x; q < (int)gridDim.x; q += blockDim.x) {
+    a += __ldcg(part + 2 * q);
+    b += __ldcg(part + 2 * q + 1);
+  }
+  a = block_sum_d<256>(a, fin);
+  b = block_sum_d<256>(b, fin);
+  if (threadIdx.x != 0) return;
+  grad[si] = (float)a;
+  grad[si + nscan] = (float)b;
+}
+
+// addProbability(d_shifts, d_shift, 0.3, positionUncertainty) (cudaConfig.cu:808-817), the
+// mean shift removed from every position (util/ptycho.cpp:569-577), the window origins
+// round(scanpos + shift) renewed; mean[0..1] receives the mean shift.  One thread.
+__global__ void k_pty_pos_update(float* __restrict__ shifts, const float* __restrict__ grad,
+                                 const float* __restrict__ scanpos, int2* __restrict__ win, int nscan, float sigma,
+                                 float* __restrict__ mean) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  for (int j = 0; j < 2 * nscan; ++j) {
+    const float d = shifts[j], v = grad[j] * 0.3f, t = d + v;
+    if (fabsf(t) > fabsf(d)) {
+      const float g = expf(-(t * t) / 2 / (sigma * sigma));   // gaussian(t, 0, sigma), cudaConfig.cu:24-26
+      shifts[j] = d + v * g;
+    } else {
+      shifts[j] = t;
+    }
+  }
+  for (int a = 0; a < 2; ++a) {
+    double sum = 0;
+    for (int i = 0; i < nscan; ++i) sum += shifts[a * nscan + i];
+    const float m = (float)sum / (float)nscan;
+    mean[a] = m;
+    for (int i = 0; i < nscan; ++i) shifts[a * nscan + i] = shifts[a * nscan + i] - m;
+  }
+  for (int i = 0; i < nscan; ++i)
+    win[i] = make_int2((int)roundf(scanpos[i] + shifts[i]), (int)roundf(scanpos[nscan + i] + shifts[nscan + i]));
+}
+
+// shiftWave(objFFT, wave, -mean) between its transforms (src/post_gpu/misc.cc:106-113): the
+// spectrum (FFT order) times multiplyShift's phase at the centred coordinates and 1/(rows cols)
+__global__ void k_pty_pos_oshift(float2* __restrict__ S, int rows, int cols, const float* __restrict__ mean) {
+  const float shx = -mean[0], shy = -mean[1], inv = (float)(1. / ((double)rows * cols));
+  const long long n = (long long)rows * cols;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(i / cols), c = (int)(i % cols);
+    const int x = (r + (rows >> 1)) % rows, y = (c + (cols >> 1)) % cols;
+    const float t = shx * (float)(x - rows / 2) / (float)rows + shy * (float)(y - cols / 2) / (float)cols;
+    float sn, cs;
+    sincosf((float)(-2 * M_PI * (double)t), &sn, &cs);
+    float2 v = cmul(S[i], make_float2(cs, sn));
+    v.x *= inv;
+    v.y *= inv;
+    S[i] = v;
+  }
+}
+
 // FISTA_step (src/post_gpu/FISTA.cc:109-135) of the object, one TV proximal step,
 // fused: o = b * s (s = 0.125/lambda), forward differences p (rows) and q
 // (columns) of o, each component of (p, q) scaled to modulus <= 1 (diffMax),
@@ -602,7 +742,8 @@ struct cdx_pty {
   bool have_scan = false, have_pats = false, have_obj = false, have_probe = false;
   // one sweep per kind: phase (object, probe, probe + noise projection) x FISTA x probe momentum
   // x Zernike pupil fit
-  cudaGraphExec_t graph[24] = {};
+  // x position refinement
+  cudaGraphExec_t graph[48] = {};
   float2* Pp = nullptr;       // probe momentum history (Zernike sweeps)
   float2* fista = nullptr;    // FISTA output before it replaces the object
   float* coefz = nullptr;     // probe momentum coefficients per sweep
@@ -613,32 +754,46 @@ struct cdx_pty {
   float last_ms = 0.f;
   float lam = 0, dist = 0, res = 0;   // propagate_pupil members (float)
   float fresnel = 0.f;                // propagate_esw's Fresnel phase factor (isFresnel), else 0
+  // scan-position refinement (position_uncertainty > 0)
+  float *shifts = nullptr, *grad = nullptr, *scanpos = nullptr, *pmean = nullptr;
+  float2 *fn = nullptr, *gw = nullptr, *dxy = nullptr, *dtmp = nullptr, *otmp = nullptr;
+  float2 *tw_or = nullptr, *tw_oc = nullptr;   // object-size twiddles (rows, cols)
+  RowLaunch orow = nullptr;                    // object row pass (length obj_cols)
+  ColLaunch ocol = nullptr;                    // object column pass (length obj_rows)
+  std::vector<int2> win0;                      // nominal window origins
 };
 
 namespace {
 
-int fft2(cdx_pty* t, const float2* in, float2* out, bool inv) {
+// unnormalised 2-D FFT of `batch` row-major rows x cols frames, in -> out
+int fft2g(cudaStream_t st, const float2* in, float2* out, bool inv, int rows, int cols, const float2* twr,
+          const float2* twc, RowLaunch rl, ColLaunch cl, int batch) {
   RowArgs r{};
   r.in = in;
   r.out = out;
-  r.in_stride = r.out_stride = t->npx;
-  r.tw = t->tw_c;
-  r.rows = t->p.rows;
+  r.in_stride = r.out_stride = (long long)rows * cols;
+  r.tw = twc;
+  r.rows = rows;
   r.mode = ROW_FFT;
   r.inv = inv;
   r.scale = 1.f;
-  PTY_CK(row_launcher(t->p.cols)(r, 1, t->st));
+  PTY_CK(rl(r, batch, st));
   ColArgs c{};
   c.in = out;
   c.out = out;
-  c.in_stride = c.out_stride = t->npx;
-  c.tw = t->tw_r;
-  c.cols = t->p.cols;
+  c.in_stride = c.out_stride = (long long)rows * cols;
+  c.tw = twr;
+  c.cols = cols;
   c.mode = COL_FFT;
   c.inv = inv;
   c.scale = 1.f;
-  PTY_CK(col_launcher(t->p.rows)(c, 1, t->st));
+  PTY_CK(cl(c, batch, st));
   return CDX_OK;
+}
+
+int fft2(cdx_pty* t, const float2* in, float2* out, bool inv, int batch = 1) {
+  return fft2g(t->st, in, out, inv, t->p.rows, t->p.cols, t->tw_r, t->tw_c, row_launcher(t->p.cols),
+               col_launcher(t->p.rows), batch);
 }
 
 // propagator::angularSpectrumPropagate(Reverse) of P in place (src/post_gpu/propagator.cc:31-49),
@@ -696,7 +851,8 @@ PtyArgs pass_args(cdx_pty* t, int k, bool probe_phase, bool noise_proj = false) 
 }
 
 // One sweep of ptycho::iterate (util/ptycho.cpp:484-690) for the iteration the device counter names.
-int enqueue_sweep(cdx_pty* t, bool probe_phase, bool noise_proj, bool fista, bool probe_momentum, bool zernike) {
+int enqueue_sweep(cdx_pty* t, bool probe_phase, bool noise_proj, bool fista, bool probe_momentum, bool zernike,
+                  bool posupd) {
   cudaStream_t st = t->st;
   const long long n = t->npx, on = t->onpx;
   PTY_CK(cudaMemsetAsync(t->scal->maxb, 0, sizeof(t->scal->maxb), st));
@@ -709,17 +865,54 @@ int enqueue_sweep(cdx_pty* t, bool probe_phase, bool noise_proj, bool fista, boo
     k_pty_scale<<<grid1(n), 256, 0, st>>>(t->P, t->Pp, n, &t->scal->isf);
   }
   PTY_CK(cudaGetLastError());
-  for (int k = 0; k < t->p.nscan; ++k) {
+  const int rows = t->p.rows, cols = t->p.cols, ns = t->p.nscan;
+  for (int k = 0; k < ns; ++k) {
     PtyArgs a = pass_args(t, k, probe_phase, noise_proj);
     a.tw = t->tw_c;
     PTY_CK(t->kc.fwd(a, st));
+    if (posupd) {   // updatePosition (util/ptycho.cpp:360-385) before the projection
+      ColArgs c{};   // Fn: the column FFT of W, row-major
+      c.in = t->W;
+      c.out = t->fn;
+      c.in_tiled = 1;
+      c.in_stride = t->pat_stride;
+      c.out_stride = n;
+      c.tw = t->tw_r;
+      c.cols = cols;
+      c.mode = COL_FFT;
+      c.scale = 1.f;
+      PTY_CK(col_launcher(rows)(c, 1, st));
+      k_pty_pos_window<<<grid1(n), 256, 0, st>>>(t->O, t->p.obj_rows, t->p.obj_cols, t->win, t->order, t->iter, ns, k,
+                                                  t->gw, rows, cols);
+      PTY_RET(fft2(t, t->gw, t->dxy, false));
+      const float nrm = (float)(1. / ((double)rows * cols));
+      k_pty_pos_deriv<<<grid1(n), 256, 0, st>>>(t->dxy, rows, cols, std::sqrt(nrm), nrm);
+      PTY_RET(fft2(t, t->dxy, t->dtmp, true, 2));
+      k_pty_pos_probe<<<grid1(n), 256, 0, st>>>(t->dtmp, t->P, n);
+      PTY_RET(fft2(t, t->dtmp, t->dxy, false, 2));
+      k_pty_pos_partial<<<kRedBlocks, 256, 0, st>>>(t->fn, t->dxy, t->pats, t->pat_stride, t->p.use_bs ? t->bs : nullptr,
+                                                    rows, cols, t->tl, a.norm, t->order, t->iter, ns, k, t->part,
+                                                    t->cnt + 4, t->grad);
+      PTY_CK(cudaGetLastError());
+    }
     a.tw = t->tw_r;
     PTY_CK(t->kr.col(a, st));
     a.tw = t->tw_c;
     PTY_CK(t->kc.upd(a, st));
   }
+  if (probe_phase) k_pty_add_step<<<grid1(n), 256, 0, st>>>(t->P, t->step, n);
+  if (posupd) {   // util/ptycho.cpp:567-585: new shifts, mean removed, the object shifted by it
+    k_pty_pos_update<<<1, 32, 0, st>>>(t->shifts, t->grad, t->scanpos, t->win, ns, (float)t->p.position_uncertainty,
+                                       t->pmean);
+    float2* objs[2] = {t->O, t->Op};
+    for (float2* o : objs) {
+      PTY_RET(fft2g(st, o, t->otmp, false, t->p.obj_rows, t->p.obj_cols, t->tw_or, t->tw_oc, t->orow, t->ocol, 1));
+      k_pty_pos_oshift<<<grid1(on), 256, 0, st>>>(t->otmp, t->p.obj_rows, t->p.obj_cols, t->pmean);
+      PTY_RET(fft2g(st, t->otmp, o, true, t->p.obj_rows, t->p.obj_cols, t->tw_or, t->tw_oc, t->orow, t->ocol, 1));
+    }
+    PTY_CK(cudaGetLastError());
+  }
   if (probe_phase) {
-    k_pty_add_step<<<grid1(n), 256, 0, st>>>(t->P, t->step, n);
     PTY_RET(angular_spectrum(t, t->P, true));
     if (zernike)   // util/ptycho.cpp:619-621: zernike_compute + zernike_reconstruct on the crop
       PTY_CK(zk_fit(t->P, t->p.rows, t->p.cols, (int)t->p.pupil_size, t->zk_tab, t->zk_part, t->zk_coef, st));
@@ -748,13 +941,17 @@ int enqueue_sweep(cdx_pty* t, bool probe_phase, bool noise_proj, bool fista, boo
 
 // sweep kind of iteration `it`: phase 0 object, 1 probe, 2 probe with applyMod; + 3 with the
 // FISTA object step (it < zernikeIter); + 6 with the probe momentum (dozernike with mPIE);
-// + 12 with the Zernike pupil fit (dozernike in the probe phase)
+// + 12 with the Zernike pupil fit (dozernike in the probe phase); + 24 with the scan-position
+// refinement (every 20 sweeps from 500 when position_uncertainty > 0)
+bool pos_update(const cdx_pty* t, int it) {
+  return t->p.position_uncertainty > 0 && it >= kPositionUpdateIter && it % 20 == 0;
+}
 int sweep_kind(const cdx_pty* t, int it) {
   const int phase = it < kUpdateProbeIter ? 0 : (it < kNoiseProjIter ? 1 : 2);
   const bool fista = it < t->p.zernike_iter;
   const bool dozernike = fista && it % 10 == 0;
   const bool pmom = dozernike && t->p.mpie;
-  return phase + (fista ? 3 : 0) + (pmom ? 6 : 0) + (dozernike && phase > 0 ? 12 : 0);
+  return phase + (fista ? 3 : 0) + (pmom ? 6 : 0) + (dozernike && phase > 0 ? 12 : 0) + (pos_update(t, it) ? 24 : 0);
 }
 
 int ensure_graph(cdx_pty* t, int kind) {
@@ -763,7 +960,8 @@ int ensure_graph(cdx_pty* t, int kind) {
   cudaGraph_t graph = nullptr;
   PTY_CK(cudaStreamBeginCapture(t->st, cudaStreamCaptureModeThreadLocal));
   const int phase = kind % 3;
-  const int r = enqueue_sweep(t, phase >= 1, phase == 2, (kind / 3) % 2 == 1, (kind / 6) % 2 == 1, kind >= 12);
+  const int r = enqueue_sweep(t, phase >= 1, phase == 2, (kind / 3) % 2 == 1, (kind / 6) % 2 == 1, (kind / 12) % 2 == 1,
+                              kind >= 24);
   const cudaError_t e = cudaStreamEndCapture(t->st, &graph);
   if (r != CDX_OK) {
     if (graph) cudaGraphDestroy(graph);
@@ -847,9 +1045,26 @@ int cdx_pty_create(const cdx_pty_params* p, void* stream, cdx_pty** out) {
       (r = dalloc(&t->pupil, t->npx)) || (r = dalloc(&t->W, t->pat_stride)) ||
       (r = dalloc(&t->pats, t->pat_stride * p->nscan)) || (r = dalloc(&t->bs, t->pat_stride)) ||
       (r = dalloc(&t->win, p->nscan)) || (r = dalloc(&t->tpos, p->nscan)) || (r = dalloc(&t->iter, 1)) ||
-      (r = dalloc(&t->scal, 1)) || (r = dalloc(&t->part, 3 * kRedBlocks)) || (r = dalloc(&t->cnt, 4)) || (r = dalloc(&t->derr, 1)) || (r = dalloc(&t->Pp, t->npx)) ||
+      (r = dalloc(&t->scal, 1)) || (r = dalloc(&t->part, 3 * kRedBlocks)) || (r = dalloc(&t->cnt, 5)) || (r = dalloc(&t->derr, 1)) || (r = dalloc(&t->Pp, t->npx)) ||
       (r = dalloc(&t->fista, p->zernike_iter > 0 ? t->onpx : 1)))
     return fail(r);
+  if (p->position_uncertainty > 0) {   // the refinement's buffers; the object transform if its size is supported
+    const int ns2 = 2 * p->nscan;
+    if ((r = dalloc(&t->shifts, ns2)) || (r = dalloc(&t->grad, ns2)) || (r = dalloc(&t->scanpos, ns2)) ||
+        (r = dalloc(&t->pmean, 2)) || (r = dalloc(&t->fn, t->npx)) || (r = dalloc(&t->gw, t->npx)) ||
+        (r = dalloc(&t->dxy, 2 * t->npx)) || (r = dalloc(&t->dtmp, 2 * t->npx)))
+      return fail(r);
+    t->orow = row_launcher(p->obj_cols);
+    t->ocol = col_launcher(p->obj_rows);
+    if (t->orow && t->ocol) {
+      e = prep_launcher(p->obj_rows)();
+      if (e == cudaSuccess) e = prep_launcher(p->obj_cols)();
+      if (e != cudaSuccess) return fail(set_error(CDX_ERR_CUDA, std::string("object FFT set-up: ") + cudaGetErrorString(e)));
+      if ((r = device_twiddles(p->obj_rows, &t->tw_or)) || (r = device_twiddles(p->obj_cols, &t->tw_oc)) ||
+          (r = dalloc(&t->otmp, t->onpx)))
+        return fail(r);
+    }
+  }
   if (p->zernike_iter > kUpdateProbeIter) {   // Zernike sweeps are possible: the fit's buffers and pixel table
     if ((r = dalloc(&t->zk_tab, (size_t)pd * pd)) || (r = dalloc(&t->zk_part, (size_t)zk_blocks(pd) * kZkModes)) ||
         (r = dalloc(&t->zk_coef, kZkModes)))
@@ -862,7 +1077,7 @@ int cdx_pty_create(const cdx_pty_params* p, void* stream, cdx_pty** out) {
   if (e == cudaSuccess) e = cudaMemsetAsync(t->bs, 0, sizeof(float) * t->pat_stride, t->st);
   if (e == cudaSuccess) e = cudaMemsetAsync(t->step, 0, sizeof(float2) * t->npx, t->st);
   if (e == cudaSuccess) e = cudaMemsetAsync(t->scal, 0, sizeof(PtyScal), t->st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(t->cnt, 0, sizeof(unsigned) * 4, t->st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(t->cnt, 0, sizeof(unsigned) * 5, t->st);
   if (e == cudaSuccess) e = cudaMemsetAsync(t->derr, 0, sizeof(int), t->st);
   if (e == cudaSuccess && p->use_bs) {
     k_pty_beamstop<<<grid1(t->npx), 256, 0, t->st>>>(t->bs, p->rows, p->cols, t->tl, (float)p->beam_stop_size);
@@ -890,7 +1105,8 @@ int cdx_pty_destroy(cdx_pty* t) {
     if (g) cudaGraphExecDestroy(g);
   void* bufs[] = {t->O, t->Op, t->P, t->step, t->W, t->tmp, t->pupil, t->pats, t->bs, t->msum, t->coef,
                   t->win, t->tpos, t->order, t->iter, t->scal, t->part, t->cnt, t->derr, t->Pp, t->fista,
-                  t->coefz, t->zk_tab, t->zk_part, t->zk_coef};
+                  t->coefz, t->zk_tab, t->zk_part, t->zk_coef, t->shifts, t->grad, t->scanpos, t->pmean, t->fn,
+                  t->gw, t->dxy, t->dtmp, t->otmp};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (t->e0) cudaEventDestroy(t->e0);
@@ -912,6 +1128,11 @@ int cdx_pty_set_scan(cdx_pty* t, const float* posx, const float* posy) {
   }
   PTY_CK(cudaMemcpyAsync(t->win, w.data(), sizeof(int2) * ns, cudaMemcpyHostToDevice, t->st));
   PTY_CK(cudaMemcpyAsync(t->tpos, tp.data(), sizeof(int2) * ns, cudaMemcpyHostToDevice, t->st));
+  t->win0 = w;
+  if (t->scanpos) {   // scanposx then scanposy, for the refined window origins
+    PTY_CK(cudaMemcpyAsync(t->scanpos, posx, sizeof(float) * ns, cudaMemcpyHostToDevice, t->st));
+    PTY_CK(cudaMemcpyAsync(t->scanpos + ns, posy, sizeof(float) * ns, cudaMemcpyHostToDevice, t->st));
+  }
   PTY_CK(cudaStreamSynchronize(t->st));
   t->have_scan = true;
   return CDX_OK;
@@ -1051,9 +1272,9 @@ int cdx_pty_simulate(cdx_pty* t) {
 int cdx_pty_iterate(cdx_pty* t, int first_iter, int n_iter, const int* orders, unsigned int seed) {
   if (!t) return set_error(CDX_ERR_ARG, "null argument");
   if (first_iter < 0 || n_iter < 0) return set_error(CDX_ERR_ARG, "negative iteration index or count");
-  if (first_iter + n_iter > kPositionUpdateIter && t->p.position_uncertainty > 0)
-    return set_error(CDX_ERR_ARG, "iterations from 500 on refine the scan positions (position_uncertainty > 0), "
-                                  "which is not built: first_iter + n_iter must be <= 500");
+  if (first_iter + n_iter > kPositionUpdateIter && t->p.position_uncertainty > 0 && !(t->orow && t->ocol))
+    return set_error(CDX_ERR_SIZE, "the scan-position refinement from iteration 500 (position_uncertainty > 0) "
+                                   "shifts the object by FFT: object rows and cols must be 2^a 3^b in [16, 4096]");
   if (!t->have_scan || !t->have_pats || !t->have_obj || !t->have_probe)
     return set_error(CDX_ERR_STATE, "scan positions, patterns, object and probe must be set first");
   const int ns = t->p.nscan;
@@ -1102,6 +1323,10 @@ int cdx_pty_iterate(cdx_pty* t, int first_iter, int n_iter, const int* orders, u
   PTY_CK(cudaMemsetAsync(t->Op, 0, sizeof(float2) * t->onpx, st));
   PTY_CK(cudaMemsetAsync(t->step, 0, sizeof(float2) * t->npx, st));
   PTY_CK(cudaMemsetAsync(t->Pp, 0, sizeof(float2) * t->npx, st));
+  if (t->shifts) {   // resetPosition (util/ptycho.cpp:299-303): zero shifts, the nominal windows
+    PTY_CK(cudaMemsetAsync(t->shifts, 0, sizeof(float) * 2 * t->p.nscan, st));
+    PTY_CK(cudaMemcpyAsync(t->win, t->win0.data(), sizeof(int2) * t->p.nscan, cudaMemcpyHostToDevice, st));
+  }
   PTY_CK(cudaMemsetAsync(t->msum, 0, sizeof(float) * t->onpx, st));
   PTY_CK(cudaMemsetAsync(t->iter, 0, sizeof(int), st));
   k_pty_masksum<<<grid1(t->npx * ns), 256, 0, st>>>(t->msum, t->tpos, ns, t->p.rows, t->p.cols, t->p.obj_rows,

@@ -350,6 +350,69 @@ def fresnel_phase(a, factor):
     return np.where(a != 0, (a * p).astype(C64), a).astype(C64)
 
 
+# ------------------------------------------------------- position refinement
+DELTA = F32(1e-3)        # src/gpu/ptycho.cu:7
+POSITION_STEP = F32(0.3)  # util/ptycho.cpp:569
+
+
+def position_gradient(w, P, Fn, pattern, bs=None):
+    """ptycho::updatePosition (util/ptycho.cpp:360-385) with calcPartial (src/gpu/ptycho.cu:156-169):
+    the window's spectrum, centred and scaled by sqrt(1/n), times (x/rows - 0.5) and
+    (y/cols - 0.5), back to FFT order scaled by 1/n, inverse transforms, times the probe,
+    forward transforms; per pixel (Fn.x d.y - Fn.y d.x)(1 - sqrt((I + 1e-3)/(|Fn|^2 + 1e-3)))
+    (zero under the beamstop) summed.  Fn is the exit wave's transform times 1/sqrt(n).
+    Returns (gx, gy)."""
+    rows, cols = w.shape
+    nrm = F32(1.0 / (rows * cols))
+    s1 = F32(math.sqrt(nrm))
+    spec = np.fft.fftshift(fft2_u(w.astype(C64))).astype(C64)
+    spec = (spec * s1).astype(C64)
+    sx = ((np.arange(rows, dtype=F32) * F32(1.0 / rows)).astype(F32) - F32(0.5)).astype(F32)[:, None]
+    sy = ((np.arange(cols, dtype=F32) * F32(1.0 / cols)).astype(F32) - F32(0.5)).astype(F32)[None, :]
+    fact = np.maximum((pattern.astype(F32) + DELTA).astype(F32), F32(0))
+    fm2 = (Fn.real * Fn.real + Fn.imag * Fn.imag).astype(F32)
+    k = (F32(1) - np.sqrt((fact / (fm2 + DELTA).astype(F32)).astype(F32)).astype(F32)).astype(F32)
+    out = []
+    for sc in (sx, sy):
+        d = np.fft.ifftshift((spec * sc).astype(C64)).astype(C64)
+        d = (d * nrm).astype(C64)
+        d = (ifft2_u(d) * P).astype(C64)
+        d = fft2_u(d)
+        part = ((Fn.real * d.imag).astype(F32) - (Fn.imag * d.real).astype(F32)).astype(F32)
+        part = (part * k).astype(F32)
+        if bs is not None:
+            part = np.where(bs > F32(0.5), F32(0), part)
+        out.append(F32(part.astype(np.float64).sum()))
+    return out[0], out[1]
+
+
+def shift_wave(wave, shiftx, shifty):
+    """shiftWave (src/post_gpu/misc.cc:97-113): FFT, centre, multiplyShift
+    (cudaConfig.cu:373-378) by (shiftx, shifty), back to FFT order, times 1/(rows cols),
+    inverse FFT."""
+    rows, cols = wave.shape
+    spec = np.fft.fftshift(fft2_u(wave.astype(C64))).astype(C64)
+    spec = multiply_shift(spec, shiftx, shifty)
+    spec = (np.fft.ifftshift(spec) * F32(1.0 / (rows * cols))).astype(C64)
+    return ifft2_u(spec).astype(C64)
+
+
+def add_probability(shifts, grad, sigma):
+    """addProbability (cudaConfig.cu:808-817): d + v (v = 0.3 grad), damped by
+    exp(-(d + v)^2 / (2 sigma^2)) when the step moves away from zero."""
+    out = shifts.astype(F32).copy()
+    for j in range(out.size):
+        d = F32(out.flat[j])
+        v = F32(F32(grad.flat[j]) * POSITION_STEP)
+        t = F32(d + v)
+        if abs(t) > abs(d):
+            g = F32(math.exp(float(-F32(F32(F32(t * t) / F32(2)) / F32(F32(sigma) * F32(sigma))))))
+            out.flat[j] = F32(d + F32(v * g))
+        else:
+            out.flat[j] = t
+    return out
+
+
 # ------------------------------------------------------- Zernike pupil fit
 ZERNIKE_MAX_N = 40                      # util/ptycho.cpp:439
 ZERNIKE_REG_L, ZERNIKE_REG_M = F32(5e-5), F32(5e-8)   # beamDecomposition.cu:585-588
@@ -600,8 +663,6 @@ def iterate(obj0, probe0, patterns, scanx, scany, n_iter, params: PtyParams, ord
     removed, as the reference leaves them.  Returns (object, pupil)."""
     rows, cols = probe0.shape
     orow, ocol = obj0.shape
-    if start_iter + n_iter > POSITION_UPDATE_ITER and params.position_uncertainty > 0:
-        raise ValueError("position refinement (iterations >= 500, positionUncertainty > 0) is outside this restatement")
     O = obj0.astype(C64).copy()
     Oprev = np.zeros_like(O)
     P = probe0.astype(C64).copy()
@@ -617,7 +678,7 @@ def iterate(obj0, probe0, patterns, scanx, scany, n_iter, params: PtyParams, ord
     msum = masksum(rows, cols, orow, ocol, scanx, scany, params.pupil_size)
     bs = circle_mask(rows, cols, rows >> 1, cols >> 1, params.beam_stop_size, True) if params.use_bs else None
     tk = F32(0.5 + math.sqrt(1.25))
-    wins = [(c_round(F32(x)), c_round(F32(y))) for x, y in zip(scanx, scany)]
+    shifts = np.zeros((2, len(scanx)), F32)    # d_shifts (util/ptycho.cpp:110-113), zero at the start
     fres = fresnel_factor(params.lam, params.d, params.pixelsize, rows) if params.is_fresnel else None
     for it in range(start_iter, start_iter + n_iter):
         probe_max = F32(np.max((P.real * P.real + P.imag * P.imag).astype(F32)))
@@ -637,17 +698,25 @@ def iterate(obj0, probe0, patterns, scanx, scany, n_iter, params: PtyParams, ord
             P = (P * F32(1.0 / np.float64(sf))).astype(C64)
             Pprev = (Pprev * F32(1.0 / np.float64(sf))).astype(C64)     # util/ptycho.cpp:507
             obj_max = probe_max = F32(math.sqrt(np.float64(F32(obj_max * probe_max))))
+        update_pos = it % 20 == 0 and it >= POSITION_UPDATE_ITER      # util/ptycho.cpp:511
+        grad = np.zeros((2, nscan), F32)
         for i in orders[it - start_iter]:
-            sx, sy = wins[i]
+            sx = c_round(F32(F32(scanx[i]) + shifts[0, i]))
+            sy = c_round(F32(F32(scany[i]) + shifts[1, i]))
             w = get_window(O, sx, sy, rows, cols)
             esw = (P * w).astype(C64)
             if fres is not None:                  # util/ptycho.cpp:526-528
                 esw = fresnel_phase(esw, fres)
             F = fft2_u(esw)
+            pnorm = norm
+            if update_pos:                        # util/ptycho.cpp:533-538: Fn * norm first
+                F = (F * norm).astype(C64)
+                pnorm = F32(1)
+                grad[0, i], grad[1, i] = position_gradient(w, P, F, patterns[i], bs)
             if it < NOISE_PROJ_ITER:
-                F = apply_mod_accurate(F, patterns[i], norm, scale, bs)
+                F = apply_mod_accurate(F, patterns[i], pnorm, scale, bs)
             else:
-                F = apply_mod_noise(F, patterns[i], norm, scale, params.noise_level, bs)
+                F = apply_mod_noise(F, patterns[i], pnorm, scale, params.noise_level, bs)
             F = (ifft2_u(F) * norm).astype(C64)
             diff = (esw - F).astype(C64)
             if fres is not None:                  # removeFresnelPhase (util/ptycho.cpp:551)
@@ -661,6 +730,16 @@ def iterate(obj0, probe0, patterns, scanx, scany, n_iter, params: PtyParams, ord
         if it >= UPDATE_PROBE_ITER:
             P = (P + step).astype(C64)
             step = (step * F32(0)).astype(C64)
+        if update_pos:                            # util/ptycho.cpp:567-585
+            with np.errstate(divide="ignore", over="ignore", invalid="ignore"):
+                shifts = add_probability(shifts, grad, F32(params.position_uncertainty))
+            mx = F32(F32(shifts[0].astype(np.float64).sum()) / F32(nscan))
+            my = F32(F32(shifts[1].astype(np.float64).sum()) / F32(nscan))
+            shifts[0] = (shifts[0] - mx).astype(F32)
+            shifts[1] = (shifts[1] - my).astype(F32)
+            O = shift_wave(O, -mx, -my)
+            Oprev = shift_wave(Oprev, -mx, -my)
+        if it >= UPDATE_PROBE_ITER:
             P = angular_spectrum(P, params.lam, params.dpupil, res, reverse=True)
             r0, c0 = (rows - pd) // 2, (cols - pd) // 2
             if it < params.zernike_iter and it % 10 == 0:    # dozernike (util/ptycho.cpp:619-621)

@@ -10,9 +10,11 @@
 // pty_harness <object.bin> <probe.bin> <patterns.bin (nscan stacked, FFT order,
 //             scaled 1/exposure)> <scan.txt ("x y" per line)> <nIter> <mPIE>
 //             <lambda> <d> <dpupil> <pixelsize> <pupilSize> <exposure>
-//             <useBS> <beamStopSize> <rand seed> <out prefix> [noiseLevel [zernikeIter [isFresnel]]]
+//             <useBS> <beamStopSize> <rand seed> <out prefix>
+//             [noiseLevel [zernikeIter [isFresnel [positionUncertainty]]]]
 // (zernikeIter > 0 runs the FISTA object step, the probe momentum and, from
-// iteration 400, the Zernike pupil fit; isFresnel the exit wave's Fresnel phase)
+// iteration 400, the Zernike pupil fit; isFresnel the exit wave's Fresnel phase;
+// positionUncertainty > 0 the scan-position refinement every 20 sweeps from 500)
 #define main cdxref_ptycho_main
 #include CDXREF_PTYCHO_CPP
 #undef main
@@ -53,7 +55,7 @@ int main(int argc, char** argv) {
   p.saveVideoEveryIter = 0;
   p.computeErrorEveryIter = 0;
   p.zernikeIter = argc > 18 ? atoi(argv[18]) : 0;
-  p.positionUncertainty = 0;
+  p.positionUncertainty = argc > 20 ? atof(argv[20]) : 0;
   p.nIter = atoi(argv[5]);
   p.mPIE = atoi(argv[6]);
   p.lambda = atof(argv[7]);

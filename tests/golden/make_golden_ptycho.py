@@ -49,11 +49,16 @@ CASES = [
     ("zernike412_mpie", 412, 1, 0, 5, 1.0, 40.0, "grid", 7),
     ("fresnel30", 30, 1, 0, 5, 1.0, 40.0, "grid", 5),
     ("fresnel405", 405, 0, 0, 5, 1.0, 40.0, "grid", 3),
+    ("posref541", 541, 0, 0, 5, 1.0, 40.0, "grid", 7),
 ]
 NOISE_LEVEL = {"noise2003": 20}
 # FISTA object step (and the probe momentum every 10); from 400 the Zernike pupil fit every 10
 ZERNIKE_ITER = {"fista45": 35, "fista405": 300, "zernike412": 1200, "zernike412_mpie": 1200}
 FRESNEL = {"fresnel30", "fresnel405"}   # isFresnel: the exit waves take the Fresnel phase of distance d
+# positionUncertainty: the scan-position refinement every 20 sweeps from 500; the patterns are
+# simulated at positions off the nominal ones by whole pixels
+UNCERTAINTY = {"posref541": 2.0}
+TRUE_OFFSETS = {"posref541": ([1, -1, 0, 2, 0, -1, 1, 0, -2], [0, 1, -1, 0, 2, 0, -1, 1, 0])}
 OPTICS = dict(lam=0.5, d=2e4, dpupil=1e3, pixelsize=20.0, pupil_size=16.0)
 
 
@@ -90,7 +95,8 @@ def main(ref=None):
             probe_t = PO.angular_spectrum(PO.pupil_func(R, R, OPTICS["pupil_size"]), OPTICS["lam"],
                                           OPTICS["dpupil"], res)
             fres = PO.fresnel_factor(OPTICS["lam"], OPTICS["d"], OPTICS["pixelsize"], R) if name in FRESNEL else 0.0
-            pats = PO.simulate_patterns(truth_object(rng), probe_t, sx, sy, 1.0, fresnel=fres)
+            ox, oy = (np.array(v, np.float32) for v in TRUE_OFFSETS.get(name, (np.zeros(len(sx)), np.zeros(len(sy)))))
+            pats = PO.simulate_patterns(truth_object(rng), probe_t, sx + ox, sy + oy, 1.0, fresnel=fres)
             pats = (pats / pats.max() * np.float32(pscale / expo)).astype(np.float32)
             obj0 = np.exp(2j * np.pi * rng.random((RO, RO))).astype(np.complex64)
             probe0 = PO.angular_spectrum(PO.pupil_func(R, R, OPTICS["pupil_size"]), OPTICS["lam"],
@@ -104,7 +110,8 @@ def main(ref=None):
             cmd = [str(harness), f"{d}/obj.bin", f"{d}/probe.bin", f"{d}/pats.bin", f"{d}/scan.txt", str(n_iter),
                    str(mpie), str(OPTICS["lam"]), str(OPTICS["d"]), str(OPTICS["dpupil"]), str(OPTICS["pixelsize"]),
                    str(OPTICS["pupil_size"]), str(expo), str(use_bs), str(bss), str(seed), f"{d}/out",
-                   str(NOISE_LEVEL.get(name, 0)), str(ZERNIKE_ITER.get(name, 0)), str(int(name in FRESNEL))]
+                   str(NOISE_LEVEL.get(name, 0)), str(ZERNIKE_ITER.get(name, 0)), str(int(name in FRESNEL)),
+                   str(UNCERTAINTY.get(name, 0.0))]
             subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL)
             p = f"{name}/"
             data[p + "obj0"] = obj0
@@ -116,6 +123,7 @@ def main(ref=None):
             data[p + "cfg"] = np.array([n_iter, mpie, use_bs, bss, seed, NOISE_LEVEL.get(name, 0),
                                         ZERNIKE_ITER.get(name, 0), int(name in FRESNEL)], np.int64)
             data[p + "exposure"] = np.float64(expo)
+            data[p + "uncertainty"] = np.float64(UNCERTAINTY.get(name, 0.0))
             data[p + "ref_object"] = read_bin(f"{d}/out_object.bin").copy()
             data[p + "ref_pupil"] = read_bin(f"{d}/out_pupil.bin").copy()
             print(name, "done")

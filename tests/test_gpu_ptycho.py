@@ -165,6 +165,27 @@ def test_one_fresnel_sweep_matches_oracle(PT, first, mpie):
         assert np.linalg.norm(t.patterns - ref) / np.linalg.norm(ref) < 2e-6
 
 
+@pytest.mark.parametrize("first", [500, 520])
+@pytest.mark.parametrize("mpie", [False, True])
+def test_position_update_sweep_matches_oracle(PT, first, mpie):
+    """A sweep with the scan-position refinement (positionUncertainty 2): gradients per
+    position, new shifts, the object shifted by their mean; against the oracle."""
+    c, prm, _n, _s = load("posref541")
+    prm.mpie = mpie
+    rng = np.random.default_rng(first)
+    obj = (c["obj0"] * (0.5 + rng.random(c["obj0"].shape))).astype(np.complex64)
+    orders = np.array([rng.permutation(len(c["scanx"]))], np.int32)
+    with make(PT, c, prm) as t:
+        t.objectWave = obj
+        t.iterate(1, first_iter=first, orders=orders)
+        O, pupil, P = PO.iterate(obj, c["probe0"], c["pats"], c["scanx"], c["scany"], 1, prm, orders, start_iter=first)
+        assert PO.rel_err(t.objectWave, O) < STEP_BOUND
+        assert PO.rel_err(t.probe, P) < STEP_BOUND
+        prm.position_uncertainty = 0.0           # without the refinement the sweep ends elsewhere
+        O0, _pu, _P = PO.iterate(obj, c["probe0"], c["pats"], c["scanx"], c["scany"], 1, prm, orders, start_iter=first)
+        assert PO.rel_err(t.objectWave, O0) > 10 * STEP_BOUND
+
+
 def test_simulate_matches_oracle(PT):
     c, prm, _n, _s = load("offedge")
     with make(PT, c, prm) as t:
@@ -194,8 +215,13 @@ def test_argument_checks(PT, cdx):
     c, prm, _n, _s = load("obj3")
     prm.position_uncertainty = 2.0
     with make(PT, c, prm) as t:
-        with pytest.raises(cdx.CdxError):
-            t.iterate(10, first_iter=495)          # position refinement from 500 is not built
+        t.iterate(10, first_iter=495)              # position refinement at 500 (64^2 object: FFT size)
+    c68 = dict(c, obj0=np.ones((68, 68), np.complex64))
+    with make(PT, c68, prm) as t:
+        with pytest.raises(cdx.CdxError) as e:
+            t.iterate(10, first_iter=495)          # 68 = 4 x 17: no object transform for the shift
+        assert e.value.code == cdx.CDX_ERR_SIZE
+        t.iterate(5, first_iter=495)               # the run ends before the refinement
     prm.position_uncertainty = 0.0
     prm.zernike_iter = 1200
     with make(PT, c, prm) as t:
