@@ -41,7 +41,9 @@ typedef struct cdx_pty_params {
   int use_bs;              /* beamstop of radius beam_stop_size at the pattern centre (useBS) */
   int beam_stop_size;
   int noise_level;         /* noiseLevel: tolerance of the modulus projection from iteration 2000 */
-  double position_uncertainty; /* positionUncertainty: > 0 asks for scan-position refinement (not built) */
+  double position_uncertainty; /* positionUncertainty: > 0 refines the scan positions every 20 sweeps from
+                                  500 (util/ptycho.cpp:511-585); the object is shifted by FFT, so its sizes
+                                  must then be 2^a 3^b in [16, 4096] */
   int zernike_iter;        /* zernikeIter: before it the object takes a FISTA (TV) step each sweep and,
                               every tenth sweep, the probe a momentum step (with mPIE) and, from
                               iteration 400, the Zernike pupil fit (861 modes up to order 40) in place of
@@ -104,7 +106,9 @@ int cdx_pty_simulate(cdx_pty* t);
  * 20 sweeps; with position_uncertainty = 0 (its default) that step leaves
  * the positions at zero shift and the object unchanged up to the rounding of
  * an FFT round trip, which is not repeated here; with position_uncertainty > 0
- * runs past iteration 500 are refused (refinement not built).  The final
+ * the shifts are refined (zero at the start of each call) and the object is
+ * shifted by their mean (object sizes 2^a 3^b, else CDX_ERR_SIZE for runs past
+ * iteration 500).  The final
  * object has its global phase removed (util/ptycho.cpp:731-735). */
 int cdx_pty_iterate(cdx_pty* t, int first_iter, int n_iter, const int* orders, unsigned int seed);
 
