@@ -165,6 +165,19 @@ __global__ void k_ccd_noise(float* __restrict__ I, long long n, double noise_lev
   }
 }
 
+// ccdRecord(data, wave, noiseLevel, state, exposure) on a float pattern (src/gpu/cdi.cu:260-266):
+// k = Poisson(noiseLevel + rcolor I exposure), clamped below rcolor, I <- (k - noiseLevel) / rcolor,
+// then times `post` (the caller's applyNorm)
+__global__ void k_ccd_record(float* __restrict__ I, long long n, int noise_level, float exposure, int rcolor,
+                             float post, unsigned long long seed) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double lam = (double)((float)noise_level + (float)rcolor * I[i] * exposure);
+    int k = (int)poisson_sample(lam > 0 ? lam : 0.0, seed, 0x43434452ull, (unsigned long long)i);
+    if (k >= rcolor) k = rcolor - 1;
+    I[i] = (float)(k - noise_level) / (float)rcolor * post;
+  }
+}
+
 }  // namespace fm
 }  // namespace cdx
 
@@ -253,5 +266,17 @@ extern "C" int cdx_fresnel_phase(void* field, int rows, int cols, int batch, flo
   k_fresnel_phase<<<g, 256, 0, (cudaStream_t)stream>>>((float2*)field, rows, cols, n, factor);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return set_error(CDX_ERR_CUDA, std::string("Fresnel phase: ") + cudaGetErrorString(e));
+  return CDX_OK;
+}
+
+extern "C" int cdx_ccd_record(float* pattern, long long count, int noise_level, float exposure, int rcolor, float post,
+                              unsigned long long seed, void* stream) {
+  if (!pattern || count < 0 || noise_level < 0 || !(exposure > 0.f) || rcolor <= 0)
+    return set_error(CDX_ERR_ARG, "bad CCD-record argument");
+  if (count == 0) return CDX_OK;
+  const int g = (int)std::min<long long>((count + 255) / 256, 152 * 32);
+  k_ccd_record<<<g, 256, 0, (cudaStream_t)stream>>>(pattern, count, noise_level, exposure, rcolor, post, seed);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return set_error(CDX_ERR_CUDA, std::string("ccd record: ") + cudaGetErrorString(e));
   return CDX_OK;
 }

@@ -646,15 +646,21 @@ __global__ void k_pty_random(float2* __restrict__ O, long long n, unsigned long 
 
 // createPattern's getMod2(pattern, esw, 1/(rows cols)), applyNorm(exposure),
 // applyNorm(1/exposure) (util/ptycho.cpp:336-358), stored column-tiled
+// (with useBS, applySupport(pattern, beamstop) zeroes the stopped pixels; with simCCDbit the
+// exposure scalings are left to the detector model that follows)
 __global__ void k_pty_sim_mod2(const float2* __restrict__ F, float* __restrict__ out, int rows, int cols, int tl,
-                               float inv_n, float expo, float inv_expo) {
+                               float inv_n, float expo, float inv_expo, const float* __restrict__ bs, int ccd) {
   const long long n = (long long)rows * cols;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const float2 v = F[i];
+    const long long ti = pty_tiled((int)(i / cols), (int)(i % cols), rows, tl);
     float m = (v.x * v.x + v.y * v.y) * inv_n;
-    m *= expo;
-    m *= inv_expo;
-    out[pty_tiled((int)(i / cols), (int)(i % cols), rows, tl)] = m;
+    if (bs && bs[ti] > 0.f) m = 0.f;
+    if (!ccd) {
+      m *= expo;
+      m *= inv_expo;
+    }
+    out[ti] = m;
   }
 }
 
@@ -1228,8 +1234,8 @@ int cdx_pty_init_object(cdx_pty* t, unsigned long long seed) {
   return CDX_OK;
 }
 
-int cdx_pty_simulate(cdx_pty* t) {
-  if (!t) return set_error(CDX_ERR_ARG, "null argument");
+namespace {
+int simulate(cdx_pty* t, bool ccd, unsigned long long seed) {
   if (!t->have_scan || !t->have_obj || !t->have_probe)
     return set_error(CDX_ERR_STATE, "scan positions, object and probe must be set first");
   const int ns = t->p.nscan;
@@ -1261,12 +1267,28 @@ int cdx_pty_simulate(cdx_pty* t) {
     PTY_CK(col_launcher(t->p.rows)(c, 1, t->st));
     k_pty_sim_mod2<<<grid1(t->npx), 256, 0, t->st>>>(t->tmp, t->pats + k * t->pat_stride, t->p.rows, t->p.cols, t->tl,
                                                       (float)(1. / ((double)t->p.rows * t->p.cols)),
-                                                      (float)t->p.exposure, (float)(1. / t->p.exposure));
+                                                      (float)t->p.exposure, (float)(1. / t->p.exposure),
+                                                      t->p.use_bs ? t->bs : nullptr, ccd ? 1 : 0);
     PTY_CK(cudaGetLastError());
+    if (ccd)   // ccdRecord(pattern, pattern, noiseLevel, devstates, exposure), then applyNorm(1/exposure)
+      PTY_RET(cdx_ccd_record(t->pats + k * t->pat_stride, t->pat_stride, t->p.noise_level, (float)t->p.exposure,
+                             (int)kRcolor, (float)(1. / t->p.exposure), seed ^ (0x9E3779B97F4A7C15ull * (k + 1)),
+                             t->st));
   }
   PTY_CK(cudaStreamSynchronize(t->st));
   t->have_pats = true;
   return CDX_OK;
+}
+}  // namespace
+
+int cdx_pty_simulate(cdx_pty* t) {
+  if (!t) return set_error(CDX_ERR_ARG, "null argument");
+  return simulate(t, false, 0);
+}
+
+int cdx_pty_simulate_ccd(cdx_pty* t, unsigned long long seed) {
+  if (!t) return set_error(CDX_ERR_ARG, "null argument");
+  return simulate(t, true, seed);
 }
 
 int cdx_pty_iterate(cdx_pty* t, int first_iter, int n_iter, const int* orders, unsigned int seed) {

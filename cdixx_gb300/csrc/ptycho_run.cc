@@ -178,9 +178,8 @@ int main(int argc, char** argv) {
   if (cdx_pty_set_scan(t, sx.data(), sy.data()) != CDX_OK) die("cdx_pty_set_scan");
   const size_t n = (size_t)p.rows * p.cols;
   if (cfg.runSim) {
-    if (cfg.simCCDbit) fprintf(stderr, "note: simCCDbit is ignored (noise-free patterns)\n");
     if (cdx_pty_set_object(t, obj_truth.data()) != CDX_OK || cdx_pty_set_pupil(t, pupil.data()) != CDX_OK ||
-        cdx_pty_simulate(t) != CDX_OK)
+        (cfg.simCCDbit ? cdx_pty_simulate_ccd(t, 0x5eedull) : cdx_pty_simulate(t)) != CDX_OK)   // simCCDbit: ccdRecord
       die("createPattern");
     pats.resize(n * p.nscan);
     if (cdx_pty_get_patterns(t, pats.data()) != CDX_OK) die("cdx_pty_get_patterns");

@@ -129,6 +129,8 @@ _SIGS = {
     "cdx_pty_set_pupil": [_P, _P],
     "cdx_pty_init_object": [_P, ctypes.c_ulonglong],
     "cdx_pty_simulate": [_P],
+    "cdx_pty_simulate_ccd": [_P, ctypes.c_ulonglong],
+    "cdx_ccd_record": [_P, _LL, _I, _F, _I, _F, ctypes.c_ulonglong, _P],
     "cdx_pty_iterate": [_P, _I, _I, _P, ctypes.c_uint],
     "cdx_pty_last_ms": [_P, ctypes.POINTER(ctypes.c_float)],
     "cdx_pty_scan_orders": [_I, _I, ctypes.c_uint, _P],

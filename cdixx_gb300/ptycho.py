@@ -168,9 +168,13 @@ class Ptycho:
         """Random-phase unit object and the propagated pupil disk as probe (util/ptycho.cpp:363-369)."""
         check(lib().cdx_pty_init_object(self._h, seed))
 
-    def createPattern(self):
-        """Noise-free diffraction patterns of the current object and probe (util/ptycho.cpp:310-359)."""
-        check(lib().cdx_pty_simulate(self._h))
+    def createPattern(self, simCCDbit=False, seed=0):
+        """Diffraction patterns of the current object and probe (util/ptycho.cpp:310-359): noise
+        free, or recorded by the CCD model (ccdRecord) with simCCDbit."""
+        if simCCDbit:
+            check(lib().cdx_pty_simulate_ccd(self._h, ctypes.c_ulonglong(seed)))
+        else:
+            check(lib().cdx_pty_simulate(self._h))
 
     def iterate(self, n_iter, first_iter=0, orders=None, seed=1):
         """ptycho::iterate: n_iter sweeps from iteration index first_iter; scan orders given

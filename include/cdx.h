@@ -192,6 +192,12 @@ int cdx_ccd_noise(float* pattern, long long count, float noise_level, float expo
  * (y - cols/2)^2)) on the entries that are not zero. */
 float cdx_fresnel_factor(double lambda, double distance, double pixelsize, int rows, int remove);
 int cdx_fresnel_phase(void* field, int rows, int cols, int batch, float factor, void* stream);
+/* ccdRecord(data, wave, noiseLevel, state, exposure) (src/gpu/cdi.cu:260-266), the detector
+ * model of ptycho::createPattern with simCCDbit: on `count` floats of a DEVICE pattern,
+ * I <- (min(Poisson(noiseLevel + rcolor I exposure), rcolor - 1) - noiseLevel) / rcolor * post.
+ * Counter-based random numbers (seed, element index), not curand MRG32k3a states. */
+int cdx_ccd_record(float* pattern, long long count, int noise_level, float exposure, int rcolor, float post,
+                   unsigned long long seed, void* stream);
 /* cdx_fft2 with the FFT arithmetic chosen by fft_mode (CDX_FFT_*). */
 int cdx_fft2_ex(const void* in, void* out, int rows, int cols, int batch, int inverse, int fft_mode, void* stream);
 /* applyModAbs(source, target) with state NULL (cudaConfig.cu:827-841). */

@@ -91,9 +91,14 @@ int cdx_pty_set_pupil(cdx_pty* t, const float* pupil);
 int cdx_pty_init_object(cdx_pty* t, unsigned long long seed);
 
 /* createPattern without detector noise (util/ptycho.cpp:310-359): pattern i =
- * |FFT(probe * window_i(object))|^2 / (rows cols), from the current object and
- * probe, stored as the context's patterns. */
+ * |FFT(probe * window_i(object))|^2 / (rows cols) (zero under the beamstop with
+ * use_bs), from the current object and probe, stored as the context's patterns. */
 int cdx_pty_simulate(cdx_pty* t);
+/* createPattern with simCCDbit: the same intensities recorded by ccdRecord
+ * (Poisson(noise_level + rcolor I exposure), clamped below rcolor, minus
+ * noise_level, / rcolor; src/gpu/cdi.cu:260-266) and scaled by 1/exposure;
+ * counter-based random numbers keyed by seed, position and pixel. */
+int cdx_pty_simulate_ccd(cdx_pty* t, unsigned long long seed);
 
 /* ptycho::iterate: n_iter sweeps starting at iteration index first_iter
  * (the reference always starts at 0; from index 400 the probe is updated and

@@ -186,6 +186,33 @@ def test_position_update_sweep_matches_oracle(PT, first, mpie):
         assert PO.rel_err(t.objectWave, O0) > 10 * STEP_BOUND
 
 
+def test_simulate_ccd_record_statistics(PT):
+    """createPattern with simCCDbit: per pixel (Poisson(noiseLevel + rcolor I exposure), clamped
+    below rcolor, - noiseLevel) / rcolor / exposure.  Against the noise-free patterns of the
+    same context: the mean residual is unbiased and its variance is the Poisson one."""
+    c, prm, _n, _s = load("obj3")
+    prm.noise_level = 20
+    prm.exposure = 1e-3
+    with make(PT, c, prm) as t:
+        rng = np.random.default_rng(2)
+        truth = (np.exp(1j * rng.random(c["obj0"].shape)) * (0.5 + rng.random(c["obj0"].shape))).astype(np.complex64)
+        t.objectWave = truth
+        t.createPattern()
+        clean = t.patterns
+        t.createPattern(simCCDbit=True, seed=3)
+        noisy = t.patterns
+        t.createPattern(simCCDbit=True, seed=4)
+        noisy2 = t.patterns
+    rc, e, nl = 65535.0, prm.exposure, prm.noise_level
+    lam = nl + rc * clean.astype(np.float64) * e
+    live = lam < rc - 5 * np.sqrt(rc)                 # away from the clamp
+    z = (noisy.astype(np.float64) * rc * e + nl - lam) / np.sqrt(np.maximum(lam, 1e-9))
+    assert abs(z[live].mean()) < 0.05
+    assert abs(z[live].std() - 1) < 0.05
+    assert not np.array_equal(noisy, noisy2)
+    assert np.all(noisy * rc * e + nl <= rc - 1 + 1e-2)
+
+
 def test_simulate_matches_oracle(PT):
     c, prm, _n, _s = load("offedge")
     with make(PT, c, prm) as t:
