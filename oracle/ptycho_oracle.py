@@ -630,10 +630,11 @@ class PtyParams:
         return F32(self.lam * self.d / self.pixelsize / rows)
 
 
-def simulate_patterns(obj, probe, scanx, scany, exposure=1.0, fresnel=0.0):
+def simulate_patterns(obj, probe, scanx, scany, exposure=1.0, fresnel=0.0, bs=None):
     """The noise-free part of ptycho::createPattern (util/ptycho.cpp:310-359):
     I_i = |FFT(P O_window)|^2 / (rows cols), times exposure then times float(1/exposure);
-    with isFresnel (fresnel = the factor) the exit wave takes the Fresnel phase first."""
+    with isFresnel (fresnel = the factor) the exit wave takes the Fresnel phase first; with a
+    beamstop (useBS) applySupport zeroes the stopped pixels."""
     rows, cols = probe.shape
     out = []
     for px, py in zip(scanx, scany):
@@ -643,6 +644,8 @@ def simulate_patterns(obj, probe, scanx, scany, exposure=1.0, fresnel=0.0):
             esw = fresnel_phase(esw, fresnel)
         F = fft2_u(esw)
         I = ((F.real * F.real + F.imag * F.imag).astype(F32) * F32(1.0 / (rows * cols))).astype(F32)
+        if bs is not None:
+            I = np.where(bs > F32(0), F32(0), I).astype(F32)
         I = (I * F32(exposure)).astype(F32)
         I = (I * F32(1.0 / exposure)).astype(F32)
         out.append(I)

@@ -213,6 +213,15 @@ def test_simulate_ccd_record_statistics(PT):
     assert np.all(noisy * rc * e + nl <= rc - 1 + 1e-2)
 
 
+def test_simulate_with_beamstop_matches_oracle(PT):
+    c, prm, _n, _s = load("beamstop")
+    with make(PT, c, prm) as t:
+        t.createPattern()
+        bs = PO.circle_mask(32, 32, 16, 16, prm.beam_stop_size, True)
+        ref = PO.simulate_patterns(c["obj0"], c["probe0"], c["scanx"], c["scany"], prm.exposure, bs=bs)
+        assert np.linalg.norm(t.patterns - ref) / np.linalg.norm(ref) < 2e-6
+
+
 def test_simulate_matches_oracle(PT):
     c, prm, _n, _s = load("offedge")
     with make(PT, c, prm) as t:
