@@ -136,8 +136,9 @@ __device__ __forceinline__ void pty_stage_rows(const PtyArgs& a, float2* o_s, fl
 }
 
 // ------------------------------------------------------- forward row pass
-template <int N>
-__global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_ROW) pty_fwd_rk(PtyArgs a) {
+// FRES: isFresnel, a separate instantiation so the plain kernels carry no phase code
+template <int N, bool FRES>
+__global__ void __launch_bounds__(Geom<N>::T, Geom<N>::MINB) pty_fwd_rk(PtyArgs a) {
   using G = Geom<N>;
   constexpr int L = G::L;
   using F0 = RFirst<N, 0>;
@@ -163,7 +164,7 @@ __global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_ROW) pty_fwd_rk(Pty
     for (int r = 0; r < F0::R; ++r) {
       const int t = l * SN + j + r * F0::NR;   // multiply(esw, probe, window): zero outside the object
       v0[b][r] = cmul(p_s[t], o_s[t]);
-      if (a.fresnel != 0.f) v0[b][r] = pty_fresnel(v0[b][r], row0 + l, j + r * F0::NR, a.rows, a.cols, a.fresnel);
+      if constexpr (FRES) v0[b][r] = pty_fresnel(v0[b][r], row0 + l, j + r * F0::NR, a.rows, a.cols, a.fresnel);
     }
   }
   float2 v[FL::B][FL::R];
@@ -253,8 +254,8 @@ __global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_COL) pty_col_rk(Pty
 }
 
 // -------------------------------------------------------- update row pass
-template <int N>
-__global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_ROW) pty_upd_rk(PtyArgs a) {
+template <int N, bool FRES>
+__global__ void __launch_bounds__(Geom<N>::T, Geom<N>::MINB) pty_upd_rk(PtyArgs a) {
   using G = Geom<N>;
   constexpr int L = G::L;
   using F0 = RFirst<N, 0>;
@@ -301,10 +302,10 @@ __global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_ROW) pty_upd_rk(Pty
       const long long pi = (long long)row * N + c;
       const float2 p = p_s[l * SN + c];
       float2 d = cmul(p, o);                     // esw = P * O_window, then esw += Fn * (-1)
-      if (a.fresnel != 0.f) d = pty_fresnel(d, row, c, a.rows, a.cols, a.fresnel);
+      if constexpr (FRES) d = pty_fresnel(d, row, c, a.rows, a.cols, a.fresnel);
       d.x -= pp.x;
       d.y -= pp.y;
-      if (a.fresnel != 0.f) d = pty_fresnel(d, row, c, a.rows, a.cols, -a.fresnel);   // removeFresnelPhase
+      if constexpr (FRES) d = pty_fresnel(d, row, c, a.rows, a.cols, -a.fresnel);   // removeFresnelPhase
       o = pty_rpie(o, p, d, pmax, kPtyAlpha, a.obj_step);
       if (a.probe_phase) {
         const float2 st = pty_rpie_step(o, d, omax, kPtyBeta);
@@ -322,9 +323,11 @@ __global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_ROW) pty_upd_rk(Pty
 template <int N>
 cudaError_t pty_prepare() {
   using G = Geom<N>;
-  cudaError_t e = cudaFuncSetAttribute(pty_fwd_rk<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, PtyRow<N>::SMEM);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(pty_upd_rk<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, PtyRow<N>::SMEM);
+  cudaError_t e = cudaSuccess;
+  const void* rows_k[] = {(const void*)pty_fwd_rk<N, false>, (const void*)pty_fwd_rk<N, true>,
+                          (const void*)pty_upd_rk<N, false>, (const void*)pty_upd_rk<N, true>};
+  for (const void* k : rows_k)
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, PtyRow<N>::SMEM);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(pty_col_rk<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              G::SMEM_LINES + 2 * G::L * N * (int)sizeof(float));
@@ -333,12 +336,16 @@ cudaError_t pty_prepare() {
 template <int N>
 cudaError_t pty_launch_fwd(const PtyArgs& a, cudaStream_t st) {
   using G = Geom<N>;
-  return launch_pdl(pty_fwd_rk<N>, dim3((a.rows + G::L - 1) / G::L), G::T, PtyRow<N>::SMEM, st, a);
+  const dim3 grid((a.rows + G::L - 1) / G::L);
+  return a.fresnel != 0.f ? launch_pdl(pty_fwd_rk<N, true>, grid, G::T, PtyRow<N>::SMEM, st, a)
+                          : launch_pdl(pty_fwd_rk<N, false>, grid, G::T, PtyRow<N>::SMEM, st, a);
 }
 template <int N>
 cudaError_t pty_launch_upd(const PtyArgs& a, cudaStream_t st) {
   using G = Geom<N>;
-  return launch_pdl(pty_upd_rk<N>, dim3((a.rows + G::L - 1) / G::L), G::T, PtyRow<N>::SMEM, st, a);
+  const dim3 grid((a.rows + G::L - 1) / G::L);
+  return a.fresnel != 0.f ? launch_pdl(pty_upd_rk<N, true>, grid, G::T, PtyRow<N>::SMEM, st, a)
+                          : launch_pdl(pty_upd_rk<N, false>, grid, G::T, PtyRow<N>::SMEM, st, a);
 }
 template <int N>
 cudaError_t pty_launch_col(const PtyArgs& a, cudaStream_t st) {
