@@ -448,10 +448,16 @@ def run_gpu(args):
     h2d = I.nbytes + psi0.nbytes
     d2h = 2 * psi0.nbytes + I.nbytes
     pe = cdx.default_params(N, N, oversampling_spt=4.0, beta=BETA, shrink_threshold=0.1, use_graph=0, autotune=1)
+    # the job's host buffers in pinned memory (inputs and the results the call writes)
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    I_h, psi0_h = pin(I), pin(psi0)
+    outs = (torch.empty(psi0.shape, dtype=torch.complex64, pin_memory=True).numpy(),
+            torch.empty(psi0.shape, dtype=torch.complex64, pin_memory=True).numpy(),
+            torch.empty(I.shape, dtype=torch.float32, pin_memory=True).numpy())
     for k in range(4):   # the first job warms the host allocator and the page cache; median of three
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        cdx.phase_retrieve_host(pe, JOB_ALGO, I, psi0)
+        cdx.phase_retrieve_host(pe, JOB_ALGO, I_h, psi0_h, out=outs)
         dt = time.perf_counter() - t0
         if k > 0:
             e2e_vals.append(JOB_ITERS / dt)
@@ -486,7 +492,7 @@ def run_gpu(args):
                          "kernel": "one fused iteration (col_pass_rk<2048> + row_pass_rk<2048>)",
                          "t_iter_us": t_iter * 1e6},
             "e2e": {"value": e2e, "unit": "iter/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "step": "whole 2000-iteration job via cdx_phase_retrieve_host"},
+                    "step": "whole 2000-iteration job via cdx_phase_retrieve_host", "host_buffers": "pinned"},
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": launches_per_step * args.steps,

@@ -338,12 +338,19 @@ class Group:
             pass
 
 
-def phase_retrieve_host(params: Params, algorithm: str, intensity, psi0=None, seed=0):
-    """One-call host-buffer path (cdx_phase_retrieve_host): returns (rho, psi, support, stats)."""
+def phase_retrieve_host(params: Params, algorithm: str, intensity, psi0=None, seed=0, out=None):
+    """One-call host-buffer path (cdx_phase_retrieve_host): returns (rho, psi, support, stats).
+    `out` = (rho, psi, support) host arrays to fill (e.g. views of pinned memory), else new ones."""
     I = np.ascontiguousarray(intensity, np.float32)
-    rho = np.empty(I.shape, np.complex64)
-    psi = np.empty(I.shape, np.complex64)
-    spt = np.empty(I.shape, np.float32)
+    if out is not None:
+        rho, psi, spt = out
+        if rho.dtype != np.complex64 or psi.dtype != np.complex64 or spt.dtype != np.float32 or \
+                not all(a.shape == I.shape and a.flags.c_contiguous for a in out):
+            raise ValueError("out: contiguous complex64, complex64, float32 arrays of the pattern's shape")
+    else:
+        rho = np.empty(I.shape, np.complex64)
+        psi = np.empty(I.shape, np.complex64)
+        spt = np.empty(I.shape, np.float32)
     p0 = None if psi0 is None else np.ascontiguousarray(psi0, np.complex64)
     s = Stats()
     vp = lambda a: a.ctypes.data_as(ctypes.c_void_p)
