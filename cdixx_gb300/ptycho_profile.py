@@ -24,11 +24,13 @@ def main(argv=None):
     ap.add_argument("--sweeps", type=int, default=10)
     ap.add_argument("--step", type=float, default=250.0)
     ap.add_argument("--first", type=int, default=0, help="iteration index of the first sweep (400+: probe phase)")
+    ap.add_argument("--zernike-iter", type=int, default=0,
+                    help="zernikeIter (the reference's ptycho.cfg: 1200): FISTA step, probe momentum, Zernike fit")
     a = ap.parse_args(argv)
     R, RO = a.probe, a.object
     sx, sy = PT.scan_triangle(RO, RO, R, R, a.step)
     t = PT.Ptycho(R, R, RO, RO, sx, sy, lam=0.6328, d=125e3, dpupil=6.8e3, pixelsize=13.0,
-                  pupil_size=min(335.0083, R * 0.65), exposure=0.01)
+                  pupil_size=min(335.0083, R * 0.65), exposure=0.01, zernike_iter=a.zernike_iter)
     x = np.linspace(-1, 1, RO, dtype=np.float32)[:, None]
     y = np.linspace(-1, 1, RO, dtype=np.float32)[None, :]
     truth = ((0.6 + 0.4 * np.cos(9 * x) * np.sin(7 * y)) * np.exp(1.2j * np.sin(5 * x + 3 * y))).astype(np.complex64)
