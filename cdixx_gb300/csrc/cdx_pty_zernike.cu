@@ -8,8 +8,9 @@
 // the disk of radius pd/2, the radius and angle of the covered part's centroid)
 // built once per context, and the recurrence coefficients of the 441 radial
 // polynomials in constant memory; per sweep three launches:
-//   k_zk_project   four pixels per thread, per mode a warp reduction, the CTA's
-//                  four warps summed into one partial per (mode, CTA)
+//   k_zk_project   four pixels per thread, the azimuthal orders split over four CTA
+//                  rows; per mode a warp reduction, the CTA's four warps summed into
+//                  one partial per (mode, pixel block)
 //   k_zk_finish    one warp per mode sums its CTAs' partials in double, scales
 //                  by 1/(pi (pd/2)^2) and soft-thresholds
 //   k_zk_rebuild   the probe rewritten: the coefficients' sum inside the crop on
@@ -160,16 +161,19 @@ __global__ void k_zk_table(float4* __restrict__ tab, int pd) {
 // cos then sin for m > 0) for P pixels at once: the radial polynomial times the
 // pixel's weight from weight * rho^m by the three-term recurrence in n, times the
 // normalisation; f(mode, z[P]) receives the basis values.
+// Modes [mode0, mode1) are the azimuthal orders [m0, m1), whose radial steps start at j0.
 template <int P, class F>
-__device__ __forceinline__ void zk_walk(const float (&rho)[P], const float (&th)[P], const float (&wt)[P], F&& f) {
+__device__ __forceinline__ void zk_walk(const float (&rho)[P], const float (&th)[P], const float (&wt)[P], F&& f,
+                                        int m0 = 0, int m1 = kZkMaxN + 1, int mode0 = 0, int j0 = 0) {
   float rp[P], rr[P];
 #pragma unroll
   for (int p = 0; p < P; ++p) {
     rp[p] = wt[p];
     rr[p] = rho[p] * rho[p];
+    for (int m = 0; m < m0; ++m) rp[p] *= rho[p];
   }
-  int mode = 0, j = 0;
-  for (int m = 0; m <= kZkMaxN; ++m) {
+  int mode = mode0, j = j0;
+  for (int m = m0; m < m1; ++m) {
     float cm[P], sm[P], r2[P], r4[P];
 #pragma unroll
     for (int p = 0; p < P; ++p) {
@@ -198,11 +202,35 @@ __device__ __forceinline__ void zk_walk(const float (&rho)[P], const float (&th)
   }
 }
 
+// The projection's CTAs split the azimuthal orders into kZkGroups ranges of about equal mode
+// counts (blockIdx.y), so a small crop still fills the GPU.
+constexpr int kZkGroups = 4;
+__device__ __forceinline__ void zk_group_range(int g, int& m0, int& m1, int& mode0, int& mode1, int& j0) {
+  int m = 0, mode = 0, j = 0;
+  auto advance_to = [&](int target) {
+    while (m <= kZkMaxN && mode < target) {
+      const int radial = (kZkMaxN - m) / 2 + 1;
+      mode += radial * (m == 0 ? 1 : 2);
+      j += radial;
+      ++m;
+    }
+  };
+  advance_to(g * kZkModes / kZkGroups);
+  m0 = m;
+  mode0 = mode;
+  j0 = j;
+  advance_to((g + 1) * kZkModes / kZkGroups);
+  m1 = m;
+  mode1 = mode;
+}
+
 __global__ void __launch_bounds__(kZkThreads) k_zk_project(const float2* __restrict__ P, int cols, int r0, int c0,
                                                             int pd, const float4* __restrict__ tab,
                                                             float2* __restrict__ part) {
   __shared__ float2 acc[kZkWarps][kZkModes];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int m0, m1, mode0, mode1, j0;
+  zk_group_range(blockIdx.y, m0, m1, mode0, mode1, j0);
   float rho[kZkPix], th[kZkPix], wt[kZkPix];
   float2 v[kZkPix];
 #pragma unroll
@@ -231,9 +259,9 @@ __global__ void __launch_bounds__(kZkThreads) k_zk_project(const float2* __restr
       im += __shfl_xor_sync(0xffffffffu, im, o);
     }
     if (lane == 0) acc[warp][k] = make_float2(re, im);
-  });
+  }, m0, m1, mode0, j0);
   __syncthreads();
-  for (int k = threadIdx.x; k < kZkModes; k += kZkThreads) {
+  for (int k = mode0 + threadIdx.x; k < mode1; k += kZkThreads) {
     float2 s = acc[0][k];
 #pragma unroll
     for (int w = 1; w < kZkWarps; ++w) {
@@ -342,7 +370,7 @@ cudaError_t zk_fit(float2* P, int rows, int cols, int pd, const float4* tab, flo
                    cudaStream_t st) {
   const int r0 = (rows - pd) / 2, c0 = (cols - pd) / 2;
   const int nblk = zk_blocks(pd);
-  k_zk_project<<<nblk, kZkThreads, 0, st>>>(P, cols, r0, c0, pd, tab, part);
+  k_zk_project<<<dim3(nblk, kZkGroups), kZkThreads, 0, st>>>(P, cols, r0, c0, pd, tab, part);
   const float rad = (float)pd / 2;
   k_zk_finish<<<(kZkModes + 7) / 8, 256, 0, st>>>(part, nblk, 1. / (M_PI * rad * rad), coef);
   const long long n = (long long)rows * cols;
