@@ -221,16 +221,24 @@ int cdx_convert_fo(const void* in, void* out, int rows, int cols, int batch, int
  * (CDX_HIO, CDX_RAAR, CDX_ER, ...; no shrinkwrap) on one rows x cols pattern,
  * with the projection of applyModAbs: the same kernels and results as
  * cdx_set_pattern + cdx_set_initial + cdx_set_support + cdx_run("<n>*ALGO").
- * The caller passes DEVICE buffers: intensity (rows*cols floats, FFT order),
- * support (floats; inside = value > threshold), psi0 (restart iterate,
- * complex) and the outputs rho_out (object, scaled like phaseRetrieve leaves
- * it) and psi_out (final Fourier iterate).  The call allocates nothing: its
- * scratch is a static device array of CDX_NOALLOC_SCRATCH_BYTES inside this
- * library, held by every GPU that loads the library until the process exits,
- * which bounds patterns to CDX_NOALLOC_MAX_PIXELS pixels (512 x 512; larger
- * sizes return CDX_ERR_SIZE).  All calls share that array: calls that overlap
- * on the GPU race.  The first call on a device looks the array up on that
- * device; make it before any stream capture.  Work is queued on `stream`. */
+ * The caller passes DEVICE buffers, each starting on a 16-byte boundary:
+ * intensity (rows*cols floats, FFT order), support (floats; inside = value >
+ * threshold), psi0 (restart iterate, complex) and the outputs rho_out
+ * (object, scaled like phaseRetrieve leaves it) and psi_out (final Fourier
+ * iterate).  rho_out must not overlap any other buffer; psi_out must not
+ * overlap intensity, support or rho_out, and may be psi0 itself (CDX_ERR_ARG
+ * otherwise).  The call allocates nothing: its scratch is a static device
+ * array of CDX_NOALLOC_SCRATCH_BYTES inside this library, held by every GPU
+ * that loads the library until the process exits, which bounds patterns to
+ * CDX_NOALLOC_MAX_PIXELS pixels (512 x 512; larger sizes return
+ * CDX_ERR_SIZE).  All calls share that array and it keeps the last call's
+ * contents (each call clears what it uses): calls that overlap on the GPU
+ * race.  The first call on a device is its set-up: it looks the array up on
+ * that device and copies the FFT twiddle tables in with a blocking copy; make
+ * it before any stream capture.  Every later call only queues work on
+ * `stream` and returns without waiting for it.  If a kernel's bounded
+ * staging wait runs out (a guard against a hang), rho_out and psi_out are
+ * filled with NaN. */
 #define CDX_NOALLOC_MAX_PIXELS (512 * 512)
 #define CDX_NOALLOC_SCRATCH_BYTES (6u << 20)
 int cdx_iterate_noalloc(int rows, int cols, int algo, float beta, int iterations, const float* intensity,
