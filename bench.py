@@ -53,6 +53,10 @@ JOB_ALGO = f"40*({SW_EVERY}*RAAR+1*shrinkWrap)"
 JOB_ITERS = 40 * SW_EVERY
 ALG_BYTES_PER_PX_ITER = 21.0
 METRIC = "iter/s"
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one 2048^2 iteration,
+# col_pass_rk<2048> + row_pass_rk<2048>, from one ncu capture of
+# `python bench.py case pass --n 2048 --iters 3` (profiles/pass_kernels_2048.md)
+PASS_TRAFFIC_2048 = 131_400_000
 WORKLOAD = "2048x2048 complex64 phase object, 1e9 photons, RAAR beta=0.9, shrinkwrap every 50"
 
 
@@ -435,14 +439,7 @@ def run_gpu(args):
     t_iter = float(np.median(it_ms)) / 1000.0
     peak, peak_kind = peaks()
     achieved = ALG_BYTES_PER_PX_ITER * N * N / t_iter / 1e9
-    # DRAM bytes per iteration (col + row pass) from the committed ncu summary
-    traffic = None
-    tf = ROOT / "profiles" / "pass_kernels_2048.md"
-    if tf.exists():
-        for ln in tf.read_text().splitlines():
-            if ln.startswith("traffic_bytes_per_iteration:"):
-                traffic = int(ln.split(":", 1)[1])
-
+    traffic = PASS_TRAFFIC_2048
     # e2e: the whole job through the host-buffer C-ABI call
     e2e_vals = []
     h2d = I.nbytes + psi0.nbytes
@@ -507,7 +504,160 @@ def run_gpu(args):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# Small self-checking workloads for kernel captures (ncu -k / -c):
+#   python bench.py case pass --n 2048 --iters 3 [--fft-mode 1] [--batch B]
+#   python bench.py case gemm --m 16384 --n 128 --k 4096
+#   python bench.py case unet [--n 256 --batch 16 --steps 3 --umma 0]
+#   python bench.py case ptycho [--probe 512 --object 1280 --sweeps 10 --first 400 --zernike-iter 1200]
+# Each exits non-zero when its result is not finite (or, for the GEMM, not the
+# FP32 product), so a capture is only taken of a run that worked.
+
+def case_pass(a):
+    """A few fused iterations of one synthetic pattern through the C ABI, graph
+    capture off: after the set-up launches each iteration is one column pass and
+    one row pass, then the final FFT, norm and reductions of the run."""
+    from cdixx_gb300 import native as cdx
+    rng = np.random.default_rng(0)
+    I = (rng.random((a.n, a.n)) * 100).astype(np.float32)
+    psi0 = (np.sqrt(I) * np.where(rng.random((a.n, a.n)) > 0.5, -1, 1)).astype(np.complex64)
+    p = cdx.default_params(a.n, a.n, batch=a.batch, oversampling_spt=4.0, beta=0.9, use_graph=0,
+                           fft_mode=a.fft_mode)
+    with cdx.Context(p) as ctx:
+        for b in range(a.batch):
+            ctx.set_pattern(b, I)
+            ctx.set_initial(b, psi0)
+        for _ in range(a.repeat):
+            s = ctx.run(f"{a.iters}*{a.algo}")
+        rho = ctx.get_object(0)
+    ok = bool(np.isfinite(rho).all()) and np.isfinite(s["residual"])
+    print(f"n={a.n} batch={a.batch} {a.iters}*{a.algo}: {s['gpu_ms'] / a.iters * 1000:.1f} us/iter, "
+          f"launches {s['launches']}, finite={ok}")
+    return 0 if ok else 1
+
+
+def case_gemm(a):
+    """D = A B^T on the tcgen05 GEMM (cdx_gemm_bf16_tc), timed with CUDA events
+    and checked against an FP32 product."""
+    import ctypes
+    import torch
+    from cdixx_gb300 import native as cdx
+    g = torch.Generator(device="cuda").manual_seed(1)
+    A = torch.randn(a.m, a.k, device="cuda", generator=g).to(torch.bfloat16)
+    B = torch.randn(a.n, a.k, device="cuda", generator=g).to(torch.bfloat16)
+    D = torch.empty(a.m, a.n, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    args = [ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(B.data_ptr()), ctypes.c_void_p(D.data_ptr()),
+            a.m, a.n, a.k, ctypes.c_void_p(err.data_ptr()), None]
+    cdx.check(cdx.lib().cdx_gemm_bf16_tc(*args))
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(a.reps):
+        cdx.lib().cdx_gemm_bf16_tc(*args)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / a.reps
+    ref = A.float() @ B.float().T
+    rel = (torch.linalg.vector_norm(D - ref) / torch.linalg.vector_norm(ref)).item()
+    tf = 2.0 * a.m * a.n * a.k / (ms / 1000) / 1e12
+    ok = rel < 1e-5 and int(err.item()) == 0
+    print(f"gemm {a.m}x{a.n}x{a.k}: {ms * 1000:.1f} us, {tf:.1f} TFLOP/s, rel L2 {rel:.2e}, ok={ok}")
+    return 0 if ok else 1
+
+
+def case_unet(a):
+    """A few Adam steps of the warm-start network on one forward-model batch:
+    mean training-step time (forward, loss, backward, Adam) by CUDA events."""
+    import torch
+    from cdixx_gb300 import unet
+    net = unet.UNet(n=a.n, levels=a.levels, base=a.base, batch=a.batch, seed=1, umma=a.umma)
+    I, amp, ph, sup = unet.forward_model(a.n, a.batch, 7, 0, 1e6)
+    net.train_step(I, amp, ph, sup)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    losses = [net.train_step(I, amp, ph, sup) for _ in range(a.steps)]
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / a.steps
+    ok = bool(np.isfinite(losses).all())
+    print(f"n={a.n} batch={a.batch} levels={a.levels} base={a.base} umma={a.umma}: {ms:.2f} ms/step, "
+          f"loss {losses[-1]:.5f}, finite={ok}")
+    net.close()
+    return 0 if ok else 1
+
+
+def case_ptycho(a):
+    """rPIE + mPIE sweeps on the triangle scan of the reference's ptychography
+    driver (its default optics) from noise-free patterns of a smooth object;
+    fails when the object is not finite or the far-field error did not fall."""
+    from cdixx_gb300 import ptycho as PT
+    R, RO = a.probe, a.object
+    sx, sy = PT.scan_triangle(RO, RO, R, R, a.step)
+    t = PT.Ptycho(R, R, RO, RO, sx, sy, lam=0.6328, d=125e3, dpupil=6.8e3, pixelsize=13.0,
+                  pupil_size=min(335.0083, R * 0.65), exposure=0.01, zernike_iter=a.zernike_iter)
+    x = np.linspace(-1, 1, RO, dtype=np.float32)[:, None]
+    y = np.linspace(-1, 1, RO, dtype=np.float32)[None, :]
+    truth = ((0.6 + 0.4 * np.cos(9 * x) * np.sin(7 * y)) * np.exp(1.2j * np.sin(5 * x + 3 * y))).astype(np.complex64)
+    t.initObject(seed=1)
+    obj0 = t.objectWave
+    t.objectWave = truth
+    t.createPattern()
+    pats = t.patterns
+    t.objectWave = obj0
+    t.iterate(1, first_iter=a.first, seed=3)
+    t.objectWave = obj0
+    ms = t.iterate(a.sweeps, first_iter=a.first, seed=5)
+    obj = t.objectWave
+    ok = bool(np.isfinite(obj).all())
+    t.objectWave = obj
+    t.createPattern()
+    sim = t.patterns
+    err = float(np.abs(np.sqrt(np.maximum(sim, 0)) - np.sqrt(pats)).sum() / np.sqrt(pats).sum())
+    print(f"probe {R} object {RO} positions {len(sx)}: {ms / a.sweeps:.3f} ms/sweep, far-field error {err:.4f}, "
+          f"finite={ok}")
+    t.close()
+    return 0 if ok and err < 1.0 else 1
+
+
+def run_case(argv):
+    ap = argparse.ArgumentParser(prog="bench.py case")
+    sub = ap.add_subparsers(dest="case", required=True)
+    c = sub.add_parser("pass")
+    c.add_argument("--n", type=int, default=2048)
+    c.add_argument("--batch", type=int, default=1)
+    c.add_argument("--iters", type=int, default=3)
+    c.add_argument("--algo", default="RAAR")
+    c.add_argument("--fft-mode", type=int, default=0)
+    c.add_argument("--repeat", type=int, default=2)
+    c = sub.add_parser("gemm")
+    c.add_argument("--m", type=int, default=16384)
+    c.add_argument("--n", type=int, default=128)
+    c.add_argument("--k", type=int, default=4096)
+    c.add_argument("--reps", type=int, default=10)
+    c = sub.add_parser("unet")
+    c.add_argument("--n", type=int, default=256)
+    c.add_argument("--batch", type=int, default=16)
+    c.add_argument("--steps", type=int, default=3)
+    c.add_argument("--levels", type=int, default=4)
+    c.add_argument("--base", type=int, default=32)
+    c.add_argument("--umma", type=int, default=0, help="1: tcgen05 convolutions, 0: mma.sync")
+    c = sub.add_parser("ptycho")
+    c.add_argument("--probe", type=int, default=512)
+    c.add_argument("--object", type=int, default=1280)
+    c.add_argument("--sweeps", type=int, default=10)
+    c.add_argument("--step", type=float, default=250.0)
+    c.add_argument("--first", type=int, default=0, help="iteration index of the first sweep (400+: probe phase)")
+    c.add_argument("--zernike-iter", type=int, default=0,
+                   help="zernikeIter (the reference's ptycho.cfg: 1200): FISTA step, probe momentum, Zernike fit")
+    a = ap.parse_args(argv)
+    return {"pass": case_pass, "gemm": case_gemm, "unet": case_unet, "ptycho": case_ptycho}[a.case](a)
+
+
 def main():
+    if len(sys.argv) > 1 and sys.argv[1] == "case":
+        return run_case(sys.argv[2:])
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)

@@ -34,8 +34,11 @@ using namespace cdx;
 
 namespace {
 
-constexpr int kRedBlocks = 152;   // reduction CTAs per pattern (one per SM)
-constexpr int kSwBlocks = 608;    // shrinkwrap y-pass CTAs per pattern (four per SM)
+// Fixed partial counts of the reductions (one per SM and four per SM of a GB300):
+// fixed rather than queried so that the summation order, and with it every
+// reduced value, is the same on any device.
+constexpr int kRedBlocks = 152;   // reduction CTAs per pattern
+constexpr int kSwBlocks = 608;    // shrinkwrap y-pass CTAs per pattern
 
 // ---------------------------------------------------------------- twiddles
 // Per-pass twiddle table of length n (cdx_dispatch.cu), one per (device, n),

@@ -1,5 +1,6 @@
 // Length -> kernel dispatch for the row/column passes, and the twiddle tables.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 
 #include "cdx_fft.cuh"
@@ -59,6 +60,20 @@ void twiddle_table(int n, float2* out) {
           blk[(r - 1) * NS + k] = make_float2((float)std::cos(a), (float)-std::sin(a));
         }
     }
+}
+
+int sm_count() {
+  static std::atomic<int> cache[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return 1;
+  if (dev < 64) {
+    const int c = cache[dev].load(std::memory_order_relaxed);
+    if (c > 0) return c;
+  }
+  int n = 0;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) return 1;
+  if (dev < 64) cache[dev].store(n, std::memory_order_relaxed);
+  return n;
 }
 
 }  // namespace cdx

@@ -12,12 +12,15 @@
 // gives the noise-free expectation |FFT(rho)|^2 scaled to -photons.
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include <algorithm>
 #include <cmath>
 #include <string>
 
 #include "cdx.h"
 #include "cdx_host.h"
+#include "cdx_types.h"
 #include "cdx_unet.h"
 
 namespace cdx {
@@ -184,6 +187,22 @@ __global__ void k_ccd_record(float* __restrict__ I, long long n, int noise_level
 using namespace cdx;
 using namespace cdx::fm;
 
+namespace {
+
+// Scratch of cdx_forward_model (blob parameters, power sums, the complex
+// field), kept per device and grown only when a call needs more, so that a
+// training loop calling it every step allocates once.  `done` marks the end of
+// the last call's use; a call on another stream waits for it on the device.
+struct FmScratch {
+  char* p = nullptr;
+  size_t bytes = 0;
+  cudaEvent_t done = nullptr;
+};
+std::mutex g_fm_mu;
+FmScratch g_fm[64];
+
+}  // namespace
+
 extern "C" int cdx_forward_model(int n, int count, unsigned long long seed, long long first, double photons,
                                  float* intensity, float* amp_t, float* phase_t, float* support_t, void* stream) {
   if (!intensity || count < 1 || first < 0 || !(photons != 0.0) || photons != photons)
@@ -191,37 +210,48 @@ extern "C" int cdx_forward_model(int n, int count, unsigned long long seed, long
   if (!cdx_size_supported(n)) return set_error(CDX_ERR_SIZE, "unsupported pattern size");
   cudaStream_t st = (cudaStream_t)stream;
   const long long P = (long long)n * n, tot = P * count;
-  double* prm = nullptr;
-  double* sum = nullptr;
-  float2* rho = nullptr;
-  auto fail = [&](const char* what, cudaError_t e) {
-    if (prm) cudaFree(prm);
-    if (sum) cudaFree(sum);
-    if (rho) cudaFree(rho);
-    return set_error(CDX_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
-  };
-  cudaError_t e;
-  if ((e = cudaMalloc(&prm, sizeof(double) * count * kBlobs * 4)) != cudaSuccess) return fail("cudaMalloc", e);
-  if ((e = cudaMalloc(&sum, sizeof(double) * count)) != cudaSuccess) return fail("cudaMalloc", e);
-  if ((e = cudaMalloc(&rho, sizeof(float2) * tot)) != cudaSuccess) return fail("cudaMalloc", e);
-  k_blob_params<<<(count + 127) / 128, 128, 0, st>>>(n, count, seed, first, prm);
-  const int g = (int)std::min<long long>((tot + 255) / 256, 152 * 32);
-  k_blob_render<<<g, 256, 0, st>>>(n, tot, prm, rho, amp_t, phase_t, support_t);
-  if ((e = cudaGetLastError()) != cudaSuccess) return fail("render", e);
-  int rc = cdx_fft2(rho, rho, n, n, count, 0, st);
-  if (rc) {
-    cudaStreamSynchronize(st);
-    cudaFree(prm); cudaFree(sum); cudaFree(rho);
-    return rc;
+  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  const size_t o_sum = al(sizeof(double) * count * kBlobs * 4);
+  const size_t o_rho = o_sum + al(sizeof(double) * count);
+  const size_t need = o_rho + sizeof(float2) * tot;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= 64) return set_error(CDX_ERR_CUDA, "forward model: no usable device");
+  std::lock_guard<std::mutex> lk(g_fm_mu);
+  FmScratch& w = g_fm[dev];
+  if (!w.done && (e = cudaEventCreateWithFlags(&w.done, cudaEventDisableTiming)) != cudaSuccess)
+    return set_error(CDX_ERR_CUDA, std::string("forward model event: ") + cudaGetErrorString(e));
+  if (w.bytes < need) {
+    if (w.p) {
+      cudaEventSynchronize(w.done);
+      cudaFree(w.p);
+      w.p = nullptr;
+      w.bytes = 0;
+    }
+    if ((e = cudaMalloc(&w.p, need)) != cudaSuccess) {
+      w.p = nullptr;
+      return set_error(CDX_ERR_NOMEM, std::string("forward model scratch: ") + cudaGetErrorString(e));
+    }
+    w.bytes = need;
+  } else if ((e = cudaStreamWaitEvent(st, w.done, 0)) != cudaSuccess) {
+    return set_error(CDX_ERR_CUDA, std::string("forward model wait: ") + cudaGetErrorString(e));
   }
-  k_power_sum<<<count, 256, 0, st>>>(rho, P, sum);
-  k_intensity<<<g, 256, 0, st>>>(rho, sum, n, tot, photons, seed, first, intensity);
-  if ((e = cudaGetLastError()) != cudaSuccess) return fail("intensity", e);
-  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return fail("sync", e);
-  cudaFree(prm);
-  cudaFree(sum);
-  cudaFree(rho);
-  return CDX_OK;
+  double* prm = (double*)w.p;
+  double* sum = (double*)(w.p + o_sum);
+  float2* rho = (float2*)(w.p + o_rho);
+  k_blob_params<<<(count + 127) / 128, 128, 0, st>>>(n, count, seed, first, prm);
+  const int g = (int)std::min<long long>((tot + 255) / 256, sm_count() * 32);
+  k_blob_render<<<g, 256, 0, st>>>(n, tot, prm, rho, amp_t, phase_t, support_t);
+  if ((e = cudaGetLastError()) != cudaSuccess) return set_error(CDX_ERR_CUDA, std::string("render: ") + cudaGetErrorString(e));
+  int rc = cdx_fft2(rho, rho, n, n, count, 0, st);
+  if (rc == CDX_OK) {
+    k_power_sum<<<count, 256, 0, st>>>(rho, P, sum);
+    k_intensity<<<g, 256, 0, st>>>(rho, sum, n, tot, photons, seed, first, intensity);
+    if ((e = cudaGetLastError()) != cudaSuccess)
+      rc = set_error(CDX_ERR_CUDA, std::string("intensity: ") + cudaGetErrorString(e));
+  }
+  cudaEventRecord(w.done, st);
+  return rc;
 }
 
 extern "C" int cdx_ccd_noise(float* pattern, long long count, float noise_level, float exposure, int rcolor,
@@ -229,7 +259,7 @@ extern "C" int cdx_ccd_noise(float* pattern, long long count, float noise_level,
   if (!pattern || count < 0 || !(noise_level >= 0.f) || !(exposure > 0.f) || rcolor <= 0)
     return set_error(CDX_ERR_ARG, "bad CCD-noise argument");
   if (count == 0) return CDX_OK;
-  const int g = (int)std::min<long long>((count + 255) / 256, 152 * 32);
+  const int g = (int)std::min<long long>((count + 255) / 256, sm_count() * 32);
   k_ccd_noise<<<g, 256, 0, (cudaStream_t)stream>>>(pattern, count, (double)noise_level, 1.f / exposure, (float)rcolor,
                                                     seed);
   const cudaError_t e = cudaGetLastError();
@@ -262,7 +292,7 @@ extern "C" float cdx_fresnel_factor(double lambda, double distance, double pixel
 extern "C" int cdx_fresnel_phase(void* field, int rows, int cols, int batch, float factor, void* stream) {
   if (!field || rows < 1 || cols < 1 || batch < 1) return set_error(CDX_ERR_ARG, "bad Fresnel-phase argument");
   const long long n = (long long)rows * cols * batch;
-  const int g = (int)std::min<long long>((n + 255) / 256, 152 * 32);
+  const int g = (int)std::min<long long>((n + 255) / 256, sm_count() * 32);
   k_fresnel_phase<<<g, 256, 0, (cudaStream_t)stream>>>((float2*)field, rows, cols, n, factor);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return set_error(CDX_ERR_CUDA, std::string("Fresnel phase: ") + cudaGetErrorString(e));
@@ -274,7 +304,7 @@ extern "C" int cdx_ccd_record(float* pattern, long long count, int noise_level, 
   if (!pattern || count < 0 || noise_level < 0 || !(exposure > 0.f) || rcolor <= 0)
     return set_error(CDX_ERR_ARG, "bad CCD-record argument");
   if (count == 0) return CDX_OK;
-  const int g = (int)std::min<long long>((count + 255) / 256, 152 * 32);
+  const int g = (int)std::min<long long>((count + 255) / 256, sm_count() * 32);
   k_ccd_record<<<g, 256, 0, (cudaStream_t)stream>>>(pattern, count, noise_level, exposure, rcolor, post, seed);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return set_error(CDX_ERR_CUDA, std::string("ccd record: ") + cudaGetErrorString(e));

@@ -7,7 +7,8 @@
 
 namespace cdx {
 
-static inline unsigned grid1d(long long n, int t, int cap = 152 * 16) {
+static inline unsigned grid1d(long long n, int t, int cap = 0) {
+  if (cap <= 0) cap = sm_count() * 16;
   long long b = (n + t - 1) / t;
   return (unsigned)(b < 1 ? 1 : (b > cap ? cap : b));
 }

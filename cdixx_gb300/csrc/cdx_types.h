@@ -108,5 +108,7 @@ int row_cb_default(int n, int tile_log2);   // butterfly chunk bits the row pass
 int row_cb_max(int n);                      // largest valid chunk bits of length n
 // host: fill the per-pass twiddle table of length n (double precision, rounded once)
 void twiddle_table(int n, float2* out);
+// host: multiprocessors of the current device (queried once per device)
+int sm_count();
 
 }  // namespace cdx

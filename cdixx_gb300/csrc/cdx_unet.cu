@@ -19,6 +19,7 @@
 
 #include "cdx.h"
 #include "cdx_host.h"
+#include "cdx_types.h"
 #include "cdx_unet.h"
 #include "cdx_unet_gemm.cuh"
 
@@ -455,7 +456,8 @@ __global__ void k_warm_psi(const float2* __restrict__ F, const float* __restrict
 // --------------------------------------------------------------------- host
 inline int grid_for(long long total, int threads = kThreads) {
   long long b = (total + threads - 1) / threads;
-  return (int)(b < 1 ? 1 : (b > 152 * 16 ? 152 * 16 : b));
+  const long long cap = sm_count() * 16LL;
+  return (int)(b < 1 ? 1 : (b > cap ? cap : b));
 }
 
 enum { L_CONV = 0, L_CONVT = 1, L_HEAD = 2 };
@@ -698,7 +700,7 @@ int launch_wgrad(Net* u, GemmArgs a, const Layer& l) {
   const long long M = (long long)s.N * s.Ho * s.Wo;
   const int K = s.KH * s.KW * s.Cin;
   const int tx = (K + 63) / 64, ty = (s.Cout + 63) / 64;
-  long long splits = (152LL * 4 + tx * ty - 1) / (tx * ty);
+  long long splits = (sm_count() * 4LL + tx * ty - 1) / (tx * ty);
   splits = std::max(1LL, std::min(splits, std::min(64LL, (M + 255) / 256)));
   long long mps = (M + splits - 1) / splits;
   mps = (mps + 31) / 32 * 32;
@@ -716,7 +718,7 @@ int launch_wgrad(Net* u, GemmArgs a, const Layer& l) {
 
 int gn_split(const Net* u, int HW, int count) {
   const int ng = count * u->cfg.groups;
-  int sp = (152 * 4 + ng - 1) / ng;
+  int sp = (sm_count() * 4 + ng - 1) / ng;
   sp = std::max(1, std::min(sp, std::min(64, HW / 64 > 0 ? HW / 64 : 1)));
   return sp;
 }
@@ -764,7 +766,7 @@ int backward(Net* u, const float* amp_t, const float* ph_t, const float* sup_t, 
   const Layer& head = u->L.back();
   const int P = c.n * c.n;
   for (auto& l : u->L) U_CK(cudaMemsetAsync(l.dact, 0, sizeof(float) * (size_t)count * l.out_h * l.out_h * l.cout_p, u->st));
-  const int lsp = std::max(1, std::min(64, (152 * 4 + count - 1) / count));
+  const int lsp = std::max(1, std::min(64, (sm_count() * 4 + count - 1) / count));
   k_loss_partial<<<dim3(count, lsp), kThreads, 0, u->st>>>(head.pre, amp_t, ph_t, sup_t, c.n, lsp, c.support_weight,
                                                             u->lpart);
   k_loss_select<<<1, 32, 0, u->st>>>(u->lpart, count, lsp, P, u->twin, u->loss);
