@@ -4,8 +4,10 @@ Builds the reference's hot-path sources (src/gpu/cdi.cu, cudaConfig.cu,
 cub_wrap.cu, src/post_gpu/cdi.cc, readConfig.cc, memManager.cc) as host code
 with oracle/build_ref.sh, runs CDI::phaseRetrieve from a restart iterate on
 seeded synthetic 64x64 patterns, and stores inputs and outputs in
-tests/golden/reference_cases.npz.  Needs the reference checkout (default
-/root/reference) and g++; run it in the container that has them:
+tests/golden/reference_cases.npz; a smaller set at 256x256 (the plain CDI
+configuration's size: 8 blobs in a 64-px disk, 1e6 photons, oversampling 4)
+goes to tests/golden/reference_cases_256.npz.  Needs the reference checkout
+(default /root/reference) and g++; run it in the container that has them:
 
     python tests/golden/make_golden.py [/path/to/reference]
 
@@ -27,7 +29,13 @@ from cdixx_gb300 import synth  # noqa: E402
 from oracle import cdi_oracle as O  # noqa: E402
 
 OUT = Path(__file__).resolve().parent / "reference_cases.npz"
+OUT256 = Path(__file__).resolve().parent / "reference_cases_256.npz"
 N = 64
+# 256x256: one HIO step from the reference's own state after k-1 steps for these k
+# (stored inputs Psi_{k-1} and outputs rho_k only for them, to keep the file small),
+# one HIO step + shrinkwrap from its state after 9 steps, and a shrinkwrap trajectory
+STEPS_256 = (1, 5, 10)
+SW_TRAJ_256 = "2*(10*HIO+1*shrinkWrap)+4*ER"
 
 # (name, algorithm, oversampling_spt, shrinkThreshold, exposure, simCCDbit, noiseLevel)
 CASES = [(f"hio_{k}", f"{k}*HIO", 2.0, 0.1, 1.0, 0, 0) for k in range(1, 11)] + [
@@ -133,7 +141,55 @@ def main(ref=None):
             prev = data[f"hio_{k}/psi"]
     np.savez_compressed(OUT, **data)
     print(f"wrote {OUT} ({OUT.stat().st_size} bytes, {len(CASES)} cases)")
+    main256(exe)
+
+
+def main256(exe):
+    """The 256x256 set: oversampling 4 (rect rows/cols 95..160), shrinkThreshold 0.1,
+    beta_HIO 1 (the reference's fixed value)."""
+    n = 256
+    obj, sup, I = synth.config0_case(seed=5, n=n, photons=1e6)
+    psi0 = synth.random_phase_start(I, 5)
+    data = {"intensity": I, "psi0": psi0}
+
+    def run(td, psi_in, alg):
+        O.write_bin(td / "pattern.bin", np.fft.fftshift(I))
+        O.write_bin(td / "restart.bin", np.asarray(psi_in, np.complex64))
+        subprocess.run([str(exe), "pattern.bin", "restart.bin", alg, "4.0", "0.1", "1.0", "0", "0", "out"], cwd=td,
+                       check=True, capture_output=True)
+        sc = dict(line.split() for line in open(td / "out_scalars.txt"))
+        return (O.read_bin(td / "out_rho.bin"), O.read_bin(td / "out_psi.bin"),
+                O.read_bin(td / "out_support.bin") if "shrinkWrap" in alg else None,
+                np.array([float(sc["threshold"]), float(sc["residual"])]))
+
+    with tempfile.TemporaryDirectory() as td:
+        td = Path(td)
+        prev = psi0
+        for k in range(1, max(STEPS_256) + 1):
+            rho, psi, _, _ = run(td, prev, "1*HIO")
+            if k in STEPS_256:
+                data[f"step_{k}/psi_in"] = np.asarray(prev, np.complex64)
+                data[f"step_{k}/rho"] = rho
+            if k == 9:
+                rho_s, _, spt_s, sc_s = run(td, psi, "1*HIO+1*shrinkWrap")
+                data["sw_step/psi_in"] = psi
+                data["sw_step/rho"] = rho_s
+                data["sw_step/support"] = spt_s
+                data["sw_step/scalars"] = sc_s
+            prev = psi
+        rho, psi, spt, sc = run(td, psi0, SW_TRAJ_256)
+        data["sw_traj/algorithm"] = np.array(SW_TRAJ_256)
+        data["sw_traj/rho"] = rho
+        data["sw_traj/support_mask"] = np.packbits(spt > sc[0])
+        data["sw_traj/scalars"] = sc
+    np.savez_compressed(OUT256, **data)
+    print(f"wrote {OUT256} ({OUT256.stat().st_size} bytes)")
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else None)
+    if len(sys.argv) > 1 and sys.argv[1] == "--256":
+        ref = sys.argv[2] if len(sys.argv) > 2 else os.environ.get("CDX_REFERENCE", "/root/reference")
+        subprocess.run([str(ROOT / "oracle" / "build_ref.sh"), ref], check=True)
+        main256(ROOT / "oracle" / "_ref" / "ref_harness")
+    else:
+        main(sys.argv[1] if len(sys.argv) > 1 else None)
