@@ -694,6 +694,7 @@ int fill_stats(cdx_ctx* c, int idx, cdx_stats* s) {
   s->flags = h.flags;
   s->launches = c->last_launches;
   s->converged_iter = h.conv_iter;
+  s->rfactor_min = h.rmin;
   float ms = 0.f;
   if (cudaEventElapsedTime(&ms, c->ev0, c->ev1) == cudaSuccess) s->gpu_ms = ms;
   else cudaGetLastError();
@@ -985,6 +986,13 @@ int cdx_set_support(cdx_ctx* c, int idx, const float* support, int where) {
   if (e) return e;
   CDX_CK(support_bits(c->spt + off, c->dstate + idx, 0.f, c->mask + (long long)idx * c->rows * c->wpr, c->rows,
                       c->cols, 1, c->st));
+  CDX_CK(cudaStreamSynchronize(c->st));
+  return CDX_OK;
+}
+
+int cdx_set_stop_rfactor(cdx_ctx* c, int idx, double stop) {
+  if (!c || idx < 0 || idx >= c->batch || !(stop >= 0.0)) return set_error(CDX_ERR_ARG, "bad stop argument");
+  CDX_CK(cudaMemcpyAsync(&c->dstate[idx].stop, &stop, sizeof(double), cudaMemcpyHostToDevice, c->st));
   CDX_CK(cudaStreamSynchronize(c->st));
   return CDX_OK;
 }

@@ -383,8 +383,9 @@ __global__ void k_rdiff(const float2* __restrict__ psi, const float* __restrict_
 }
 
 // Fixed-order final sums.  what: 0 amp_sum, 1 residual, 2 rfactor (= sum / amp_sum).
-// For an in-loop R-factor (iter >= 0) a pattern with R <= stop (stop > 0) gets
-// flags bit 1 and conv_iter = iter + 1 (it still completes this iteration).
+// For an in-loop R-factor (iter >= 0) a pattern with R <= stop gets flags bit 1
+// and conv_iter = iter + 1 (it still completes this iteration); stop is the
+// pattern's own PatState::stop when set, else the run's `stop` (> 0 to act).
 __global__ void k_finalize_sum(const double* __restrict__ part, int nblk, PatState* __restrict__ stt, int what,
                                double stop, int iter) {
   const int p = blockIdx.x;
@@ -397,7 +398,9 @@ __global__ void k_finalize_sum(const double* __restrict__ part, int nblk, PatSta
   else {
     const double r = stt[p].amp_sum > 0.0 ? s / stt[p].amp_sum : 0.0;
     stt[p].rfactor = r;
-    if (iter >= 0 && stop > 0.0 && r <= stop) {
+    if (iter >= 0 && r < stt[p].rmin) stt[p].rmin = r;
+    const double sp = stt[p].stop > 0.0 ? stt[p].stop : stop;
+    if (iter >= 0 && sp > 0.0 && r <= sp) {
       stt[p].flags |= 2;
       stt[p].conv_iter = iter + 1;
     }
@@ -431,7 +434,12 @@ cudaError_t rfactor_from_partials(const double* part, int nblk, int batch, PatSt
 // Start of phaseRetrieve: avg and the flags are locals of the call (cdi.cc:315).
 __global__ void k_run_begin(PatState* stt, int batch) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p < batch) { stt[p].avg = 0.f; stt[p].flags = 0; stt[p].conv_iter = -1; }
+  if (p < batch) {
+    stt[p].avg = 0.f;
+    stt[p].flags = 0;
+    stt[p].conv_iter = -1;
+    stt[p].rmin = __longlong_as_double(0x7ff0000000000000LL);   // +inf
+  }
 }
 cudaError_t run_begin(PatState* stt, int batch, cudaStream_t st) {
   k_run_begin<<<(batch + 127) / 128, 128, 0, st>>>(stt, batch);

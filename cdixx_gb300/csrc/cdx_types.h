@@ -34,6 +34,8 @@ struct PatState {
   int flags;         // bit 0: NaN/zero max seen at a shrinkwrap; bit 1: R <= stop reached;
                      // bit 2: frozen (set by the column pass after bit 1; both passes then skip)
   int conv_iter;     // iterations run when the pattern froze (-1: never)
+  double stop;       // this pattern's stop R-factor (0: the run's stop_rfactor)
+  double rmin;       // lowest in-loop R-factor of the run (reset to +inf by run_begin)
 };
 
 // Per-pattern PRTF state (phaseRetrieve's phi0 and the phase of the current step).

@@ -47,7 +47,7 @@ class Stats(ctypes.Structure):
         ("steps", ctypes.c_int), ("iterations", ctypes.c_int), ("shrinkwraps", ctypes.c_int),
         ("residual", ctypes.c_double), ("rfactor", ctypes.c_double), ("threshold", ctypes.c_float),
         ("flags", ctypes.c_int), ("gpu_ms", ctypes.c_double), ("launches", ctypes.c_int),
-        ("converged_iter", ctypes.c_int),
+        ("converged_iter", ctypes.c_int), ("rfactor_min", ctypes.c_double),
     ]
 
     def as_dict(self):
@@ -70,6 +70,7 @@ _SIGS = {
     "cdx_set_initial": [_P, _I, _P, _I],
     "cdx_random_start": [_P, ctypes.c_ulonglong],
     "cdx_set_support": [_P, _I, _P, _I],
+    "cdx_set_stop_rfactor": [_P, _I, ctypes.c_double],
     "cdx_run": [_P, ctypes.c_char_p, ctypes.POINTER(Stats)],
     "cdx_run_async": [_P, ctypes.c_char_p],
     "cdx_get_stats": [_P, _I, ctypes.POINTER(Stats)],
@@ -268,6 +269,9 @@ class Context:
     def set_support(self, idx, spt):
         p, w, _k = _buf(spt)
         check(lib().cdx_set_support(self._h, idx, p, w))
+
+    def set_stop_rfactor(self, idx, stop):
+        check(lib().cdx_set_stop_rfactor(self._h, idx, float(stop)))
 
     def run(self, algorithm: str) -> dict:
         s = Stats()

@@ -91,6 +91,7 @@ typedef struct cdx_stats {
   double gpu_ms;             /* device time of the run (CUDA events) */
   int launches;              /* kernels the run enqueued */
   int converged_iter;        /* iterations run before the pattern froze at stop_rfactor (-1: never) */
+  double rfactor_min;        /* lowest R-factor of the in-loop checks (rf_every); +inf without any */
 } cdx_stats;
 
 typedef struct cdx_ctx cdx_ctx;
@@ -124,6 +125,11 @@ int cdx_set_initial(cdx_ctx* ctx, int idx, const float* psi0, int where);
 int cdx_random_start(cdx_ctx* ctx, unsigned long long seed);
 /* Float support of pattern idx (inside = value > current threshold). */
 int cdx_set_support(cdx_ctx* ctx, int idx, const float* support, int where);
+/* Stop R-factor of pattern idx alone (0: the context's stop_rfactor); with
+ * rf_every > 0 the pattern freezes once its in-loop R-factor <= stop, e.g. a
+ * noise-aware stop just above that pattern's Poisson floor.  No reference
+ * counterpart (the reference has no in-loop stop). */
+int cdx_set_stop_rfactor(cdx_ctx* ctx, int idx, double stop);
 
 /* ---------------------------------------------------------------- the loop */
 /* CDI::phaseRetrieve (cdi.cc:297-449) on every pattern of the context, with
