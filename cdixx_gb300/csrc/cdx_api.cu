@@ -375,7 +375,9 @@ int enqueue_run(cdx_ctx* c, const std::vector<int>& steps, const SwPlan& sw, boo
     const bool pstep = prtf && step >= c->p.prtf_iter;
     int e = col_iter(c, from_psi, rf, pstep ? c->pr_psi : nullptr);
     if (e) return e;
-    if (rf) CDX_CK(rfactor_from_partials(c->part, c->col_blocks, c->batch, c->dstate, c->p.stop_rfactor, it, c->st));
+    if (rf)
+      CDX_CK(rfactor_from_partials(c->part, c->col_blocks, c->batch, c->dstate, c->p.stop_rfactor, it,
+                                   c->p.plateau_iters, c->p.plateau_tol, c->st));
     e = row_iter(c, a);
     if (e) return e;
     nl += rf ? 3 : 2;
@@ -721,6 +723,8 @@ int cdx_params_default(cdx_params* p) {
   p->sigma_decay = 0.99f;      // cdi.cc:339
   p->use_graph = 1;
   p->rf_every = 0;
+  p->plateau_iters = 0;
+  p->plateau_tol = 0.01f;
   p->prtf_iter = -1;
   return CDX_OK;
 }
@@ -741,6 +745,8 @@ int cdx_create(const cdx_params* p, void* stream, cdx_ctx** out) {
   if (!(p->exposure > 0)) return set_error(CDX_ERR_ARG, "exposure must be > 0");
   if (!(p->oversampling_spt > 0)) return set_error(CDX_ERR_ARG, "oversampling_spt must be > 0");
   if (p->fft_mode != CDX_FFT_FP32 && p->fft_mode != CDX_FFT_TC_BF16) return set_error(CDX_ERR_ARG, "unknown fft_mode");
+  if (p->plateau_iters < 0 || !(p->plateau_tol >= 0.f && p->plateau_tol < 1.f))
+    return set_error(CDX_ERR_ARG, "plateau_iters must be >= 0 and plateau_tol in [0, 1)");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
     cudaGetLastError();

@@ -386,8 +386,10 @@ __global__ void k_rdiff(const float2* __restrict__ psi, const float* __restrict_
 // For an in-loop R-factor (iter >= 0) a pattern with R <= stop gets flags bit 1
 // and conv_iter = iter + 1 (it still completes this iteration); stop is the
 // pattern's own PatState::stop when set, else the run's `stop` (> 0 to act).
+// With plateau > 0 a pattern whose R-factor has not fallen below (1 - tol)
+// times its last improvement for `plateau` iterations freezes the same way.
 __global__ void k_finalize_sum(const double* __restrict__ part, int nblk, PatState* __restrict__ stt, int what,
-                               double stop, int iter) {
+                               double stop, int iter, int plateau, float tol) {
   const int p = blockIdx.x;
   if (threadIdx.x != 0) return;
   if (iter >= 0 && (stt[p].flags & 6)) return;   // already converged: partials are stale
@@ -403,6 +405,14 @@ __global__ void k_finalize_sum(const double* __restrict__ part, int nblk, PatSta
     if (iter >= 0 && sp > 0.0 && r <= sp) {
       stt[p].flags |= 2;
       stt[p].conv_iter = iter + 1;
+    } else if (iter >= 0 && plateau > 0) {
+      if (r < stt[p].rbest * (1.0 - (double)tol)) {
+        stt[p].rbest = r;
+        stt[p].best_iter = iter;
+      } else if (iter - stt[p].best_iter >= plateau) {
+        stt[p].flags |= 2 | 8;
+        stt[p].conv_iter = iter + 1;
+      }
     }
   }
 }
@@ -410,24 +420,24 @@ __global__ void k_finalize_sum(const double* __restrict__ part, int nblk, PatSta
 cudaError_t pattern_amp_sum(const float* amp, long long npx, int batch, double* part, int nblk, PatState* stt,
                             cudaStream_t st) {
   k_sum_real<<<dim3(nblk, batch), 256, 0, st>>>(amp, npx, part, nblk);
-  k_finalize_sum<<<batch, 32, 0, st>>>(part, nblk, stt, 0, 0.0, -1);
+  k_finalize_sum<<<batch, 32, 0, st>>>(part, nblk, stt, 0, 0.0, -1, 0, 0.f);
   return cudaGetLastError();
 }
 cudaError_t residual(const float2* psi, const float* inten, long long npx, int batch, double* part, int nblk,
                      PatState* stt, cudaStream_t st) {
   k_residual<<<dim3(nblk, batch), 256, 0, st>>>(psi, inten, npx, part, nblk);
-  k_finalize_sum<<<batch, 32, 0, st>>>(part, nblk, stt, 1, 0.0, -1);
+  k_finalize_sum<<<batch, 32, 0, st>>>(part, nblk, stt, 1, 0.0, -1, 0, 0.f);
   return cudaGetLastError();
 }
 cudaError_t rfactor(const float2* psi, const float* inten, long long npx, int batch, double* part, int nblk,
                     PatState* stt, cudaStream_t st) {
   k_rdiff<<<dim3(nblk, batch), 256, 0, st>>>(psi, inten, npx, part, nblk);
-  k_finalize_sum<<<batch, 32, 0, st>>>(part, nblk, stt, 2, 0.0, -1);
+  k_finalize_sum<<<batch, 32, 0, st>>>(part, nblk, stt, 2, 0.0, -1, 0, 0.f);
   return cudaGetLastError();
 }
 cudaError_t rfactor_from_partials(const double* part, int nblk, int batch, PatState* stt, double stop, int iter,
-                                  cudaStream_t st) {
-  k_finalize_sum<<<batch, 32, 0, st>>>(part, nblk, stt, 2, stop, iter);
+                                  int plateau, float tol, cudaStream_t st) {
+  k_finalize_sum<<<batch, 32, 0, st>>>(part, nblk, stt, 2, stop, iter, plateau, tol);
   return cudaGetLastError();
 }
 
@@ -439,6 +449,8 @@ __global__ void k_run_begin(PatState* stt, int batch) {
     stt[p].flags = 0;
     stt[p].conv_iter = -1;
     stt[p].rmin = __longlong_as_double(0x7ff0000000000000LL);   // +inf
+    stt[p].rbest = stt[p].rmin;
+    stt[p].best_iter = 0;
   }
 }
 cudaError_t run_begin(PatState* stt, int batch, cudaStream_t st) {

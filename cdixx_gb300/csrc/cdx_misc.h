@@ -31,7 +31,7 @@ cudaError_t residual(const float2* psi, const float* inten, long long npx, int b
 cudaError_t rfactor(const float2* psi, const float* inten, long long npx, int batch, double* part, int nblk,
                     PatState* stt, cudaStream_t st);
 cudaError_t rfactor_from_partials(const double* part, int nblk, int batch, PatState* stt, double stop, int iter,
-                                  cudaStream_t st);
+                                  int plateau, float tol, cudaStream_t st);
 cudaError_t run_begin(PatState* stt, int batch, cudaStream_t st);
 cudaError_t state_init(PatState* stt, int batch, float thr, cudaStream_t st);
 cudaError_t random_start(const float* inten, const float* bs, float bs_thr, float2* psi, long long npx, int batch,

@@ -31,11 +31,14 @@ struct PatState {
   double rfactor;    // last R-factor
   double amp_sum;    // sum sqrt(I)
   double residual;   // final residual
-  int flags;         // bit 0: NaN/zero max seen at a shrinkwrap; bit 1: R <= stop reached;
-                     // bit 2: frozen (set by the column pass after bit 1; both passes then skip)
+  int flags;         // bit 0: NaN/zero max seen at a shrinkwrap; bit 1: R <= stop reached (or a
+                     // plateau); bit 2: frozen (set by the column pass after bit 1; both passes then
+                     // skip); bit 3: the plateau set bit 1
   int conv_iter;     // iterations run when the pattern froze (-1: never)
   double stop;       // this pattern's stop R-factor (0: the run's stop_rfactor)
   double rmin;       // lowest in-loop R-factor of the run (reset to +inf by run_begin)
+  double rbest;      // plateau stop: the R-factor of the last improvement by the tolerance
+  int best_iter;     // plateau stop: iteration of that improvement
 };
 
 // Per-pattern PRTF state (phaseRetrieve's phi0 and the phase of the current step).

@@ -37,3 +37,32 @@ def r_factor(psi, intensity, mask=None) -> float:
     if mask is not None:
         a, s = a[mask], s[mask]
     return float(np.sum(np.abs(a - s)) / max(np.sum(s), 1e-300))
+
+
+def _register_t(g, t):
+    import torch
+    b, n, m = g.shape
+    cc = torch.fft.ifft2(torch.fft.fft2(t) * torch.conj(torch.fft.fft2(g))).abs()
+    k = torch.argmax(cc.reshape(b, -1), dim=1)
+    kx, ky = k // m, k % m
+    ix = (torch.arange(n, device=g.device)[None, :, None] - kx[:, None, None]) % n
+    iy = (torch.arange(m, device=g.device)[None, None, :] - ky[:, None, None]) % m
+    gs = g[torch.arange(b, device=g.device)[:, None, None], ix, iy]          # np.roll(g, (kx, ky))
+    c = (torch.conj(gs) * t).sum(dim=(1, 2)) / torch.clamp((gs.abs() ** 2).sum(dim=(1, 2)), min=1e-300)
+    num = torch.linalg.vector_norm((c[:, None, None] * gs - t).reshape(b, -1), dim=1)
+    return num / torch.clamp(torch.linalg.vector_norm(t.reshape(b, -1), dim=1), min=1e-300)
+
+
+def error_vs_truth_batch(rho, truth, chunk=64):
+    """error_vs_truth of every pattern of a batch, on torch tensors [b, n, m]
+    (complex, any device; computed in complex128): returns a float64 NumPy
+    array.  Same definition as error_vs_truth, for evaluating thousands of
+    reconstructions without a host round trip per pattern."""
+    import torch
+    out = []
+    for s in range(0, rho.shape[0], chunk):
+        g = rho[s:s + chunk].to(torch.complex128)
+        t = truth[s:s + chunk].to(torch.complex128)
+        twin = torch.conj(torch.roll(torch.flip(g, dims=(1, 2)), shifts=(1, 1), dims=(1, 2)))
+        out.append(torch.minimum(_register_t(g, t), _register_t(twin, t)).cpu())
+    return torch.cat(out).numpy()

@@ -38,7 +38,7 @@ class Params(ctypes.Structure):
         ("shrink_mode", ctypes.c_int), ("sigma0", ctypes.c_float), ("sigma_min", ctypes.c_float),
         ("sigma_decay", ctypes.c_float), ("use_graph", ctypes.c_int), ("rf_every", ctypes.c_int),
         ("stop_rfactor", ctypes.c_float), ("fft_mode", ctypes.c_int), ("prtf_iter", ctypes.c_int),
-        ("autotune", ctypes.c_int),
+        ("autotune", ctypes.c_int), ("plateau_iters", ctypes.c_int), ("plateau_tol", ctypes.c_float),
     ]
 
 

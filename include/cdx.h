@@ -73,6 +73,9 @@ typedef struct cdx_params {
                                 (programmatic dependent launch on/off x row-pass butterfly chunk width) on the
                                 context's own data and keep the fastest (cached per device, size and batch for
                                 the process); 0 (default): the per-length defaults */
+  int plateau_iters;         /* with rf_every > 0: a pattern whose lowest in-loop R-factor has not fallen by
+                                a factor (1 - plateau_tol) within this many iterations freezes (0 = off) */
+  float plateau_tol;         /* relative improvement that counts for plateau_iters (default 0.01) */
 } cdx_params;
 
 /* FFT arithmetic.  CDX_FFT_TC_BF16: the radix-16 passes run as tensor-core
@@ -90,7 +93,8 @@ typedef struct cdx_stats {
   int flags;                 /* pattern 0: bit 0 = a shrinkwrap saw max ~ 0 or NaN (cdi.cc:334-337) */
   double gpu_ms;             /* device time of the run (CUDA events) */
   int launches;              /* kernels the run enqueued */
-  int converged_iter;        /* iterations run before the pattern froze at stop_rfactor (-1: never) */
+  int converged_iter;        /* iterations run before the pattern froze at stop_rfactor or on a plateau
+                                (-1: never); flags bit 3 set when the plateau froze it */
   double rfactor_min;        /* lowest R-factor of the in-loop checks (rf_every); +inf without any */
 } cdx_stats;
 

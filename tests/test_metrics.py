@@ -21,3 +21,18 @@ def test_r_factor_zero_for_exact_modulus():
     obj, _ = synth.blob_object(32, 1)
     F = np.fft.fft2(obj)
     assert metrics.r_factor(F, np.abs(F) ** 2) < 1e-12
+
+
+def test_batched_error_matches_host_error():
+    import torch
+    from cdixx_gb300 import metrics as M
+    g = np.random.default_rng(3)
+    truth = (g.random((5, 32, 48)) + 1j * g.random((5, 32, 48))) * (g.random((5, 32, 48)) > 0.6)
+    rho = np.stack([np.roll(np.conj(t[::-1, ::-1]), (3 + i, -2), axis=(0, 1)) * np.exp(0.7j) for i, t in
+                    enumerate(truth)])
+    rho[1] = truth[1] + 0.3 * g.standard_normal((32, 48))
+    rho[2] = g.standard_normal((32, 48))
+    got = M.error_vs_truth_batch(torch.from_numpy(rho), torch.from_numpy(truth), chunk=2)
+    want = np.array([M.error_vs_truth(r, t) for r, t in zip(rho, truth)])
+    assert np.allclose(got, want, rtol=1e-10, atol=1e-12)
+    assert got[0] < 1e-12
