@@ -239,23 +239,34 @@ def eval_set(n, photons, seed, first=0):
     return I, truth, floor
 
 
-def warm_starts(net, I):
+def warm_starts(net, I, truth=None):
     """Network forward + warm start in chunks of the network's batch: (Psi0,
-    support, GPU seconds by CUDA events)."""
+    support, GPU seconds by CUDA events[, median error against the truth of the
+    network's own object a e^{i atan2(s, c)} on sigmoid(logit) > 0.5])."""
     import torch
+    from cdixx_gb300 import metrics
     b, n = I.shape[0], I.shape[1]
     psi = torch.empty((b, n, n), dtype=torch.complex64, device="cuda")
     sup = torch.empty((b, n, n), dtype=torch.float32, device="cuda")
+    obj = torch.empty((b, n, n), dtype=torch.complex64, device="cuda")
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
     B = net.cfg.batch
+    outs = []
+    e0.record()
     for s in range(0, b, B):
         out = net.forward(I[s:s + B])
         p, q = net.warm_start(I[s:s + B], out, WARM_DILATE)
         psi[s:s + B], sup[s:s + B] = p, q
+        outs.append(out)
     e1.record()
     torch.cuda.synchronize()
-    return psi, sup, e0.elapsed_time(e1) / 1000.0
+    secs = e0.elapsed_time(e1) / 1000.0
+    if truth is None:
+        return psi, sup, secs
+    for k, out in enumerate(outs):
+        a, c, si, lg = out[:, 0], out[:, 1], out[:, 2], out[:, 3]
+        obj[k * B:k * B + out.shape[0]] = torch.polar(a, torch.atan2(si, c)) * (lg > 0)
+    return psi, sup, secs, float(np.median(metrics.error_vs_truth_batch(obj, truth)))
 
 
 def run_arm(sets, starts, crit, fft_mode, seed):
@@ -327,7 +338,7 @@ def warm_start_section(net):
     from cdixx_gb300 import native as cdx
     I, truth, floor = eval_set(WARM_N, [WARM_PHOTONS] * WARM_EVAL, SEED + 1)
     sets = {WARM_N: (I, truth, floor)}
-    psi, sup, net_s = warm_starts(net, I)
+    psi, sup, net_s, net_err = warm_starts(net, I, truth)
     arms = {"plain": {}, "learned": {}}
     for crit in CRITERIA:
         arms["plain"][crit] = run_arm(sets, None, crit, cdx.FFT_FP32, SEED)
@@ -336,7 +347,8 @@ def warm_start_section(net):
             "patterns": WARM_EVAL, "n": WARM_N, "photons": WARM_PHOTONS,
             "data": "held-out forward-model seeds (8 blobs in a 64-px disk), Poisson noise",
             "algorithm": EVAL_ALGO, "rf_every": RF_EVERY, "criteria": CRITERIA,
-            "median_poisson_floor": float(np.median(floor)), "arms": arms, "compare": compare(arms)}
+            "median_poisson_floor": float(np.median(floor)), "network_alone_median_error_vs_truth": net_err,
+            "arms": arms, "compare": compare(arms)}
 
 
 def combined_section(nets):
@@ -346,11 +358,11 @@ def combined_section(nets):
     from cdixx_gb300 import native as cdx
     rng = np.random.default_rng(SEED + 4)
     counts = {256: COMBINED_PATTERNS * 3 // 4, 512: COMBINED_PATTERNS // 4}
-    sets, starts = {}, {}
+    sets, starts, net_err = {}, {}, {}
     for k, n in enumerate(COMBINED_SIZES):
         photons = 10 ** rng.uniform(5, 8, counts[n])
         sets[n] = eval_set(n, photons, SEED + 40 + k)
-        starts[n] = warm_starts(nets[n], sets[n][0])
+        *starts[n], net_err[str(n)] = warm_starts(nets[n], sets[n][0], sets[n][1])
     arms = {"plain": {}, "learned_tc": {}, "learned": {}}
     for crit in CRITERIA:
         arms["plain"][crit] = run_arm(sets, None, crit, cdx.FFT_FP32, SEED)
@@ -360,7 +372,8 @@ def combined_section(nets):
     return {"metric": "patterns/s to the stop criterion (learned + TC-FFT vs plain FP32 HIO)",
             "patterns": COMBINED_PATTERNS, "sizes": {str(n): counts[n] for n in COMBINED_SIZES},
             "photons": "log-uniform 1e5..1e8", "algorithm": EVAL_ALGO, "rf_every": RF_EVERY, "criteria": CRITERIA,
-            "median_poisson_floor": float(np.median(floors)), "arms": arms,
+            "median_poisson_floor": float(np.median(floors)), "network_alone_median_error_vs_truth": net_err,
+            "arms": arms,
             "compare": compare(arms, learned="learned_tc"), "compare_fp32": compare(arms, learned="learned"),
             "launch": "one CUDA graph per run (cdx_group), one branch per size"}
 
@@ -423,6 +436,81 @@ def batched_section():
             "algorithm": BATCH_ALGO, "patterns_per_s": BATCH_PATTERNS / (ms / 1000.0),
             "pixel_iterations_per_s": px * iters / (ms / 1000.0), "gpu_ms": ms, "wall_ms_incl_graph_build": wall * 1000,
             "contexts": len(ctxs), "launch": "one CUDA graph (cdx_group) with one branch per size"}
+
+
+# ---------------------------------------------------------------------------
+# GPU comparator (bench only, not the product and not `--impl reference`): the
+# reference's iteration structure on the same GPU -- cuFFT C2C and one
+# element-wise kernel per operation (applyModAbs, IFFT, applyNorm,
+# ApplyHIOSupport, FFT; cdi.cc:349-381) from _lib/libcdx_cufft_cmp.so --
+# against the fused two-kernel HIO iteration, same pattern, same start.
+CMP_ITERS = 50
+
+
+def comparator_section():
+    import ctypes
+    import torch
+    from cdixx_gb300 import native as cdx
+    from cdixx_gb300 import synth
+    lib = ctypes.CDLL(str(ROOT / "cdixx_gb300" / "_lib" / "libcdx_cufft_cmp.so"))
+    lib.cmp_iterate.argtypes = [ctypes.c_int] * 4 + [ctypes.c_void_p] * 5 + [ctypes.c_float, ctypes.c_float,
+                                                                              ctypes.c_void_p]
+    P = lambda t: ctypes.c_void_p(t.data_ptr())
+    out = {"structure": "cuFFT C2C + applyModAbs + applyNorm + ApplyHIOSupport kernels (5 launches/iteration) vs "
+                        "col_pass_rk + row_pass_rk (2 launches/iteration)", "algorithm": "HIO beta 0.9"}
+    cases = [("2048x2048 x1", 2048, 1, lambda: make_inputs()),
+             ("256x256 x64", 256, 64, None)]
+    stream = torch.cuda.Stream()
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    for name, n, b, mk in cases:
+        if mk is not None:
+            I_np, psi_np = mk()
+            I_np, psi_np = I_np[None], psi_np[None]
+        else:
+            I_np = np.stack([synth.config0_case(seed=SEED + i, n=n, photons=1e6)[2] for i in range(b)])
+            psi_np = np.stack([synth.random_phase_start(I_np[i], SEED + i) for i in range(b)])
+        prm = cdx.default_params(n, n, batch=b, oversampling_spt=4.0, beta=0.9)
+        ctx = cdx.Context(prm, stream=stream.cuda_stream)
+        for i in range(b):
+            ctx.set_pattern(i, I_np[i])
+            ctx.set_initial(i, psi_np[i])
+        spt = torch.from_numpy(np.stack([ctx.get_support(i) for i in range(b)])).cuda()
+        I = torch.from_numpy(I_np).cuda()
+        psi = torch.from_numpy(psi_np).cuda()
+        rho = torch.fft.ifft2(psi)                    # rho0 = IFFT(Psi0)/N
+        rhop = torch.empty_like(rho)
+        torch.cuda.synchronize()
+        # agreement: 5 iterations from the same start
+        rc = lib.cmp_iterate(n, n, b, 5, P(psi), P(rho), P(rhop), P(I), P(spt), 0.5, 0.9, stream.cuda_stream)
+        if rc:
+            raise RuntimeError(f"comparator failed: {rc}")
+        ctx.run("5*HIO")
+        torch.cuda.synchronize()
+        a = rho[0].cpu().numpy() * np.float32(n)      # phaseRetrieve leaves rho scaled by sqrt(N)
+        g = ctx.get_object(0)
+        agree = float(np.linalg.norm(a - g) / np.linalg.norm(g))
+
+        def timed(fn):
+            vals = []
+            for _ in range(5):
+                with torch.cuda.stream(stream):
+                    flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                fn()
+                e1.record(stream)
+                torch.cuda.synchronize()
+                vals.append(e0.elapsed_time(e1) * 1000.0 / CMP_ITERS)
+            return float(np.median(vals))
+
+        us_cmp = timed(lambda: lib.cmp_iterate(n, n, b, CMP_ITERS, P(psi), P(rho), P(rhop), P(I), P(spt), 0.5, 0.9,
+                                               stream.cuda_stream))
+        us_fused = timed(lambda: ctx.run_async(f"{CMP_ITERS}*HIO"))
+        ctx.close()
+        out[name] = {"us_per_iteration_cufft_structure": us_cmp, "us_per_iteration_fused": us_fused,
+                     "fused_speedup": us_cmp / us_fused, "rel_l2_after_5_iterations": agree,
+                     "l2": "flushed (512 MB write) before each block of 50"}
+    return out
 
 
 # Ptychography: the reference's own configuration (html/default/ptycho.cfg optics,
@@ -605,7 +693,9 @@ def run_gpu(args):
         cpu = {"value": v, "unit": "iter/s", "cores": threads, "kind": "port",
                "sample": "2 RAAR iterations of the 2048^2 pattern, float32 oracle, "
                          f"scipy.fft with {threads} workers ({dt:.2f} s)"}
-    warm = comb = batched = pty = None
+    warm = comb = batched = pty = cmpr = None
+    if rank == 0 and not args.no_comparator:
+        cmpr = comparator_section()
     if rank == 0 and not args.no_ptycho:
         pty = ptycho_section(cpu=not args.no_cpu)
     if rank == 0 and not args.no_warm:
@@ -630,6 +720,7 @@ def run_gpu(args):
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": launches_per_step * args.steps,
+            "gpu_comparator": cmpr,
             "warm_start": warm,
             "combined": comb,
             "batched": batched,
@@ -805,6 +896,7 @@ def main():
     ap.add_argument("--no-warm", action="store_true", help="skip the learned warm-start section")
     ap.add_argument("--no-batched", action="store_true", help="skip the uneven-size batch section")
     ap.add_argument("--no-ptycho", action="store_true", help="skip the ptychography section")
+    ap.add_argument("--no-comparator", action="store_true", help="skip the cuFFT-structure comparator section")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

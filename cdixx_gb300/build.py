@@ -97,6 +97,16 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("ptycho_run link failed:\n" + r.stdout + r.stderr)
+    # bench-only comparator: the reference's iteration structure on cuFFT (never loaded by the product)
+    cmp_src = CSRC / "cufft_cmp.cu"
+    CMP = LIBDIR / "libcdx_cufft_cmp.so"
+    if not CMP.exists() or CMP.stat().st_mtime < cmp_src.stat().st_mtime:
+        cmd = [nvcc, "-std=c++17", "-O3", "-gencode", GENCODE, "-Xcompiler", "-fPIC", "-shared", str(cmp_src), "-o",
+               str(CMP) + ".tmp", "-lcufft", "-lcudart"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("comparator build failed:\n" + r.stdout + r.stderr)
+        os.replace(str(CMP) + ".tmp", CMP)
     if verbose:
         print(f"built {LIB}")
     return LIB
