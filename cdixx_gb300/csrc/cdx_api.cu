@@ -270,7 +270,7 @@ int col_iter(cdx_ctx* c, bool from_psi, bool rf, float2* psi_proj = nullptr) {
   a.bs = c->bs_t;
   a.aux_stride = c->wstride;
   a.state = c->dstate;
-  a.tc = c->p.fft_mode == CDX_FFT_TC_BF16;
+  a.tc = c->p.fft_mode;
   a.rf_partials = rf ? c->part : nullptr;
   a.tw = c->tw_r;
   a.cols = c->cols;
@@ -299,7 +299,7 @@ int row_iter(cdx_ctx* c, int algo) {
   a.mask = c->mask;
   a.mask_stride = (long long)c->rows * c->wpr;
   a.state = c->dstate;
-  a.tc = c->p.fft_mode == CDX_FFT_TC_BF16;
+  a.tc = c->p.fft_mode;
   a.tw = c->tw_c;
   a.rows = c->rows;
   a.mode = ROW_ITER;
@@ -421,7 +421,7 @@ int enqueue_run(cdx_ctx* c, const std::vector<int>& steps, const SwPlan& sw, boo
     a.cols = c->cols;
     a.mode = COL_FFT;
     a.inv = 0;
-    a.tc = c->p.fft_mode == CDX_FFT_TC_BF16;
+    a.tc = c->p.fft_mode;
     a.scale = 1.f;
     CDX_CK(col_launcher(c->rows)(a, c->batch, c->st));
     ++nl;
@@ -744,7 +744,8 @@ int cdx_create(const cdx_params* p, void* stream, cdx_ctx** out) {
   if (p->batch < 1 || p->batch > 65535) return set_error(CDX_ERR_ARG, "batch must be in [1, 65535]");
   if (!(p->exposure > 0)) return set_error(CDX_ERR_ARG, "exposure must be > 0");
   if (!(p->oversampling_spt > 0)) return set_error(CDX_ERR_ARG, "oversampling_spt must be > 0");
-  if (p->fft_mode != CDX_FFT_FP32 && p->fft_mode != CDX_FFT_TC_BF16) return set_error(CDX_ERR_ARG, "unknown fft_mode");
+  if (p->fft_mode != CDX_FFT_FP32 && p->fft_mode != CDX_FFT_TC_BF16 && p->fft_mode != CDX_FFT_TC_MMA)
+    return set_error(CDX_ERR_ARG, "unknown fft_mode");
   if (p->plateau_iters < 0 || !(p->plateau_tol >= 0.f && p->plateau_tol < 1.f))
     return set_error(CDX_ERR_ARG, "plateau_iters must be >= 0 and plateau_tol in [0, 1)");
   int ndev = 0;
@@ -948,7 +949,7 @@ static int init_rho_from_psi(cdx_ctx* c, int idx, int count) {
   const long long off = (long long)idx * c->npx;
   const float f = (float)(1.0 / std::sqrt((double)c->rows * c->cols));
   return fft2_enqueue(c->psi + off, c->rho + off, c->rows, c->cols, count, true, f, c->tw_r, c->tw_c, c->st,
-                      c->p.fft_mode == CDX_FFT_TC_BF16);
+                      c->p.fft_mode);
 }
 
 int cdx_set_initial(cdx_ctx* c, int idx, const float* psi0, int where) {
@@ -1113,7 +1114,8 @@ int cdx_fft2(const void* in, void* out, int rows, int cols, int batch, int inver
 
 int cdx_fft2_ex(const void* in, void* out, int rows, int cols, int batch, int inverse, int fft_mode, void* stream) {
   if (!in || !out || batch < 1) return set_error(CDX_ERR_ARG, "bad fft argument");
-  if (fft_mode != CDX_FFT_FP32 && fft_mode != CDX_FFT_TC_BF16) return set_error(CDX_ERR_ARG, "unknown fft_mode");
+  if (fft_mode != CDX_FFT_FP32 && fft_mode != CDX_FFT_TC_BF16 && fft_mode != CDX_FFT_TC_MMA)
+    return set_error(CDX_ERR_ARG, "unknown fft_mode");
   int e = check_len(rows);
   if (e) return e;
   if ((e = check_len(cols))) return e;
@@ -1122,7 +1124,7 @@ int cdx_fft2_ex(const void* in, void* out, int rows, int cols, int batch, int in
   float2 *tr, *tc;
   if ((e = twiddles(rows, &tr)) || (e = twiddles(cols, &tc))) return e;
   return fft2_enqueue((const float2*)in, (float2*)out, rows, cols, batch, inverse != 0, 1.f, tr, tc,
-                      (cudaStream_t)stream, fft_mode == CDX_FFT_TC_BF16);
+                      (cudaStream_t)stream, fft_mode);
 }
 
 int cdx_apply_mod_abs(void* psi, const float* inten, long long n, void* stream) {

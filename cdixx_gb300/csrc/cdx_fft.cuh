@@ -24,6 +24,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "cdx_umma.cuh"
+
 namespace cdx {
 
 #define CDX_HD __host__ __device__ __forceinline__
@@ -418,23 +420,200 @@ __device__ __forceinline__ void fft_pass_tc16(float2* buf, const float2* tw, con
   __syncthreads();
 }
 
-template <int N, int P, bool INV, bool TC>
-__device__ __forceinline__ void fft_passes(float2* buf, const float2* tw, const DftFrag& F) {
+// ------------------------------------------------- tcgen05 (UMMA) radix 16
+// The DFT-16 of every butterfly of a pass on the 5th-generation tensor cores.
+// Thread t owns butterfly t (rows of 128-butterfly tiles, NT = T/128 tiles).
+// Its 16 twiddled inputs are split into BF16 heads and tails and written as
+// one 128-byte row of the tile's A operand, K-major SWIZZLE_128B:
+//     A[t] = [Xr_hi(16) | Xi_hi(16) | Xr_lo(16) | Xi_lo(16)]        (K = 64)
+// The DFT matrix in real form G (32 outputs x 32 inputs: Yr = Fr Xr - Fi Xi,
+// Yi = Fi Xr + Fr Xi), split the same way, is the B operand twice:
+//     Bm[n] = [G_hi(n, :) | G_hi(n, :)]   (K = 64),   Bl[n] = G_lo(n, :)  (K = 32)
+// so D = A Bm^T + A[:, 0:32] Bl^T = X_hi G_hi + X_lo G_hi + X_hi G_lo, the
+// compensated product (the tail x tail term, O(2^-16), dropped) in six
+// m128n32k16 MMAs per tile, FP32 accumulation in TMEM (32 columns per tile).
+// One elected thread issues them and commits to an mbarrier; warp w then
+// reads its 32 butterflies' rows (TMEM lanes 32 (w % 4) .., columns of tile
+// w / 4) with one tcgen05.ld.32x32b.x32: each thread gets Yr[0..15], Yi[0..15]
+// of its own butterfly and stores them to the Stockham positions.
+// Every wait is bounded (umma::kSpinLimit polls); a wait that runs out sets
+// bit 0 of *err, and the kernel carries on to its end (results invalid).
+struct UmmaFft {
+  unsigned a;       // shared address of the NT A tiles (16 KB each, 1024-aligned)
+  unsigned bm, bl;  // shared addresses of Bm and Bl (4 KB each, 1024-aligned) for the current direction
+  unsigned tmem;    // TMEM base (32 columns per tile)
+  unsigned bar;     // mbarrier (one arrival per pass)
+  unsigned phase;   // parity of the next completion
+  int* err;
+};
+constexpr int kUmmaTileBytes = 128 * 128;
+constexpr int kUmmaBBytes = 32 * 128;
+
+// G_hi / G_lo rows for direction INV into Bm and Bl (SW128 K-major): entry
+// (n, k) of G is +-cos or +-sin of 2 pi q / 16, q = m r mod 16, from float
+// values of cos(pi j/8) (float rounding of the exact constants), split.
+template <bool INV, int T>
+__device__ __forceinline__ void umma_dft16_b(const UmmaFft& U, unsigned char* smem_base) {
+  const float c1 = 0.923879532511286756f, s1 = 0.382683432365089772f, h = 0.707106781186547524f;
+  const float c16[16] = {1.f, c1, h, s1, 0.f, -s1, -h, -c1, -1.f, -c1, -h, -s1, 0.f, s1, h, c1};
+  const float sg = INV ? 1.f : -1.f;
+  unsigned char* bm = smem_base + (U.bm - (unsigned)__cvta_generic_to_shared(smem_base));
+  unsigned char* bl = smem_base + (U.bl - (unsigned)__cvta_generic_to_shared(smem_base));
+  // 32 rows x 8 chunks of 8 BF16: thread t fills (row, chunk) pairs t, t + T, ...
+  for (int q = threadIdx.x; q < 32 * 8; q += T) {
+    const int n = q >> 3, ch = q & 7;
+    const int m = n & 15;
+    __align__(16) __nv_bfloat16 hv[8], lv[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int k = ((ch & 3) << 3) + e;   // input index 0..31 (k < 16: Xr[k], else Xi[k - 16])
+      const int r = k & 15, qq = (m * r) & 15;
+      const float cs = c16[qq], sn = sg * c16[(qq + 12) & 15];   // Fr, Fi
+      float g;
+      if (n < 16) g = k < 16 ? cs : -sn;   // Yr row
+      else g = k < 16 ? sn : cs;           // Yi row
+      const __nv_bfloat16 hi = __float2bfloat16_rn(g);
+      hv[e] = hi;
+      lv[e] = __float2bfloat16_rn(g - __bfloat162float(hi));
+    }
+    // Bm: chunks 0-3 and 4-7 both hold G_hi; Bl: chunks 0-3 hold G_lo (4-7 unused)
+    *reinterpret_cast<uint4*>(bm + umma::sw128(n, ch)) = *reinterpret_cast<const uint4*>(hv);
+    if (ch < 4) *reinterpret_cast<uint4*>(bl + umma::sw128(n, ch)) = *reinterpret_cast<const uint4*>(lv);
+  }
+}
+
+template <int N, int P, bool INV>
+__device__ __forceinline__ void fft_pass_umma16(float2* buf, const float2* tw, UmmaFft& U, unsigned char* smem_base) {
+  using G = Geom<N>;
+  constexpr int L = G::L, T = G::T;
+  constexpr int R = 16;
+  static_assert(plan_radix(N, P) == 16, "tensor-core pass is radix 16");
+  constexpr int NS = plan_ns(N, P);
+  constexpr int NR = N / R;
+  constexpr int NB = L * NR;
+  static_assert(NB <= T && T % 128 == 0, "one butterfly per thread, whole 128-row tiles");
+  constexpr int NT = T / 128;
+  const int t = threadIdx.x, warp = t >> 5;
+  const bool mine = NB == T || t < NB;
+  int l = 0, j = 0, k = 0;
+  float2 x[16];
+  if (mine) {
+    l = t / NR;
+    j = t - l * NR;
+    k = j % NS;
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+      float2 v = buf[G::idx(l, j + r * NR)];
+      if constexpr (NS > 1) {
+        if (r > 0) {
+          float2 w = __ldg(tw + tw_offset(N, P) + (r - 1) * NS + k);
+          if (INV) w.y = -w.y;
+          v = cmul(v, w);
+        }
+      }
+      x[r] = v;
+    }
+  } else {
+#pragma unroll
+    for (int r = 0; r < 16; ++r) x[r] = make_float2(0.f, 0.f);
+  }
+  // A row: chunks 0-1 Xr_hi, 2-3 Xi_hi, 4-5 Xr_lo, 6-7 Xi_lo (8 BF16 each)
+  {
+    unsigned char* arow = smem_base + (U.a - (unsigned)__cvta_generic_to_shared(smem_base)) + (t >> 7) * kUmmaTileBytes;
+    const int row = t & 127;
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      __align__(16) __nv_bfloat16 rh[8], ih[8], rl[8], il[8];
+#pragma unroll
+      for (int e = 0; e < 8; ++e) {
+        const float2 v = x[half * 8 + e];
+        const __nv_bfloat16 a = __float2bfloat16_rn(v.x), b = __float2bfloat16_rn(v.y);
+        rh[e] = a;
+        ih[e] = b;
+        rl[e] = __float2bfloat16_rn(v.x - __bfloat162float(a));
+        il[e] = __float2bfloat16_rn(v.y - __bfloat162float(b));
+      }
+      *reinterpret_cast<uint4*>(arow + umma::sw128(row, 0 + half)) = *reinterpret_cast<const uint4*>(rh);
+      *reinterpret_cast<uint4*>(arow + umma::sw128(row, 2 + half)) = *reinterpret_cast<const uint4*>(ih);
+      *reinterpret_cast<uint4*>(arow + umma::sw128(row, 4 + half)) = *reinterpret_cast<const uint4*>(rl);
+      *reinterpret_cast<uint4*>(arow + umma::sw128(row, 6 + half)) = *reinterpret_cast<const uint4*>(il);
+    }
+  }
+  // the tensor core (async proxy) reads what the threads wrote; every thread
+  // has also finished reading buf, which the outputs overwrite below
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+  __syncthreads();
+  if (t == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    constexpr uint32_t IDESC = umma::idesc_bf16(128, 32);
+#pragma unroll
+    for (int tile = 0; tile < NT; ++tile) {
+      if (tile * 128 < NB) {
+        const unsigned d = U.tmem + (unsigned)(tile * 32);
+        const unsigned a0 = U.a + tile * kUmmaTileBytes;
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) umma::mma_f16(d, umma::sdesc(a0 + kk * 32), umma::sdesc(U.bm + kk * 32), IDESC, kk);
+#pragma unroll
+        for (int kk = 0; kk < 2; ++kk) umma::mma_f16(d, umma::sdesc(a0 + kk * 32), umma::sdesc(U.bl + kk * 32), IDESC, 1);
+      }
+    }
+    umma::mma_commit(U.bar);
+  }
+  if (!umma::mbar_wait(U.bar, U.phase) && (t & 31) == 0 && U.err) atomicOr(U.err, 1);
+  U.phase ^= 1u;
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  uint32_t v[32];
+  {
+    const unsigned ta = U.tmem + ((unsigned)((warp & 3) * 32) << 16) + (unsigned)((warp >> 2) * 32);
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+          "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+          "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+        : "r"(ta)
+        : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+  }
+  if (mine) {
+    const int base = (j - k) * R + k;
+#pragma unroll
+    for (int m = 0; m < 16; ++m)
+      buf[G::idx(l, base + m * NS)] = make_float2(__uint_as_float(v[m]), __uint_as_float(v[16 + m]));
+  }
+  // the next pass's MMAs overwrite TMEM and A: every warp's loads are done
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+}
+
+// TCM: 0 SIMT butterflies, 1 radix-16 passes on mma.sync, 2 radix-16 passes on tcgen05
+template <int N, int P, bool INV, int TCM>
+__device__ __forceinline__ void fft_passes(float2* buf, const float2* tw, const DftFrag& F, UmmaFft* U,
+                                           unsigned char* smem_base) {
   if constexpr (plan_radix(N, P) != 0) {
-    if constexpr (TC && plan_radix(N, P) == 16 && (Geom<N>::L * (N / 16)) % 8 == 0) fft_pass_tc16<N, P, INV>(buf, tw, F);
+    if constexpr (TCM == 1 && plan_radix(N, P) == 16 && (Geom<N>::L * (N / 16)) % 8 == 0)
+      fft_pass_tc16<N, P, INV>(buf, tw, F);
+    else if constexpr (TCM == 2 && plan_radix(N, P) == 16) fft_pass_umma16<N, P, INV>(buf, tw, *U, smem_base);
     else fft_pass<N, P, INV>(buf, tw);
-    fft_passes<N, P + 1, INV, TC>(buf, tw, F);
+    fft_passes<N, P + 1, INV, TCM>(buf, tw, F, U, smem_base);
   }
 }
 
 // Transform all L lines in place.  Callers synchronise before the call (the
-// lines must be fully written); the call ends with a barrier.  TC selects the
-// tensor-core radix-16 passes.
-template <int N, bool INV, bool TC = false>
-__device__ __forceinline__ void fft_lines(float2* buf, const float2* tw) {
+// lines must be fully written); the call ends with a barrier.  TCM selects the
+// tensor-core radix-16 passes (1: mma.sync, 2: tcgen05 with the resources of *U).
+template <int N, bool INV, int TCM = 0>
+__device__ __forceinline__ void fft_lines(float2* buf, const float2* tw, UmmaFft* U = nullptr,
+                                          unsigned char* smem_base = nullptr) {
   DftFrag F;
-  if constexpr (TC) dft16_fragments<INV>(F);
-  fft_passes<N, 0, INV, TC>(buf, tw, F);
+  if constexpr (TCM == 1) dft16_fragments<INV>(F);
+  if constexpr (TCM == 2) {
+    umma_dft16_b<INV, Geom<N>::T>(*U, smem_base);
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    __syncthreads();
+  }
+  fft_passes<N, 0, INV, TCM>(buf, tw, F, U, smem_base);
 }
 
 }  // namespace cdx

@@ -238,9 +238,58 @@ __device__ __forceinline__ void row_elem(int e, int tiled, int tl, int& l, int& 
   }
 }
 
+// ------------------------------------------------------------ tcgen05 set-up
+// Extra dynamic shared memory of the tcgen05 radix-16 passes: the A tiles
+// (T/128 x 16 KB), Bm and Bl (4 KB each), 1 KB for the 1024-byte alignment.
+template <int N>
+constexpr int umma_smem_extra() { return (Geom<N>::T / 128) * kUmmaTileBytes + 2 * kUmmaBBytes + 1024; }
+
+// Allocates the kernel's TMEM (32 columns per 128-butterfly tile), initialises
+// the mbarrier and places the operand tiles after `base_bytes` of dynamic
+// shared memory.  Every thread of the CTA calls it; it ends with a barrier.
+template <int N>
+__device__ __forceinline__ void umma_fft_begin(UmmaFft& U, unsigned char* smem_base, int base_bytes, uint64_t* bar,
+                                               unsigned* tmem_slot, int* err) {
+  constexpr int NT = Geom<N>::T / 128;
+  constexpr unsigned COLS = NT * 32 < 32 ? 32 : NT * 32;
+  const unsigned s0 = (unsigned)__cvta_generic_to_shared(smem_base);
+  const unsigned a = (s0 + (unsigned)base_bytes + 1023u) & ~1023u;
+  U.a = a;
+  U.bm = a + NT * kUmmaTileBytes;
+  U.bl = U.bm + kUmmaBBytes;
+  U.bar = (unsigned)__cvta_generic_to_shared(bar);
+  U.phase = 0;
+  U.err = err;
+  if ((threadIdx.x >> 5) == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                     (unsigned)__cvta_generic_to_shared(tmem_slot)),
+                 "r"(COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  if (threadIdx.x == 0) {
+    umma::mbar_init(U.bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  U.tmem = *tmem_slot;
+}
+
+template <int N>
+__device__ __forceinline__ void umma_fft_end(const UmmaFft& U) {
+  constexpr int NT = Geom<N>::T / 128;
+  constexpr unsigned COLS = NT * 32 < 32 ? 32 : NT * 32;
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if ((threadIdx.x >> 5) == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(U.tmem), "r"(COLS) : "memory");
+}
+
 // ------------------------------------------------------------------ row pass
 // Lines are rows of length N (= number of columns).  Grid: (ceil(rows/L), batch).
-template <int N, int MODE, bool TC>
+template <int N, int MODE, int TC>
 __global__ void __launch_bounds__(Geom<N>::T, (TC && Geom<N>::MINB > 2) ? 2 : Geom<N>::MINB) row_pass_kernel(RowArgs a) {
   using G = Geom<N>;
   constexpr int L = G::L, T = G::T;
@@ -287,12 +336,18 @@ __global__ void __launch_bounds__(Geom<N>::T, (TC && Geom<N>::MINB > 2) ? 2 : Ge
   cp_commit();
   cp_wait<1>();
   __syncthreads();
+  // tcgen05 passes: TMEM, mbarrier and operand tiles after this mode's buffers
+  __shared__ __align__(8) uint64_t um_bar;
+  __shared__ unsigned um_tmem;
+  UmmaFft U{};
+  unsigned char* ub = reinterpret_cast<unsigned char*>(smem);
+  if constexpr (TC == 2) umma_fft_begin<N>(U, ub, iter ? G::SMEM_ROW_ITER : G::SMEM_LINES, &um_bar, &um_tmem, a.err);
 
   if constexpr (!iter) {
-    if (a.inv) fft_lines<N, true, TC>(buf, tw);
-    else fft_lines<N, false, TC>(buf, tw);
+    if (a.inv) fft_lines<N, true, TC>(buf, tw, &U, ub);
+    else fft_lines<N, false, TC>(buf, tw, &U, ub);
   } else {
-    fft_lines<N, true, TC>(buf, tw);
+    fft_lines<N, true, TC>(buf, tw, &U, ub);
     cp_wait<0>();
     __syncthreads();
     // rho' = IFFT/N, update against rho and the support bits
@@ -311,8 +366,9 @@ __global__ void __launch_bounds__(Geom<N>::T, (TC && Geom<N>::MINB > 2) ? 2 : Ge
       buf[G::idx(l, c)] = r;
     }
     __syncthreads();
-    fft_lines<N, false, TC>(buf, tw);
+    fft_lines<N, false, TC>(buf, tw, &U, ub);
   }
+  if constexpr (TC == 2) umma_fft_end<N>(U);
   // store rows
   const float s = a.scale;
   for (int e = threadIdx.x; e < L * N / 2; e += T) {
@@ -332,7 +388,7 @@ __global__ void __launch_bounds__(Geom<N>::T, (TC && Geom<N>::MINB > 2) ? 2 : Ge
 // Lines are columns of length N (= number of rows).  Grid: (ceil(cols/L), batch).
 // Column-tiled arrays here have tile width L, so the CTA's tile is the
 // contiguous block [blockIdx.x * N * L, +N*L) with element t = r*L + l.
-template <int N, int MODE, bool TC>
+template <int N, int MODE, int TC>
 __global__ void __launch_bounds__(Geom<N>::T, (TC && Geom<N>::MINB > 2) ? 2 : Geom<N>::MINB) col_pass_kernel(ColArgs a) {
   using G = Geom<N>;
   constexpr int L = G::L, T = G::T, LL = G::LOG2L;
@@ -396,12 +452,19 @@ __global__ void __launch_bounds__(Geom<N>::T, (TC && Geom<N>::MINB > 2) ? 2 : Ge
   cp_commit();
   cp_wait<1>();
   __syncthreads();
+  __shared__ __align__(8) uint64_t um_bar;
+  __shared__ unsigned um_tmem;
+  UmmaFft U{};
+  unsigned char* ub = reinterpret_cast<unsigned char*>(smem);
+  if constexpr (TC == 2)
+    umma_fft_begin<N>(U, ub, iter ? (ccd ? G::SMEM_COL_CCD : G::SMEM_COL_ITER) : G::SMEM_LINES, &um_bar, &um_tmem,
+                      a.err);
 
   if constexpr (!iter) {
-    if (a.inv) fft_lines<N, true, TC>(buf, tw);
-    else fft_lines<N, false, TC>(buf, tw);
+    if (a.inv) fft_lines<N, true, TC>(buf, tw, &U, ub);
+    else fft_lines<N, false, TC>(buf, tw, &U, ub);
   } else {
-    if (!a.from_psi) fft_lines<N, false, TC>(buf, tw);
+    if (!a.from_psi) fft_lines<N, false, TC>(buf, tw, &U, ub);
     cp_wait<0>();
     __syncthreads();
     // Psi is complete here: optional copy-out, R-factor partial, projection
@@ -424,8 +487,9 @@ __global__ void __launch_bounds__(Geom<N>::T, (TC && Geom<N>::MINB > 2) ? 2 : Ge
       if (threadIdx.x == 0) a.rf_partials[(long long)blockIdx.y * gridDim.x + blockIdx.x] = tsum;
     }
     __syncthreads();
-    fft_lines<N, true, TC>(buf, tw);
+    fft_lines<N, true, TC>(buf, tw, &U, ub);
   }
+  if constexpr (TC == 2) umma_fft_end<N>(U);
   const float s = a.scale;
   float2* out = a.out + (long long)blockIdx.y * a.out_stride;
   if (a.out_tiled) {

@@ -1,26 +1,36 @@
 // Per-length instantiation of the row/column pass kernels and their launchers.
 // FP32 (tc == 0): the register-handoff kernels of cdx_rfft.cuh.  Tensor-core
-// radix-16 passes (tc == 1): the staged kernels of cdx_kernels.cuh.
+// radix-16 passes: the staged kernels of cdx_kernels.cuh, on tcgen05 (tc == 1)
+// or on warp-level mma.sync (tc == 2).
 #pragma once
 #include "cdx_rfft.cuh"
 
 namespace cdx {
 
+template <int N, int TCM>
+cudaError_t prepare_tc_mode() {
+  using G = Geom<N>;
+  constexpr int X = TCM == 2 ? umma_smem_extra<N>() : 0;
+  cudaError_t e;
+  if ((e = cudaFuncSetAttribute(row_pass_kernel<N, ROW_FFT, TCM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                G::SMEM_LINES + X)) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(row_pass_kernel<N, ROW_ITER, TCM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                G::SMEM_ROW_ITER + X)) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(col_pass_kernel<N, COL_FFT, TCM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                G::SMEM_LINES + X)) != cudaSuccess)
+    return e;
+  // at 4096 the noise-tolerant projection's three staged tiles and the tcgen05
+  // operands exceed a CTA's 227 KB: that one combination is refused at launch
+  constexpr int CI = G::SMEM_COL_CCD + X <= 232448 ? G::SMEM_COL_CCD + X : G::SMEM_COL_ITER + X;
+  return cudaFuncSetAttribute(col_pass_kernel<N, COL_ITER, TCM>, cudaFuncAttributeMaxDynamicSharedMemorySize, CI);
+}
+
 template <int N>
 cudaError_t prepare_tc() {
-  using G = Geom<N>;
-  cudaError_t e;
-  if ((e = cudaFuncSetAttribute(row_pass_kernel<N, ROW_FFT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                G::SMEM_LINES)) != cudaSuccess)
-    return e;
-  if ((e = cudaFuncSetAttribute(row_pass_kernel<N, ROW_ITER, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                G::SMEM_ROW_ITER)) != cudaSuccess)
-    return e;
-  if ((e = cudaFuncSetAttribute(col_pass_kernel<N, COL_FFT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                G::SMEM_LINES)) != cudaSuccess)
-    return e;
-  return cudaFuncSetAttribute(col_pass_kernel<N, COL_ITER, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              G::SMEM_COL_CCD);
+  cudaError_t e = prepare_tc_mode<N, 1>();
+  return e != cudaSuccess ? e : prepare_tc_mode<N, 2>();
 }
 
 template <int N>
@@ -69,9 +79,13 @@ template <int N>
 cudaError_t launch_row(const RowArgs& a, int batch, cudaStream_t st) {
   using G = Geom<N>;
   dim3 grid((a.rows + G::L - 1) / G::L, batch);
-  if (a.tc) {
-    if (a.mode == ROW_ITER) row_pass_kernel<N, ROW_ITER, true><<<grid, G::T, G::SMEM_ROW_ITER, st>>>(a);
-    else row_pass_kernel<N, ROW_FFT, true><<<grid, G::T, G::SMEM_LINES, st>>>(a);
+  if (a.tc == 1) {   // tcgen05 (the kernels' TCM 2)
+    constexpr int X = umma_smem_extra<N>();
+    if (a.mode == ROW_ITER) row_pass_kernel<N, ROW_ITER, 2><<<grid, G::T, G::SMEM_ROW_ITER + X, st>>>(a);
+    else row_pass_kernel<N, ROW_FFT, 2><<<grid, G::T, G::SMEM_LINES + X, st>>>(a);
+  } else if (a.tc == 2) {   // mma.sync (the kernels' TCM 1)
+    if (a.mode == ROW_ITER) row_pass_kernel<N, ROW_ITER, 1><<<grid, G::T, G::SMEM_ROW_ITER, st>>>(a);
+    else row_pass_kernel<N, ROW_FFT, 1><<<grid, G::T, G::SMEM_LINES, st>>>(a);
   } else {
     constexpr int SM = RGeom<N>::SMEM_ROW_ITER;
     if (a.mode != ROW_ITER) return launch_pdl(row_pass_rk<N, ROW_FFT, ALGO_ER>, grid, G::T, G::SMEM_LINES, st, a, pdl_of<N>(a.pdl_mode));
@@ -92,9 +106,13 @@ cudaError_t launch_col(const ColArgs& a, int batch, cudaStream_t st) {
   using G = Geom<N>;
   dim3 grid((a.cols + G::L - 1) / G::L, batch);
   const int smem_iter = a.proj == PROJ_CCD ? G::SMEM_COL_CCD : G::SMEM_COL_ITER;
-  if (a.tc) {
-    if (a.mode == COL_ITER) col_pass_kernel<N, COL_ITER, true><<<grid, G::T, smem_iter, st>>>(a);
-    else col_pass_kernel<N, COL_FFT, true><<<grid, G::T, G::SMEM_LINES, st>>>(a);
+  if (a.tc == 1) {
+    constexpr int X = umma_smem_extra<N>();
+    if (a.mode == COL_ITER) col_pass_kernel<N, COL_ITER, 2><<<grid, G::T, smem_iter + X, st>>>(a);
+    else col_pass_kernel<N, COL_FFT, 2><<<grid, G::T, G::SMEM_LINES + X, st>>>(a);
+  } else if (a.tc == 2) {
+    if (a.mode == COL_ITER) col_pass_kernel<N, COL_ITER, 1><<<grid, G::T, smem_iter, st>>>(a);
+    else col_pass_kernel<N, COL_FFT, 1><<<grid, G::T, G::SMEM_LINES, st>>>(a);
   } else {
     if (a.mode != COL_ITER) return launch_pdl(col_pass_rk<N, COL_FFT, PROJ_MODABS>, grid, G::T, G::SMEM_LINES, st, a, pdl_of<N>(a.pdl_mode));
     if (a.proj == PROJ_CCD) return launch_pdl(col_pass_rk<N, COL_ITER, PROJ_CCD>, grid, G::T, smem_iter, st, a, pdl_of<N>(a.pdl_mode));

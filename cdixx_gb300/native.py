@@ -20,7 +20,7 @@ CDX_HOST, CDX_DEVICE = 0, 1
 CDX_FFT_ORDER, CDX_CENTERED = 0, 1
 RAAR, ER, POSER, HIO, POSHIO, FHIO, SHRINKWRAP, XCORRELATION, KKT, TV = range(10)
 SHRINK_FOURIER, SHRINK_SPATIAL = 0, 1
-FFT_FP32, FFT_TC_BF16 = 0, 1
+FFT_FP32, FFT_TC_BF16, FFT_TC_MMA = 0, 1, 2
 
 
 class CdxError(RuntimeError):
@@ -374,6 +374,7 @@ def fft2(x, out, inverse=False, stream=None, fft_mode=0):
     """myFFT / myIFFT on device tensors (complex64, shape [..., rows, cols]).
 
     fft_mode 0 (FFT_FP32) is the FP32 SIMT path; 1 (FFT_TC_BF16) runs the
+    radix-16 passes on tcgen05, 2 (FFT_TC_MMA) on mma.sync; both run the
     radix-16 passes on the tensor cores with a split-BF16 operand.
     """
     rows, cols = x.shape[-2], x.shape[-1]

@@ -78,10 +78,12 @@ typedef struct cdx_params {
   float plateau_tol;         /* relative improvement that counts for plateau_iters (default 0.01) */
 } cdx_params;
 
-/* FFT arithmetic.  CDX_FFT_TC_BF16: the radix-16 passes run as tensor-core
- * MMAs with BF16 head/tail operands and FP32 accumulation (relative error per
- * 2-D transform ~1e-5 instead of ~1.5e-7); no reference counterpart. */
-enum { CDX_FFT_FP32 = 0, CDX_FFT_TC_BF16 = 1 };
+/* FFT arithmetic.  CDX_FFT_TC_BF16: the radix-16 passes run as tcgen05
+ * tensor-core MMAs (accumulator in TMEM) with BF16 head/tail operands and FP32
+ * accumulation (relative error per 2-D transform ~1e-5 instead of ~1.5e-7);
+ * CDX_FFT_TC_MMA: the same split product on warp-level mma.sync.  No
+ * reference counterpart. */
+enum { CDX_FFT_FP32 = 0, CDX_FFT_TC_BF16 = 1, CDX_FFT_TC_MMA = 2 };
 
 typedef struct cdx_stats {
   int steps;                 /* algorithm steps executed (iterations + shrinkwraps) */

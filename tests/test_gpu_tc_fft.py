@@ -1,8 +1,10 @@
-"""Tensor-core FFT mode (fft_mode = FFT_TC_BF16) against the FP64 oracle.
+"""Tensor-core FFT modes against the FP64 oracle: FFT_TC_BF16 (the radix-16
+passes as tcgen05 MMAs, accumulator in TMEM) and FFT_TC_MMA (the same product
+on warp-level mma.sync m16n8k16).
 
-The radix-16 passes run as m16n8k16 BF16 MMAs on a two-term split of each
-operand (x = hi + lo, both BF16; three products, FP32 accumulate), the other
-passes stay on the FP32 SIMT path.  The split keeps about 16 mantissa bits
+The radix-16 passes run as BF16 MMAs on a two-term split of each operand
+(x = hi + lo, both BF16; three products, FP32 accumulate), the other passes
+stay on the FP32 SIMT path.  The split keeps about 16 mantissa bits
 of each operand, so the error per radix-16 pass is ~2^-17 relative instead of
 FP32's 2^-24.  Stated tolerances:
   * 2-D FFT: relative L2 <= 5e-5 against float64 (measured ~1e-5),
@@ -29,23 +31,30 @@ def rel_l2(a, b):
 
 
 SIZES = [16, 32, 48, 64, 96, 128, 256, 384, 512, 768, 1024, 1536, 2048, 3072, 4096]
+MODES = ["tcgen05", "mma"]
 
 
+def mode_of(cdx, name):
+    return cdx.FFT_TC_BF16 if name == "tcgen05" else cdx.FFT_TC_MMA
+
+
+@pytest.mark.parametrize("mode", MODES)
 @pytest.mark.parametrize("n", SIZES)
-def test_tc_fft2_square(cdx, torch_cuda, n):
+def test_tc_fft2_square(cdx, torch_cuda, n, mode):
     torch = torch_cuda
     rng = np.random.default_rng(100 + n)
     batch = 2 if n <= 1024 else 1
     x = (rng.standard_normal((batch, n, n)) + 1j * rng.standard_normal((batch, n, n))).astype(np.complex64)
     xd = torch.from_numpy(x).cuda()
     out = torch.empty_like(xd)
-    cdx.fft2(xd, out, inverse=False, fft_mode=cdx.FFT_TC_BF16)
+    m = mode_of(cdx, mode)
+    cdx.fft2(xd, out, inverse=False, fft_mode=m)
     torch.cuda.synchronize()
     e_f = rel_l2(out.cpu().numpy(), np.fft.fft2(x.astype(np.complex128)))
-    cdx.fft2(xd, out, inverse=True, fft_mode=cdx.FFT_TC_BF16)
+    cdx.fft2(xd, out, inverse=True, fft_mode=m)
     torch.cuda.synchronize()
     e_i = rel_l2(out.cpu().numpy(), np.fft.ifft2(x.astype(np.complex128)) * n * n)
-    print(f"tc fft2 {n}x{n}: rel L2 vs float64 fwd {e_f:.3e} inv {e_i:.3e}")
+    print(f"{mode} fft2 {n}x{n}: rel L2 vs float64 fwd {e_f:.3e} inv {e_i:.3e}")
     assert e_f < TC_FFT_TOL and e_i < TC_FFT_TOL
 
 
@@ -85,15 +94,16 @@ def test_unknown_fft_mode_is_an_error(cdx, torch_cuda):
         cdx.Context(cdx.default_params(64, 64, fft_mode=7))
 
 
+@pytest.mark.parametrize("mode", MODES)
 @pytest.mark.parametrize("algo,beta", [("HIO", 1.0), ("RAAR", 0.9), ("ER", 1.0)])
-def test_tc_one_step_per_iterate(cdx, algo, beta):
+def test_tc_one_step_per_iterate(cdx, algo, beta, mode):
     """From the FP64 oracle's state after k-1 steps, one TC step gives rho_k
     within relative L2 1e-4 of the oracle's."""
     obj, sup, I = synth.config0_case(seed=11, n=256, photons=1e6)
     psi0 = synth.random_phase_start(I, 11)
     steps = 6
     ref = O.phase_retrieve(psi0, I, f"{steps}*{algo}", oversampling_spt=4.0, beta=beta, record=set(range(steps)))
-    p = cdx.default_params(256, 256, oversampling_spt=4.0, beta=beta, fft_mode=cdx.FFT_TC_BF16)
+    p = cdx.default_params(256, 256, oversampling_spt=4.0, beta=beta, fft_mode=mode_of(cdx, mode))
     worst = 0.0
     with cdx.Context(p) as ctx:
         ctx.set_pattern(0, I)
@@ -106,7 +116,7 @@ def test_tc_one_step_per_iterate(cdx, algo, beta):
             worst = max(worst, e)
             assert e <= TC_STEP_TOL, (algo, k + 1, e)
             state = psi_k
-    print(f"tc {algo}: worst one-step rel L2 {worst:.3e}")
+    print(f"{mode} {algo}: worst one-step rel L2 {worst:.3e}")
 
 
 def test_tc_reconstruction_quality_matches_fp32(cdx):
