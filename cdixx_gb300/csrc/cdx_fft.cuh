@@ -523,20 +523,20 @@ __device__ __forceinline__ void fft_pass_umma16(float2* buf, const float2* tw, U
     const int row = t & 127;
 #pragma unroll
     for (int half = 0; half < 2; ++half) {
-      __align__(16) __nv_bfloat16 rh[8], ih[8], rl[8], il[8];
+      uint32_t rh[4], ih[4], rl[4], il[4];   // packed pairs (element 2e in the low half)
 #pragma unroll
-      for (int e = 0; e < 8; ++e) {
-        const float2 v = x[half * 8 + e];
-        const __nv_bfloat16 a = __float2bfloat16_rn(v.x), b = __float2bfloat16_rn(v.y);
-        rh[e] = a;
-        ih[e] = b;
-        rl[e] = __float2bfloat16_rn(v.x - __bfloat162float(a));
-        il[e] = __float2bfloat16_rn(v.y - __bfloat162float(b));
+      for (int e = 0; e < 4; ++e) {
+        const float2 v0 = x[half * 8 + 2 * e], v1 = x[half * 8 + 2 * e + 1];
+        const BF2 re = split_bf16x2(v0.x, v1.x), im = split_bf16x2(v0.y, v1.y);
+        rh[e] = re.hi;
+        rl[e] = re.lo;
+        ih[e] = im.hi;
+        il[e] = im.lo;
       }
-      *reinterpret_cast<uint4*>(arow + umma::sw128(row, 0 + half)) = *reinterpret_cast<const uint4*>(rh);
-      *reinterpret_cast<uint4*>(arow + umma::sw128(row, 2 + half)) = *reinterpret_cast<const uint4*>(ih);
-      *reinterpret_cast<uint4*>(arow + umma::sw128(row, 4 + half)) = *reinterpret_cast<const uint4*>(rl);
-      *reinterpret_cast<uint4*>(arow + umma::sw128(row, 6 + half)) = *reinterpret_cast<const uint4*>(il);
+      *reinterpret_cast<uint4*>(arow + umma::sw128(row, 0 + half)) = make_uint4(rh[0], rh[1], rh[2], rh[3]);
+      *reinterpret_cast<uint4*>(arow + umma::sw128(row, 2 + half)) = make_uint4(ih[0], ih[1], ih[2], ih[3]);
+      *reinterpret_cast<uint4*>(arow + umma::sw128(row, 4 + half)) = make_uint4(rl[0], rl[1], rl[2], rl[3]);
+      *reinterpret_cast<uint4*>(arow + umma::sw128(row, 6 + half)) = make_uint4(il[0], il[1], il[2], il[3]);
     }
   }
   // the tensor core (async proxy) reads what the threads wrote; every thread

@@ -6,11 +6,7 @@
 // four keys with the SplitMix64 finaliser, so any pattern of any batch is
 // reproducible on its own.  Pattern p: 8 Gaussian blobs (centre uniform in a
 // centred disk of diameter n/4 by rejection, sigma U[2, 6] px, amplitude
-// U[0.3, 1]), masked to the disk, the whole object then shifted by whole
-// pixels so that the blobs' weighted centre (weights a sigma^2, the blobs'
-// integrals) sits at the array centre: |FFT|^2 cannot tell translations
-// apart, and a fixed centre gives the network a target it can predict;
-// I = |FFT(rho)|^2 scaled to `photons` and
+// U[0.3, 1]), masked to the disk; I = |FFT(rho)|^2 scaled to `photons` and
 // Poisson sampled (inversion for lambda < 10, Hoermann's transformed
 // rejection PTRS above; both with bounded loops).  A negative photon count
 // gives the noise-free expectation |FFT(rho)|^2 scaled to -photons.
@@ -50,10 +46,8 @@ __host__ __device__ __forceinline__ double unif(unsigned long long seed, unsigne
 
 enum { S_POS = 1, S_SIG = 2, S_AMP = 3, S_NOISE = 4 };
 constexpr int kBlobs = 8;
-constexpr int kPrm = kBlobs * 4 + 2;   // per pattern: 8 x (dy, dx, sigma, amplitude), disk offset (oy, ox)
 
-// blob parameters (dy, dx, sigma, amplitude) of pattern `first + b`, shifted by
-// the rounded weighted centre, and the disk's offset (the same shift)
+// blob parameters (dx, dy, sigma, amplitude) of pattern `first + b`
 __global__ void k_blob_params(int n, int count, unsigned long long seed, long long first, double* __restrict__ prm) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= count) return;
@@ -71,27 +65,12 @@ __global__ void k_blob_params(int n, int count, unsigned long long seed, long lo
         break;
       }
     }
-    double* q = prm + (long long)b * kPrm + k * 4;
+    double* q = prm + ((long long)b * kBlobs + k) * 4;
     q[0] = dx;
     q[1] = dy;
     q[2] = 2.0 + 4.0 * unif(seed, pat, S_SIG, (unsigned long long)k);
     q[3] = 0.3 + 0.7 * unif(seed, pat, S_AMP, (unsigned long long)k);
   }
-  double* q = prm + (long long)b * kPrm;
-  double w = 0.0, cy = 0.0, cx = 0.0;
-  for (int k = 0; k < kBlobs; ++k) {
-    const double wk = q[4 * k + 3] * q[4 * k + 2] * q[4 * k + 2];
-    w += wk;
-    cy += wk * q[4 * k];
-    cx += wk * q[4 * k + 1];
-  }
-  const double oy = rint(cy / w), ox = rint(cx / w);
-  for (int k = 0; k < kBlobs; ++k) {
-    q[4 * k] -= oy;
-    q[4 * k + 1] -= ox;
-  }
-  q[4 * kBlobs] = -oy;
-  q[4 * kBlobs + 1] = -ox;
 }
 
 // object (centred), its amplitude / phase / support targets
@@ -104,9 +83,8 @@ __global__ void k_blob_render(int n, long long total, const double* __restrict__
     const int p = (int)(i - b * P);
     const int y = p / n, x = p - y * n;
     double v = 0.0;
-    const double* q = prm + b * kPrm;
-    const double ry = y - c - q[4 * kBlobs], rx = x - c - q[4 * kBlobs + 1];
-    if (ry * ry + rx * rx <= r * r) {
+    if ((y - c) * (y - c) + (x - c) * (x - c) <= r * r) {
+      const double* q = prm + b * kBlobs * 4;
       for (int k = 0; k < kBlobs; ++k) {
         const double ey = y - c - q[4 * k], ex = x - c - q[4 * k + 1], s = q[4 * k + 2];
         v += q[4 * k + 3] * exp(-(ey * ey + ex * ex) / (2.0 * s * s));
@@ -233,7 +211,7 @@ extern "C" int cdx_forward_model(int n, int count, unsigned long long seed, long
   cudaStream_t st = (cudaStream_t)stream;
   const long long P = (long long)n * n, tot = P * count;
   auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
-  const size_t o_sum = al(sizeof(double) * count * kPrm);
+  const size_t o_sum = al(sizeof(double) * count * kBlobs * 4);
   const size_t o_rho = o_sum + al(sizeof(double) * count);
   const size_t need = o_rho + sizeof(float2) * tot;
   int dev = 0;

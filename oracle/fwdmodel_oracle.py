@@ -48,26 +48,14 @@ def blob_params(n, seed, pat):
     return out
 
 
-def centre_shift(prm):
-    """Whole-pixel shift that puts the blobs' weighted centre (weights a sigma^2)
-    at the array centre (k_blob_params)."""
-    w = sum(a * s * s for _, _, s, a in prm)
-    cy = sum(a * s * s * dy for dy, _, s, a in prm) / w
-    cx = sum(a * s * s * dx for _, dx, s, a in prm) / w
-    return float(np.rint(cy)), float(np.rint(cx))
-
-
 def render(n, seed, pat):
-    """(object amplitude, support target) of pattern `pat`, float64: the blobs
-    masked to the disk, shifted so their weighted centre is the array centre."""
+    """(object amplitude, support target) of pattern `pat`, centred, float64."""
     c, r = n / 2.0, 0.25 * n / 2.0
     yy, xx = np.mgrid[0:n, 0:n].astype(np.float64)
-    prm = blob_params(n, seed, pat)
-    oy, ox = centre_shift(prm)
     v = np.zeros((n, n))
-    for dy, dx, s, a in prm:
-        v += a * np.exp(-((yy - c - (dy - oy)) ** 2 + (xx - c - (dx - ox)) ** 2) / (2.0 * s * s))
-    v *= (yy - c + oy) ** 2 + (xx - c + ox) ** 2 <= r * r
+    for dx, dy, s, a in blob_params(n, seed, pat):
+        v += a * np.exp(-((yy - c - dx) ** 2 + (xx - c - dy) ** 2) / (2.0 * s * s))
+    v *= (yy - c) ** 2 + (xx - c) ** 2 <= r * r
     return v, (v > 1e-3).astype(np.float64)
 
 

@@ -42,22 +42,3 @@ def test_backward_matches_finite_differences():
         lm = U.forward_backward(q, I, amp, ph, sup, n, levels, base, backward=False)[0]
         fd = (lp - lm) / (2 * h)
         assert abs(fd - g[i]) <= 1e-6 + 1e-4 * abs(fd), (i, fd, g[i])
-
-
-def test_forward_model_objects_sit_on_the_array_centre():
-    """The restated forward model shifts each object by whole pixels so that
-    its blobs' weighted centre (weights a sigma^2) is within half a pixel of
-    the array centre; the shift moves the disk mask with the blobs."""
-    from oracle import fwdmodel_oracle as FM
-    n = 64
-    for pat in range(6):
-        prm = FM.blob_params(n, 5, pat)
-        oy, ox = FM.centre_shift(prm)
-        w = sum(a * s * s for _, _, s, a in prm)
-        cy = sum(a * s * s * (dy - oy) for dy, _, s, a in prm) / w
-        cx = sum(a * s * s * (dx - ox) for _, dx, s, a in prm) / w
-        assert abs(cy) <= 0.5 and abs(cx) <= 0.5
-        v, sup = FM.render(n, 5, pat)
-        yy, xx = np.mgrid[0:n, 0:n]
-        disk = (yy - n / 2 + oy) ** 2 + (xx - n / 2 + ox) ** 2 <= (n / 8) ** 2
-        assert np.all(v[~disk] == 0) and v[disk].max() > 0.1
