@@ -399,7 +399,10 @@ BATCH_ALGO = "500*HIO+500*ER"
 def batched_section():
     """512 patterns of uneven sizes (uniform over BATCH_SIZES squared, photons
     log-uniform 1e5..1e8, blob objects in a support of 1/4 linear size), HIO and
-    ER 500 iterations each, every size one context, all run as one CUDA graph."""
+    ER 500 iterations each, every size one context, all run as one CUDA graph.
+    Each context first tunes its launch variant (autotune) and is timed alone,
+    so the line shows the tuner's choice per size and what running the sizes
+    as concurrent branches of one graph gains over running them one by one."""
     import torch
     from cdixx_gb300 import native as cdx
     from cdixx_gb300 import unet
@@ -407,16 +410,24 @@ def batched_section():
     sizes = rng.choice(BATCH_SIZES, BATCH_PATTERNS)
     photons = 10 ** rng.uniform(5, 8, BATCH_PATTERNS)
     ctxs = []
+    per_size = {}
     px = 0
     for n in BATCH_SIZES:
         idx = np.nonzero(sizes == n)[0]
         if len(idx) == 0:
             continue
-        ctx = cdx.Context(cdx.default_params(int(n), int(n), batch=len(idx), beta=0.9, oversampling_spt=2.0))
+        ctx = cdx.Context(cdx.default_params(int(n), int(n), batch=len(idx), beta=0.9, oversampling_spt=2.0,
+                                             autotune=1))
         for j, p in enumerate(idx):
             I, _, _, _ = unet.forward_model(int(n), 1, SEED + 2, int(p), float(photons[p]))
             ctx.set_pattern(j, I[0])
         ctx.random_start(SEED + int(n))
+        ctx.run("2*HIO")                  # tunes the launch variant on this context's data
+        ctx.random_start(SEED + int(n))
+        alone = ctx.run(BATCH_ALGO)["gpu_ms"]
+        pdl, chunk, _ = ctx.tuning()
+        per_size[str(n)] = {"patterns": int(len(idx)), "alone_ms": alone,
+                            "tuned": {"pdl": pdl, "row_chunk_bits": chunk}}
         ctxs.append(ctx)
         px += len(idx) * int(n) * int(n)
     g = cdx.Group(ctxs)
@@ -432,10 +443,13 @@ def batched_section():
     for c in ctxs:
         c.close()
     iters = 1000
+    sum_alone = float(sum(v["alone_ms"] for v in per_size.values()))
     return {"metric": "patterns/s", "patterns": BATCH_PATTERNS, "sizes": list(BATCH_SIZES),
             "algorithm": BATCH_ALGO, "patterns_per_s": BATCH_PATTERNS / (ms / 1000.0),
             "pixel_iterations_per_s": px * iters / (ms / 1000.0), "gpu_ms": ms, "wall_ms_incl_graph_build": wall * 1000,
-            "contexts": len(ctxs), "launch": "one CUDA graph (cdx_group) with one branch per size"}
+            "contexts": len(ctxs), "per_size": per_size, "sizes_one_by_one_ms": sum_alone,
+            "graph_gain_over_one_by_one": sum_alone / ms,
+            "launch": "one CUDA graph (cdx_group) with one branch per size"}
 
 
 # ---------------------------------------------------------------------------
