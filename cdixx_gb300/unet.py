@@ -7,6 +7,11 @@
     psi0, support = net.warm_start(I, out)                        # for Context.set_initial / set_support
 
 Everything runs on the GPU through the library; there is no CPU fallback.
+The network's kernels run on a stream of its own; every method first makes
+that stream wait for the caller's current stream (so tensors the caller just
+produced, e.g. by forward_model, are complete) and afterwards makes the
+caller's current stream wait for the network's (so its outputs are complete
+for whatever the caller runs next).
 """
 from __future__ import annotations
 
@@ -41,11 +46,21 @@ def default_config(**kw) -> UNetConfig:
 
 class UNet:
     def __init__(self, stream=None, **cfg):
+        import torch
         self.cfg = default_config(**cfg)
         self._h = ctypes.c_void_p()
-        st = ctypes.c_void_p(stream) if stream is not None else None
-        native.check(native.lib().cdx_unet_create(ctypes.byref(self.cfg), st, ctypes.byref(self._h)))
+        self.stream = torch.cuda.Stream() if stream is None else torch.cuda.ExternalStream(stream)
+        native.check(native.lib().cdx_unet_create(ctypes.byref(self.cfg), ctypes.c_void_p(self.stream.cuda_stream),
+                                                  ctypes.byref(self._h)))
         self.n_params = int(native.lib().cdx_unet_param_count(self._h))
+
+    def _enter(self):
+        import torch
+        self.stream.wait_stream(torch.cuda.current_stream())
+
+    def _leave(self):
+        import torch
+        torch.cuda.current_stream().wait_stream(self.stream)
 
     def close(self):
         if self._h:
@@ -86,17 +101,23 @@ class UNet:
         n = self.cfg.n
         if out is None:
             out = torch.empty((b, 4, n, n), dtype=torch.float32, device=intensity.device)
+        self._enter()
         native.check(native.lib().cdx_unet_forward(self._h, _ptr(intensity), _ptr(out), b))
+        self._leave()
         return out
 
     def loss_backward(self, intensity, amp_t, phase_t, support_t) -> float:
         loss = ctypes.c_double()
+        self._enter()
         native.check(native.lib().cdx_unet_loss_backward(self._h, _ptr(intensity), _ptr(amp_t), _ptr(phase_t),
                                                          _ptr(support_t), intensity.shape[0], ctypes.byref(loss)))
+        self._leave()
         return loss.value
 
     def adam_step(self, lr=1e-3):
+        self._enter()
         native.check(native.lib().cdx_unet_adam_step(self._h, ctypes.c_float(lr)))
+        self._leave()
 
     def train_step(self, intensity, amp_t, phase_t, support_t, lr=1e-3) -> float:
         loss = self.loss_backward(intensity, amp_t, phase_t, support_t)
@@ -109,19 +130,22 @@ class UNet:
         b, n = intensity.shape[0], self.cfg.n
         psi0 = torch.empty((b, n, n), dtype=torch.complex64, device=intensity.device)
         sup = torch.empty((b, n, n), dtype=torch.float32, device=intensity.device)
+        self._enter()
         native.check(native.lib().cdx_unet_warm_start(self._h, _ptr(intensity), _ptr(out), b, int(dilate), _ptr(psi0),
                                                       _ptr(sup)))
+        self._leave()
         return psi0, sup
 
 
 def forward_model(n, count, seed, first=0, photons=1e6, device="cuda", stream=None):
-    """Seeded synthetic pairs on the GPU: (intensity FFT order, amplitude, phase, support; centred)."""
+    """Seeded synthetic pairs on the GPU: (intensity FFT order, amplitude, phase, support; centred).
+    Queued on `stream` (default: the current torch stream) without waiting for it."""
     import torch
     I = torch.empty((count, n, n), dtype=torch.float32, device=device)
     a = torch.empty_like(I)
     p = torch.empty_like(I)
     s = torch.empty_like(I)
-    st = ctypes.c_void_p(stream) if stream is not None else None
+    st = ctypes.c_void_p(stream if stream is not None else torch.cuda.current_stream().cuda_stream)
     native.check(native.lib().cdx_forward_model(n, count, ctypes.c_ulonglong(seed), first, ctypes.c_double(photons),
                                                 _ptr(I), _ptr(a), _ptr(p), _ptr(s), st))
     return I, a, p, s

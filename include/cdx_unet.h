@@ -75,7 +75,9 @@ int cdx_unet_warm_start(cdx_unet* u, const float* intensity, const float* out, i
  * I = |FFT(rho)|^2 scaled to `photons` and Poisson-sampled).  Pattern p of
  * the call uses counter-based random numbers keyed by (seed, first + p).
  * intensity [count][n][n] FFT order; amp_t, phase_t, support_t centred (any
- * of the three may be null).  photons < 0: no Poisson step, I scaled to -photons. */
+ * of the three may be null).  photons < 0: no Poisson step, I scaled to -photons.
+ * The work is queued on `stream` and the call returns without waiting for it:
+ * a consumer on another stream must wait for `stream` first. */
 int cdx_forward_model(int n, int count, unsigned long long seed, long long first, double photons,
                       float* intensity, float* amp_t, float* phase_t, float* support_t, void* stream);
 

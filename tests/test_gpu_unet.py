@@ -192,3 +192,24 @@ def test_tcgen05_and_mma_sync_convolutions_agree(cdx, torch_cuda):
     rg = np.linalg.norm(g1 - g0) / np.linalg.norm(g0)
     print(f"tcgen05 vs mma.sync: output {ro:.2e}, loss {abs(l1 - l0) / l0:.2e}, gradient {rg:.2e}")
     assert ro < 5e-3 and abs(l1 - l0) <= 2e-3 * l0 and rg < 3e-2
+
+
+def test_training_needs_no_host_synchronisation(cdx, torch_cuda):
+    """The forward model queues its batch on the caller's stream and returns;
+    the network's own stream waits for it.  Training with no host sync must
+    give the same losses, bit for bit, as training with a device sync after
+    every generated batch (every kernel here is deterministic)."""
+    torch = torch_cuda
+    from cdixx_gb300 import unet
+    runs = []
+    for sync in (False, True):
+        with unet.UNet(n=64, levels=3, base=16, batch=16, seed=9) as net:
+            losses = []
+            for k in range(25):
+                I, a, p, s = unet.forward_model(64, 16, 4321, k * 16, 1e6)
+                if sync:
+                    torch.cuda.synchronize()
+                losses.append(net.train_step(I, a, p, s, 2e-3))
+            runs.append(losses)
+    assert np.all(np.isfinite(runs[0]))
+    assert runs[0] == runs[1]
