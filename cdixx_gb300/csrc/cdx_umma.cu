@@ -20,23 +20,9 @@ extern "C" int cdx_gemm_bf16_tc(const void* A, const void* B, float* D, int M, i
   umma::DenseOp op{(const __nv_bfloat16*)A, (const __nv_bfloat16*)B, D, K, N};
   cudaStream_t st = (cudaStream_t)stream;
   cudaError_t e;
-  if (N <= 32) {
-    e = cudaFuncSetAttribute(umma::k_umma<32, umma::DenseOp>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             umma::smem_bytes(32));
-    if (e == cudaSuccess)
-      umma::k_umma<32><<<dim3((M + 127) / 128, (N + 31) / 32), 128, umma::smem_bytes(32), st>>>(op, M, N, K, err_flag);
-  } else if (N <= 64) {
-    e = cudaFuncSetAttribute(umma::k_umma<64, umma::DenseOp>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             umma::smem_bytes(64));
-    if (e == cudaSuccess)
-      umma::k_umma<64><<<dim3((M + 127) / 128, (N + 63) / 64), 128, umma::smem_bytes(64), st>>>(op, M, N, K, err_flag);
-  } else {
-    e = cudaFuncSetAttribute(umma::k_umma<128, umma::DenseOp>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             umma::smem_bytes(128));
-    if (e == cudaSuccess)
-      umma::k_umma<128><<<dim3((M + 127) / 128, (N + 127) / 128), 128, umma::smem_bytes(128), st>>>(op, M, N, K,
-                                                                                                   err_flag);
-  }
+  if (N <= 32) e = umma::launch_ps<32>(op, M, N, K, err_flag, st);
+  else if (N <= 64) e = umma::launch_ps<64>(op, M, N, K, err_flag, st);
+  else e = umma::launch_ps<128>(op, M, N, K, err_flag, st);
   if (e == cudaSuccess) e = cudaGetLastError();
   if (e != cudaSuccess) return set_error(CDX_ERR_CUDA, std::string("tensor-core GEMM: ") + cudaGetErrorString(e));
   return CDX_OK;

@@ -661,15 +661,8 @@ ConvShape conv_shape(const Net* u, const Layer& l, int count) {
 
 template <int BN, class Op>
 int launch_umma(const Op& op, long long M, int NC, int K, int* err, cudaStream_t st) {
-  static bool attr = false;   // per process; the attribute is per device function, cheap to repeat
-  if (!attr) {
-    U_CK(cudaFuncSetAttribute(umma::k_umma<BN, Op>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              umma::smem_bytes(BN)));
-    attr = true;
-  }
-  const dim3 grid((unsigned)((M + 127) / 128), (unsigned)((NC + BN - 1) / BN));
-  umma::k_umma<BN, Op><<<grid, 128, umma::smem_bytes(BN), st>>>(op, (int)M, NC, K, err);
-  U_CK(cudaGetLastError());
+  const cudaError_t e = umma::launch_ps<BN, Op>(op, (int)M, NC, K, err, st);
+  U_CK(e);
   return CDX_OK;
 }
 
