@@ -683,14 +683,15 @@ def run_gpu(args):
     e2e_vals = []
     h2d = I.nbytes + psi0.nbytes
     d2h = 2 * psi0.nbytes + I.nbytes
-    pe = cdx.default_params(N, N, oversampling_spt=4.0, beta=BETA, shrink_threshold=0.1, use_graph=0, autotune=1)
+    # the call keeps its context and the job's CUDA graph for the next call with the same parameters
+    pe = cdx.default_params(N, N, oversampling_spt=4.0, beta=BETA, shrink_threshold=0.1, autotune=1)
     # the job's host buffers in pinned memory (inputs and the results the call writes)
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
     I_h, psi0_h = pin(I), pin(psi0)
     outs = (torch.empty(psi0.shape, dtype=torch.complex64, pin_memory=True).numpy(),
             torch.empty(psi0.shape, dtype=torch.complex64, pin_memory=True).numpy(),
             torch.empty(I.shape, dtype=torch.float32, pin_memory=True).numpy())
-    for k in range(4):   # the first job warms the host allocator and the page cache; median of three
+    for k in range(4):   # the first job warms the host allocator, the page cache and the kept graph; median of three
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         cdx.phase_retrieve_host(pe, JOB_ALGO, I_h, psi0_h, out=outs)

@@ -106,6 +106,7 @@ struct cdx_ctx {
   float* weights = nullptr;
   size_t weights_cap = 0;
   void* arena = nullptr;
+  size_t arena_bytes = 0;
 
   // host state
   std::vector<char> have_pattern;
@@ -803,6 +804,7 @@ int cdx_create(const cdx_params* p, void* stream, cdx_ctx** out) {
     cudaGetLastError();
     return fail(set_error(CDX_ERR_NOMEM, "device arena of " + std::to_string(off) + " bytes"));
   }
+  c->arena_bytes = off;
   char* a = (char*)c->arena;
   c->rho = (float2*)(a + o_rho);
   c->work = (float2*)(a + o_work);
@@ -1086,15 +1088,68 @@ int cdx_get_support(cdx_ctx* c, int idx, float* out, int where) {
   return copy_out(out, c->spt + (long long)idx * c->npx, sizeof(float) * c->npx, where, c->st);
 }
 
+namespace {
+
+// cdx_phase_retrieve_host keeps the context of its last call (device arrays and
+// the CUDA graph of the last algorithm) for the next call with the same
+// parameters on the same device, as the reference keeps its memory pool and its
+// cuFFT plan for the whole process (memManager.cc, cudaConfig.cu:137-159).
+struct HostSlot {
+  cdx_ctx* ctx = nullptr;
+  cdx_params key{};
+  int device = -1;
+  bool busy = false;
+};
+std::mutex g_host_mu;
+HostSlot g_host_slot;
+
+// Return a kept context to the state cdx_create leaves: arena zeroed,
+// vars.threshold 0.5, rect support, no pattern or initial iterate set.
+int ctx_reset(cdx_ctx* c) {
+  CDX_CK(cudaSetDevice(c->device));
+  CDX_CK(cudaMemsetAsync(c->arena, 0, c->arena_bytes, c->st));
+  CDX_CK(state_init(c->dstate, c->batch, 0.5f, c->st));
+  int e = reset_support(c, 0, c->batch);
+  if (e) return e;
+  if (c->pr_cache) {
+    const size_t nb = (size_t)c->batch * c->npx;
+    CDX_CK(cudaMemsetAsync(c->pr_cache, 0, sizeof(float2) * nb, c->st));
+    CDX_CK(cudaMemsetAsync(c->pr_gamma0, 0, sizeof(float2) * nb, c->st));
+    CDX_CK(cudaMemsetAsync(c->pr_state, 0, sizeof(PrtfState) * c->batch, c->st));
+  }
+  c->have_pattern.assign(c->batch, 0);
+  c->fresh.assign(c->batch, 0);
+  c->have_initial = false;
+  c->psi_in_work = false;
+  c->pr_valid = false;
+  CDX_CK(cudaStreamSynchronize(c->st));
+  return CDX_OK;
+}
+
+}  // namespace
+
 int cdx_phase_retrieve_host(const cdx_params* p, const char* algorithm, const float* inten, const float* psi0,
                             unsigned long long seed, float* rho_out, float* psi_out, float* support_out,
                             cdx_stats* stats) {
   if (!p || !inten) return set_error(CDX_ERR_ARG, "null argument");
   cdx_params q = *p;
   q.batch = 1;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return set_error(CDX_ERR_NOLIB, "no CUDA device");
   cdx_ctx* c = nullptr;
-  int e = cdx_create(&q, nullptr, &c);
-  if (e) return e;
+  bool kept = false;
+  {
+    std::lock_guard<std::mutex> lk(g_host_mu);
+    if (g_host_slot.ctx && !g_host_slot.busy && g_host_slot.device == dev &&
+        std::memcmp(&g_host_slot.key, &q, sizeof q) == 0) {
+      c = g_host_slot.ctx;
+      g_host_slot.busy = true;
+      kept = true;
+    }
+  }
+  int e = kept ? ctx_reset(c) : cdx_create(&q, nullptr, &c);
+  if (e && !kept) return e;
+  if (e) goto done;
   if ((e = cdx_set_pattern(c, 0, inten, CDX_HOST, CDX_FFT_ORDER, 1.f))) goto done;
   e = psi0 ? cdx_set_initial(c, 0, psi0, CDX_HOST) : cdx_random_start(c, seed);
   if (e) goto done;
@@ -1103,8 +1158,35 @@ int cdx_phase_retrieve_host(const cdx_params* p, const char* algorithm, const fl
   if (psi_out && (e = cdx_get_fourier(c, 0, psi_out, CDX_HOST))) goto done;
   if (support_out && (e = cdx_get_support(c, 0, support_out, CDX_HOST))) goto done;
 done:
-  cdx_destroy(c);
+  {
+    std::unique_lock<std::mutex> lk(g_host_mu);
+    if (kept) {
+      if (e) g_host_slot = HostSlot{};   // a context that failed is not kept
+      else {
+        g_host_slot.busy = false;
+        c = nullptr;
+      }
+    } else if (!e && !g_host_slot.ctx) {
+      g_host_slot.ctx = c;
+      g_host_slot.key = q;
+      g_host_slot.device = dev;
+      g_host_slot.busy = false;
+      c = nullptr;
+    }
+  }
+  if (c) cdx_destroy(c);
   return e;
+}
+
+int cdx_release_host_cache(void) {
+  cdx_ctx* c = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_host_mu);
+    if (g_host_slot.busy) return set_error(CDX_ERR_STATE, "the kept context is in use by a running call");
+    c = g_host_slot.ctx;
+    g_host_slot = HostSlot{};
+  }
+  return c ? cdx_destroy(c) : CDX_OK;
 }
 
 // ---------------------------------------------------------------- primitives

@@ -84,6 +84,7 @@ _SIGS = {
     "cdx_get_tuning": [_P, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.c_char_p, _I],
     "cdx_phase_retrieve_host": [ctypes.POINTER(Params), ctypes.c_char_p, _P, _P, ctypes.c_ulonglong,
                                 _P, _P, _P, ctypes.POINTER(Stats)],
+    "cdx_release_host_cache": [],
     "cdx_fft2": [_P, _P, _I, _I, _I, _I, _P],
     "cdx_fft2_ex": [_P, _P, _I, _I, _I, _I, _I, _P],
     "cdx_ccd_noise": [_P, _LL, _F, _F, _I, ctypes.c_ulonglong, _P],
@@ -362,6 +363,11 @@ def phase_retrieve_host(params: Params, algorithm: str, intensity, psi0=None, se
                                         None if p0 is None else vp(p0), seed, vp(rho), vp(psi), vp(spt),
                                         ctypes.byref(s)))
     return rho, psi, spt, s.as_dict()
+
+
+def release_host_cache():
+    """Free the context phase_retrieve_host keeps for its next call (cdx_release_host_cache)."""
+    check(lib().cdx_release_host_cache())
 
 
 def _stream_ptr(stream):

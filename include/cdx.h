@@ -181,10 +181,16 @@ int cdx_get_tuning(cdx_ctx* ctx, int* pdl, int* row_chunk, char* report, int cap
 /* ---------------------------------------------------------------- one call, host buffers */
 /* Whole path for one pattern with HOST buffers: create, set pattern, set
  * Psi0 (or a random start when psi0 is NULL), run, copy rho/Psi/support
- * back, destroy.  Outputs may be NULL. */
+ * back.  Outputs may be NULL.  The call keeps its context (device arrays and
+ * the CUDA graph of the last algorithm) for the next call with the same
+ * parameters on the same device, returned to the state of a new context
+ * before reuse (the reference keeps its memory pool and cuFFT plan for the
+ * whole process, memManager.cc, cudaConfig.cu:137-159); concurrent calls
+ * each get their own.  cdx_release_host_cache frees the kept context. */
 int cdx_phase_retrieve_host(const cdx_params* p, const char* algorithm, const float* intensity,
                             const float* psi0, unsigned long long seed, float* rho_out, float* psi_out,
                             float* support_out, cdx_stats* stats);
+int cdx_release_host_cache(void);
 
 /* ---------------------------------------------------------------- primitives (device pointers) */
 /* myFFT / myIFFT (cudaConfig.cu:175-180): unnormalised 2-D C2C transform of

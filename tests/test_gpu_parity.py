@@ -334,6 +334,30 @@ def test_host_buffer_entry_matches_context(cdx):
         assert np.array_equal(ctx.get_support(0), spt)
 
 
+def test_host_buffer_entry_reuses_its_context_like_a_new_one(cdx):
+    """The host-buffer call keeps its context (arrays and CUDA graph) for the
+    next call with the same parameters.  A reused context must give the bits
+    of a new one: three calls in a row -- different patterns, the same, the
+    shrinkwrap threshold of the previous run not carried over -- each equal
+    to a fresh context's run; then after the kept context is released."""
+    alg = "3*(8*HIO+1*shrinkWrap)+4*ER"
+    cases = [blob_case(n=128, seed=s) for s in (3, 4, 3)]
+    p = cdx.default_params(128, 128, oversampling_spt=2.0, shrink_threshold=0.1, beta=0.9)
+    for k, (I, psi0) in enumerate(cases + cases[:1]):
+        if k == 3:
+            cdx.release_host_cache()
+        rho, psi, spt, st = cdx.phase_retrieve_host(p, alg, I, psi0)
+        with cdx.Context(p) as ctx:
+            ctx.set_pattern(0, I)
+            ctx.set_initial(0, psi0)
+            s = ctx.run(alg)
+            assert np.array_equal(ctx.get_object(0), rho), k
+            assert np.array_equal(ctx.get_fourier(0), psi), k
+            assert np.array_equal(ctx.get_support(0), spt), k
+            assert s["threshold"] == st["threshold"], k
+    cdx.release_host_cache()
+
+
 def test_random_start_is_binary_phase(cdx):
     I, _ = blob_case(n=128)
     p = cdx.default_params(128, 128, oversampling_spt=2.0)
