@@ -38,15 +38,18 @@ struct RPass {
   static constexpr int TWO = tw_offset_x(N, PLAN, P);
 };
 
-// largest chunk bits valid for every pass: NR is a multiple of 2^cb
+// largest chunk bits valid for every pass: NR = N / R is a multiple of 2^cb for
+// every radix R of the length (both plans have the same radices), so the map
+// below is a bijection onto (line, butterfly) in every pass; e.g. 2048 -> 7,
+// 192 (NR 12, 48, 64) -> 2, 384 -> 3, 96 -> 1, 48 -> 0
 template <int N>
 __host__ __device__ constexpr int rfft_cb_max() {
-  if ((N & (N - 1)) != 0) return 0;
-  int rmax = 1;
-  for (int p = 0; plan_radix(N, p) != 0; ++p) rmax = plan_radix(N, p) > rmax ? plan_radix(N, p) : rmax;
-  int nr = N / rmax, c = 0;
-  while ((2 << c) <= nr) ++c;
-  return c;
+  int c = 0;
+  for (;;) {
+    for (int p = 0; plan_radix(N, p) != 0; ++p)
+      if ((N / plan_radix(N, p)) % (2 << c) != 0) return c;
+    ++c;
+  }
 }
 
 // (l, j) of butterfly b of this thread in a radix-R pass; false past the end
