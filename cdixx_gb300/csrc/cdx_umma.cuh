@@ -304,11 +304,15 @@ inline int ps_smem_bytes(int bn) { return ws_smem_bytes(bn); }
 
 // Launch k_umma_ps with as many CTAs per N tile as fit on the device at once
 // (each loops over M tiles).  The attribute and occupancy are looked up once
-// per instantiation.
+// per instantiation and device (a benign race between host threads writes
+// the same value).
 template <int BN, class Op>
 cudaError_t launch_ps(const Op& op, int M, int N, int K, int* err, cudaStream_t st) {
-  static int per_sm = 0;
-  cudaError_t e;
+  static int cached[64];   // resident CTAs per SM, per device (0: not looked up yet)
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  int per_sm = (dev >= 0 && dev < 64) ? cached[dev] : 0;
   if (per_sm == 0) {
     if ((e = cudaFuncSetAttribute(k_umma_ps<BN, Op>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   ps_smem_bytes(BN))) != cudaSuccess)
@@ -318,6 +322,7 @@ cudaError_t launch_ps(const Op& op, int M, int N, int K, int* err, cudaStream_t 
         cudaSuccess)
       return e;
     per_sm = b > 0 ? b : 1;
+    if (dev >= 0 && dev < 64) cached[dev] = per_sm;
   }
   const int mt = (M + BM - 1) / BM, nt = (N + BN - 1) / BN;
   const long long slots = (long long)per_sm * sm_count();
