@@ -427,7 +427,8 @@ def batched_section():
         alone = ctx.run(BATCH_ALGO)["gpu_ms"]
         pdl, chunk, _ = ctx.tuning()
         per_size[str(n)] = {"patterns": int(len(idx)), "alone_ms": alone,
-                            "tuned": {"pdl": pdl, "row_chunk_bits": chunk}}
+                            "tuned": {"pdl_col": int(pdl > 0 and pdl & 1), "pdl_row": int(pdl > 0 and pdl >> 1 & 1),
+                                      "row_chunk_bits": chunk}}
         ctxs.append(ctx)
         px += len(idx) * int(n) * int(n)
     g = cdx.Group(ctxs)

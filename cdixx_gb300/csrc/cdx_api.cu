@@ -10,6 +10,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <tuple>
@@ -126,7 +127,7 @@ struct cdx_ctx {
   bool pr_reached = false;     // set while enqueueing
 
   // launch variant (autotune): RowArgs/ColArgs knobs, and what was measured
-  int tune_pdl_mode = 0, tune_cb_plus1 = 0;
+  int tune_pdl_col = 0, tune_pdl_row = 0, tune_cb_plus1 = 0;   // pdl: 0 per-length default, 1 plain, 2 PDL
   int* derr = nullptr;        // bulk-copy wait timeouts of the pass kernels (bit 0)
   bool tuned = false;
   std::string tune_report;
@@ -282,7 +283,7 @@ int col_iter(cdx_ctx* c, bool from_psi, bool rf, float2* psi_proj = nullptr) {
   a.scale = 1.f;
   a.ccd_scale = 1.f / c->p.exposure;
   a.ccd_rcolor = (float)c->p.rcolor;
-  a.pdl_mode = c->tune_pdl_mode;
+  a.pdl_mode = c->tune_pdl_col;
   a.err = c->derr;
   CDX_CK(col_launcher(c->rows)(a, c->batch, c->st));
   return CDX_OK;
@@ -309,7 +310,7 @@ int row_iter(cdx_ctx* c, int algo) {
   a.inv_n = (float)(1.0 / ((double)c->rows * c->cols));   // applyNorm(.., 1./(row*column)), cdi.cc:353
   a.beta = c->p.beta;
   a.cb_plus1 = c->tune_cb_plus1;
-  a.pdl_mode = c->tune_pdl_mode;
+  a.pdl_mode = c->tune_pdl_row;
   a.err = c->derr;
   CDX_CK(row_launcher(c->cols)(a, c->batch, c->st));
   return CDX_OK;
@@ -472,24 +473,49 @@ int prepare_run(cdx_ctx* c, const char* algorithm, std::vector<int>& steps, SwPl
 
 // Autotuner: before the first run of a context with autotune set, time the
 // iteration (column pass + row pass, HIO; eight of them captured in a graph,
-// as runs execute) under each launch variant --
-// programmatic dependent launch off/on x the row pass's butterfly chunk bits
-// (the default and up to two below it) -- on a copy of the context's own
-// state, restore the state, and keep the fastest.  Decisions are cached per
-// (device, rows, cols, batch) for the process.
+// as runs execute) under each launch variant -- programmatic dependent launch
+// off/on for the column pass and for the row pass, x the row pass's butterfly
+// chunk bits (the default and up to two below it) -- on a copy of the
+// context's own state, restore the state, and keep the fastest.  Decisions are
+// cached per (device, rows, cols, batch) for the process, and can be saved to
+// and loaded from a JSON file (cdx_tuning_save / cdx_tuning_load), where they
+// are keyed by the device's name so that they carry over to the same model.
+struct TuneRec {
+  int pdl_col = 0, pdl_row = 0, cb_plus1 = 0;
+  double us = 0.0;
+};
 std::mutex g_tune_mu;
-std::map<std::tuple<int, int, int, int>, std::pair<int, int>> g_tune;
+std::map<std::tuple<int, int, int, int>, TuneRec> g_tune;                   // (device, rows, cols, batch)
+std::map<std::tuple<std::string, int, int, int>, TuneRec> g_tune_named;    // (device name, rows, cols, batch)
+
+std::string device_name(int dev) {
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return std::string();
+  }
+  return std::string(prop.name);
+}
 
 int autotune(cdx_ctx* c) {
   const auto key = std::make_tuple(c->device, c->rows, c->cols, c->batch);
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune.find(key);
+    const char* how = "cached";
+    if (it == g_tune.end()) {
+      auto nt = g_tune_named.find(std::make_tuple(device_name(c->device), c->rows, c->cols, c->batch));
+      if (nt != g_tune_named.end()) {
+        it = g_tune.emplace(key, nt->second).first;
+        how = "loaded";
+      }
+    }
     if (it != g_tune.end()) {
-      c->tune_pdl_mode = it->second.first;
-      c->tune_cb_plus1 = it->second.second;
+      c->tune_pdl_col = it->second.pdl_col;
+      c->tune_pdl_row = it->second.pdl_row;
+      c->tune_cb_plus1 = it->second.cb_plus1;
       c->tuned = true;
-      c->tune_report = "cached";
+      c->tune_report = how;
       return CDX_OK;
     }
   }
@@ -515,46 +541,53 @@ int autotune(cdx_ctx* c) {
   CDX_CK(cudaMemcpyAsync(srho, c->rho, sizeof(float2) * nrho, cudaMemcpyDeviceToDevice, c->st));
   CDX_CK(cudaMemcpyAsync(sw, c->work, sizeof(float2) * nw, cudaMemcpyDeviceToDevice, c->st));
   const int cbd = row_cb_default(c->cols, c->tl);
-  int best_pdl = 0, best_cb = 0;
-  double best = 1e30;
+  TuneRec best;
+  best.us = 1e30;
   std::string rep;
   int e = CDX_OK;
-  for (int pdl = 1; pdl <= 2 && e == CDX_OK; ++pdl)
-    for (int cb = cbd; cb >= std::max(0, cbd - 2) && e == CDX_OK; --cb) {
-      c->tune_pdl_mode = pdl;
-      c->tune_cb_plus1 = cb + 1;
-      // timed as the runs execute: kTimed iterations captured in one graph,
-      // launched once to warm up and once under the events
-      constexpr int kTimed = 8;
-      cudaGraph_t g = nullptr;
-      cudaGraphExec_t ge = nullptr;
-      CDX_CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
-      for (int i = 0; i < kTimed && e == CDX_OK; ++i) {
-        e = col_iter(c, false, false);
-        if (e == CDX_OK) e = row_iter(c, ALGO_HIO);
+  for (int pc = 1; pc <= 2 && e == CDX_OK; ++pc)
+    for (int pr = 1; pr <= 2 && e == CDX_OK; ++pr)
+      for (int cb = cbd; cb >= std::max(0, cbd - 2) && e == CDX_OK; --cb) {
+        c->tune_pdl_col = pc;
+        c->tune_pdl_row = pr;
+        c->tune_cb_plus1 = cb + 1;
+        // timed as the runs execute: kTimed iterations captured in one graph,
+        // launched once to warm up and once under the events
+        constexpr int kTimed = 8;
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t ge = nullptr;
+        CDX_CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+        for (int i = 0; i < kTimed && e == CDX_OK; ++i) {
+          e = col_iter(c, false, false);
+          if (e == CDX_OK) e = row_iter(c, ALGO_HIO);
+        }
+        const cudaError_t ce = cudaStreamEndCapture(c->st, &g);
+        if (e == CDX_OK && ce != cudaSuccess) e = set_error(CDX_ERR_CUDA, std::string("autotune capture: ") + cudaGetErrorString(ce));
+        if (e == CDX_OK && cudaGraphInstantiate(&ge, g, 0) != cudaSuccess) e = set_error(CDX_ERR_CUDA, "autotune graph");
+        if (g) cudaGraphDestroy(g);
+        float ms = 0.f;
+        if (e == CDX_OK) {
+          cudaError_t le = cudaGraphLaunch(ge, c->st);
+          if (le == cudaSuccess) le = cudaEventRecord(c->ev0, c->st);
+          if (le == cudaSuccess) le = cudaGraphLaunch(ge, c->st);
+          if (le == cudaSuccess) le = cudaEventRecord(c->ev1, c->st);
+          if (le == cudaSuccess) le = cudaEventSynchronize(c->ev1);
+          if (le == cudaSuccess) le = cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+          if (le != cudaSuccess) e = set_error(CDX_ERR_CUDA, std::string("autotune: ") + cudaGetErrorString(le));
+        }
+        if (ge) cudaGraphExecDestroy(ge);
+        if (e != CDX_OK) break;
+        const double us = 1000.0 * ms / kTimed;
+        char line[128];
+        snprintf(line, sizeof line, "pdl_col=%d pdl_row=%d chunk=%d: %.2f us\n", pc - 1, pr - 1, cb, us);
+        rep += line;
+        if (us < best.us) {
+          best.us = us;
+          best.pdl_col = pc;
+          best.pdl_row = pr;
+          best.cb_plus1 = cb + 1;
+        }
       }
-      const cudaError_t ce = cudaStreamEndCapture(c->st, &g);
-      if (e == CDX_OK && ce != cudaSuccess) e = set_error(CDX_ERR_CUDA, std::string("autotune capture: ") + cudaGetErrorString(ce));
-      if (e == CDX_OK && cudaGraphInstantiate(&ge, g, 0) != cudaSuccess) e = set_error(CDX_ERR_CUDA, "autotune graph");
-      if (g) cudaGraphDestroy(g);
-      float ms = 0.f;
-      if (e == CDX_OK) {
-        cudaError_t le = cudaGraphLaunch(ge, c->st);
-        if (le == cudaSuccess) le = cudaEventRecord(c->ev0, c->st);
-        if (le == cudaSuccess) le = cudaGraphLaunch(ge, c->st);
-        if (le == cudaSuccess) le = cudaEventRecord(c->ev1, c->st);
-        if (le == cudaSuccess) le = cudaEventSynchronize(c->ev1);
-        if (le == cudaSuccess) le = cudaEventElapsedTime(&ms, c->ev0, c->ev1);
-        if (le != cudaSuccess) e = set_error(CDX_ERR_CUDA, std::string("autotune: ") + cudaGetErrorString(le));
-      }
-      if (ge) cudaGraphExecDestroy(ge);
-      if (e != CDX_OK) break;
-      const double us = 1000.0 * ms / kTimed;
-      char line[96];
-      snprintf(line, sizeof line, "pdl=%d chunk=%d: %.2f us\n", pdl - 1, cb, us);
-      rep += line;
-      if (us < best) { best = us; best_pdl = pdl; best_cb = cb + 1; }
-    }
   // restore the state the runs iterated on
   if (e == CDX_OK) {
     CDX_CK(cudaMemcpyAsync(c->rho, srho, sizeof(float2) * nrho, cudaMemcpyDeviceToDevice, c->st));
@@ -562,12 +595,111 @@ int autotune(cdx_ctx* c) {
     CDX_CK(cudaStreamSynchronize(c->st));
   }
   if (e != CDX_OK) return e;
-  c->tune_pdl_mode = best_pdl;
-  c->tune_cb_plus1 = best_cb;
+  c->tune_pdl_col = best.pdl_col;
+  c->tune_pdl_row = best.pdl_row;
+  c->tune_cb_plus1 = best.cb_plus1;
   c->tuned = true;
   c->tune_report = rep;
+  const std::string name = device_name(c->device);
   std::lock_guard<std::mutex> lk(g_tune_mu);
-  g_tune[key] = {best_pdl, best_cb};
+  g_tune[key] = best;
+  if (!name.empty()) g_tune_named[std::make_tuple(name, c->rows, c->cols, c->batch)] = best;
+  return CDX_OK;
+}
+
+// ---------------------------------------------------------- tuning file (JSON)
+// {"cdx_tuning": 1, "entries": [{"device": "<name>", "rows": R, "cols": C,
+//   "batch": B, "pdl_col": 0|1, "pdl_row": 0|1, "row_chunk_bits": k, "us": t}, ...]}
+// A small reader for exactly this shape: flat objects of string and number
+// values inside the "entries" array; anything else is an error.
+struct JsonLex {
+  const std::string& t;
+  size_t i = 0;
+  explicit JsonLex(const std::string& s) : t(s) {}
+  void ws() {
+    while (i < t.size() && (t[i] == ' ' || t[i] == '\n' || t[i] == '\r' || t[i] == '\t')) ++i;
+  }
+  bool eat(char ch) {
+    ws();
+    if (i < t.size() && t[i] == ch) {
+      ++i;
+      return true;
+    }
+    return false;
+  }
+  bool str(std::string& out) {
+    ws();
+    if (i >= t.size() || t[i] != '"') return false;
+    out.clear();
+    for (++i; i < t.size() && t[i] != '"'; ++i) {
+      if (t[i] == '\\' && i + 1 < t.size()) ++i;
+      out.push_back(t[i]);
+    }
+    if (i >= t.size()) return false;
+    ++i;
+    return true;
+  }
+  bool num(double& v) {
+    ws();
+    const char* b = t.c_str() + i;
+    char* e = nullptr;
+    v = std::strtod(b, &e);
+    if (e == b) return false;
+    i += (size_t)(e - b);
+    return true;
+  }
+};
+
+int parse_tuning(const std::string& text, std::vector<std::pair<std::string, std::pair<std::tuple<int, int, int>, TuneRec>>>& out) {
+  JsonLex L(text);
+  std::string k;
+  double v = 0;
+  if (!L.eat('{')) return set_error(CDX_ERR_IO, "tuning file: expected '{'");
+  bool entries = false;
+  do {
+    if (!L.str(k) || !L.eat(':')) return set_error(CDX_ERR_IO, "tuning file: expected a key");
+    if (k == "entries") {
+      if (!L.eat('[')) return set_error(CDX_ERR_IO, "tuning file: entries must be an array");
+      entries = true;
+      if (L.eat(']')) continue;
+      do {
+        if (!L.eat('{')) return set_error(CDX_ERR_IO, "tuning file: expected an entry object");
+        std::string dev;
+        int rows = 0, cols = 0, batch = 0, pc = -1, pr = -1, cb = -1;
+        double us = 0;
+        do {
+          if (!L.str(k) || !L.eat(':')) return set_error(CDX_ERR_IO, "tuning file: expected an entry key");
+          if (k == "device") {
+            if (!L.str(dev)) return set_error(CDX_ERR_IO, "tuning file: device must be a string");
+          } else {
+            if (!L.num(v)) return set_error(CDX_ERR_IO, "tuning file: expected a number for " + k);
+            if (k == "rows") rows = (int)v;
+            else if (k == "cols") cols = (int)v;
+            else if (k == "batch") batch = (int)v;
+            else if (k == "pdl_col") pc = (int)v;
+            else if (k == "pdl_row") pr = (int)v;
+            else if (k == "row_chunk_bits") cb = (int)v;
+            else if (k == "us") us = v;
+          }
+        } while (L.eat(','));
+        if (!L.eat('}')) return set_error(CDX_ERR_IO, "tuning file: expected '}'");
+        if (dev.empty() || !cdx_size_supported(rows) || !cdx_size_supported(cols) || batch < 1 || pc < 0 ||
+            pc > 1 || pr < 0 || pr > 1 || cb < 0 || cb > row_cb_max(cols))
+          return set_error(CDX_ERR_IO, "tuning file: entry out of range");
+        TuneRec r;
+        r.pdl_col = pc + 1;
+        r.pdl_row = pr + 1;
+        r.cb_plus1 = cb + 1;
+        r.us = us;
+        out.push_back({dev, {std::make_tuple(rows, cols, batch), r}});
+      } while (L.eat(','));
+      if (!L.eat(']')) return set_error(CDX_ERR_IO, "tuning file: expected ']'");
+    } else if (!L.num(v)) {
+      std::string skip;
+      if (!L.str(skip)) return set_error(CDX_ERR_IO, "tuning file: unexpected value for " + k);
+    }
+  } while (L.eat(','));
+  if (!L.eat('}') || !entries) return set_error(CDX_ERR_IO, "tuning file: expected an \"entries\" array");
   return CDX_OK;
 }
 
@@ -887,12 +1019,70 @@ int cdx_get_prtf(cdx_ctx* c, int idx, float* out, int where) {
 
 int cdx_get_tuning(cdx_ctx* c, int* pdl, int* row_chunk, char* report, int cap) {
   if (!c) return set_error(CDX_ERR_ARG, "null context");
-  if (pdl) *pdl = c->tune_pdl_mode == 0 ? -1 : c->tune_pdl_mode - 1;
+  if (pdl)
+    *pdl = (c->tune_pdl_col == 0 && c->tune_pdl_row == 0)
+               ? -1
+               : (c->tune_pdl_col == 2 ? 1 : 0) | (c->tune_pdl_row == 2 ? 2 : 0);
   if (row_chunk) *row_chunk = c->tune_cb_plus1 - 1;
   if (report && cap > 0) {
     std::strncpy(report, c->tune_report.c_str(), (size_t)cap - 1);
     report[cap - 1] = 0;
   }
+  return CDX_OK;
+}
+
+int cdx_tuning_save(const char* path) {
+  if (!path) return set_error(CDX_ERR_ARG, "null path");
+  std::string out = "{\"cdx_tuning\": 1, \"entries\": [";
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    bool first = true;
+    for (const auto& kv : g_tune_named) {
+      const TuneRec& r = kv.second;
+      char line[512];
+      snprintf(line, sizeof line,
+               "%s\n  {\"device\": \"%s\", \"rows\": %d, \"cols\": %d, \"batch\": %d, \"pdl_col\": %d, "
+               "\"pdl_row\": %d, \"row_chunk_bits\": %d, \"us\": %.3f}",
+               first ? "" : ",", std::get<0>(kv.first).c_str(), std::get<1>(kv.first), std::get<2>(kv.first),
+               std::get<3>(kv.first), r.pdl_col - 1, r.pdl_row - 1, r.cb_plus1 - 1, r.us);
+      out += line;
+      first = false;
+    }
+  }
+  out += "\n]}\n";
+  FILE* f = std::fopen(path, "w");
+  if (!f) return set_error(CDX_ERR_IO, std::string("cannot write ") + path);
+  const bool ok = std::fwrite(out.data(), 1, out.size(), f) == out.size();
+  std::fclose(f);
+  return ok ? CDX_OK : set_error(CDX_ERR_IO, std::string("short write to ") + path);
+}
+
+int cdx_tuning_load(const char* path, int* count) {
+  if (!path) return set_error(CDX_ERR_ARG, "null path");
+  FILE* f = std::fopen(path, "r");
+  if (!f) return set_error(CDX_ERR_IO, std::string("cannot read ") + path);
+  std::string text;
+  char buf[4096];
+  size_t n;
+  while ((n = std::fread(buf, 1, sizeof buf, f)) > 0) text.append(buf, n);
+  std::fclose(f);
+  std::vector<std::pair<std::string, std::pair<std::tuple<int, int, int>, TuneRec>>> entries;
+  int e = parse_tuning(text, entries);
+  if (e) return e;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  for (const auto& en : entries) {
+    const auto& k = en.second.first;
+    g_tune_named[std::make_tuple(en.first, std::get<0>(k), std::get<1>(k), std::get<2>(k))] = en.second.second;
+    // a decision already made in this process for the same size on a device of that name gives way
+    for (auto it = g_tune.begin(); it != g_tune.end();) {
+      if (std::get<1>(it->first) == std::get<0>(k) && std::get<2>(it->first) == std::get<1>(k) &&
+          std::get<3>(it->first) == std::get<2>(k) && device_name(std::get<0>(it->first)) == en.first)
+        it = g_tune.erase(it);
+      else
+        ++it;
+    }
+  }
+  if (count) *count = (int)entries.size();
   return CDX_OK;
 }
 

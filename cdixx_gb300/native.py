@@ -82,6 +82,8 @@ _SIGS = {
     "cdx_get_support": [_P, _I, _P, _I],
     "cdx_get_prtf": [_P, _I, _P, _I],
     "cdx_get_tuning": [_P, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.c_char_p, _I],
+    "cdx_tuning_save": [ctypes.c_char_p],
+    "cdx_tuning_load": [ctypes.c_char_p, ctypes.POINTER(_I)],
     "cdx_phase_retrieve_host": [ctypes.POINTER(Params), ctypes.c_char_p, _P, _P, ctypes.c_ulonglong,
                                 _P, _P, _P, ctypes.POINTER(Stats)],
     "cdx_release_host_cache": [],
@@ -246,7 +248,8 @@ class Context:
         self.close()
 
     def tuning(self):
-        """(pdl, row_chunk, report) of the launch variant in use (cdx_get_tuning)."""
+        """(pdl bits, row_chunk, report) of the launch variant in use (cdx_get_tuning): pdl bit 0 =
+        the column pass is a programmatic dependent launch, bit 1 = the row pass, -1 = defaults."""
         pdl, chunk = ctypes.c_int(), ctypes.c_int()
         buf = ctypes.create_string_buffer(1024)
         check(lib().cdx_get_tuning(self._h, ctypes.byref(pdl), ctypes.byref(chunk), buf, 1024))
@@ -363,6 +366,19 @@ def phase_retrieve_host(params: Params, algorithm: str, intensity, psi0=None, se
                                         None if p0 is None else vp(p0), seed, vp(rho), vp(psi), vp(spt),
                                         ctypes.byref(s)))
     return rho, psi, spt, s.as_dict()
+
+
+def tuning_save(path):
+    """Write the autotuner's decisions of this process to a JSON file (cdx_tuning_save)."""
+    check(lib().cdx_tuning_save(str(path).encode()))
+
+
+def tuning_load(path) -> int:
+    """Read autotuner decisions from a JSON file written by tuning_save (cdx_tuning_load);
+    returns the number of entries."""
+    n = ctypes.c_int()
+    check(lib().cdx_tuning_load(str(path).encode(), ctypes.byref(n)))
+    return n.value
 
 
 def release_host_cache():

@@ -172,11 +172,20 @@ int cdx_get_support(cdx_ctx* ctx, int idx, float* out, int where);  /* support (
  * divided by the angular sum of the |P_M Psi| > 1e-6 mask at prtf_iter (the
  * prtf.txt column).  CDX_ERR_STATE when the run did not reach prtf_iter. */
 int cdx_get_prtf(cdx_ctx* ctx, int idx, float* out, int where);
-/* The launch variant the iteration uses (autotune): *pdl 1 = programmatic
- * dependent launch, 0 = plain; *row_chunk = butterfly chunk bits of the row
- * pass (-1: the default); `report` (may be NULL) receives the timings the
- * autotuner measured, one "pdl=<0|1> chunk=<k>: <us> us" line per variant. */
+/* The launch variant the iteration uses (autotune): *pdl bit 0 = the column
+ * pass is a programmatic dependent launch, bit 1 = the row pass (-1: the
+ * per-length defaults); *row_chunk = butterfly chunk bits of the row pass
+ * (-1: the default); `report` (may be NULL) receives the timings the
+ * autotuner measured, one "pdl_col=<0|1> pdl_row=<0|1> chunk=<k>: <us> us"
+ * line per variant ("cached" / "loaded" when the decision was reused). */
 int cdx_get_tuning(cdx_ctx* ctx, int* pdl, int* row_chunk, char* report, int cap);
+/* The autotuner's decisions as a JSON file, keyed by device name, rows, cols
+ * and batch: save writes every decision of this process (and every loaded
+ * one); load reads a file written by save (*count = its entries, may be NULL),
+ * and contexts created afterwards on a device of that name take those
+ * decisions instead of timing the variants. */
+int cdx_tuning_save(const char* path);
+int cdx_tuning_load(const char* path, int* count);
 
 /* ---------------------------------------------------------------- one call, host buffers */
 /* Whole path for one pattern with HOST buffers: create, set pattern, set

@@ -97,3 +97,33 @@ def test_default_params(cdx):
     p = cdx.default_params(256, 256)
     assert p.beta == 1.0 and p.rcolor == 65535 and p.sigma0 == 3.0 and p.sigma_min == 2.0
     assert abs(p.sigma_decay - 0.99) < 1e-7 and p.batch == 1 and p.use_graph == 1
+
+
+def test_tuning_file_round_trip(cdx, tmp_path):
+    """The autotuner's JSON file: a file in the documented shape loads, and
+    saving writes its entries back; malformed or out-of-range entries are
+    refused.  Host-only (no kernel runs)."""
+    good = tmp_path / "tune.json"
+    good.write_text('{"cdx_tuning": 1, "entries": [\n'
+                    '  {"device": "Some GPU", "rows": 256, "cols": 256, "batch": 64, "pdl_col": 1, "pdl_row": 0,'
+                    ' "row_chunk_bits": 3, "us": 45.5},\n'
+                    '  {"device": "Some GPU", "rows": 192, "cols": 384, "batch": 2, "pdl_col": 0, "pdl_row": 1,'
+                    ' "row_chunk_bits": 2, "us": 30.25}]}\n')
+    assert cdx.tuning_load(good) == 2
+    out = tmp_path / "saved.json"
+    cdx.tuning_save(out)
+    text = out.read_text()
+    for frag in ['"device": "Some GPU", "rows": 256, "cols": 256, "batch": 64, "pdl_col": 1, "pdl_row": 0, '
+                 '"row_chunk_bits": 3', '"rows": 192, "cols": 384, "batch": 2, "pdl_col": 0, "pdl_row": 1, '
+                 '"row_chunk_bits": 2']:
+        assert frag in text
+    assert cdx.tuning_load(out) == 2
+    bad = tmp_path / "bad.json"
+    for body in ['{"entries": [{"device": "X", "rows": 256, "cols": 256, "batch": 1, "pdl_col": 0, "pdl_row": 0,'
+                 ' "row_chunk_bits": 9}]}',                     # 9 > the chunk bits 256 allows
+                 '{"entries": [{"device": "X", "rows": 250, "cols": 256, "batch": 1, "pdl_col": 0, "pdl_row": 0,'
+                 ' "row_chunk_bits": 1}]}',                     # unsupported length
+                 '{"entries": [ {"device": "X", "rows": 256 ', '[]']:
+        bad.write_text(body)
+        with pytest.raises(cdx.CdxError):
+            cdx.tuning_load(bad)

@@ -608,3 +608,34 @@ def test_autotune_keeps_results_and_caches(cdx, n, batch):
     assert pdl in (0, 1) and chunk >= 0 and report.count("us") >= 2
     assert outs[2][1][2] == "cached" and outs[2][1][:2] == (pdl, chunk)
     assert outs[0][1][:2] == (-1, -1)
+
+
+def test_autotuner_decisions_save_and_load(cdx, tmp_path):
+    """A context tunes its launch variant; the decision saved to JSON and
+    loaded again (edited) is what a new context of the same size takes."""
+    import json
+    I, psi0 = blob_case(n=256)
+    p = cdx.default_params(256, 256, batch=3, oversampling_spt=4.0, autotune=1)
+    with cdx.Context(p) as ctx:
+        for i in range(3):
+            ctx.set_pattern(i, I)
+            ctx.set_initial(i, psi0)
+        ctx.run("3*HIO")
+        pdl, chunk, rep = ctx.tuning()
+    assert "pdl_col=" in rep or rep in ("cached", "loaded")
+    path = tmp_path / "tune.json"
+    cdx.tuning_save(path)
+    d = json.loads(path.read_text())
+    mine = [e for e in d["entries"] if (e["rows"], e["cols"], e["batch"]) == (256, 256, 3)]
+    assert len(mine) == 1 and mine[0]["row_chunk_bits"] == chunk
+    mine[0]["row_chunk_bits"] = 1 if chunk != 1 else 2
+    mine[0]["pdl_col"], mine[0]["pdl_row"] = 1, 0
+    path.write_text(json.dumps(d))
+    assert cdx.tuning_load(path) >= 1
+    with cdx.Context(p) as ctx:
+        for i in range(3):
+            ctx.set_pattern(i, I)
+            ctx.set_initial(i, psi0)
+        ctx.run("3*HIO")
+        pdl2, chunk2, rep2 = ctx.tuning()
+    assert rep2 == "loaded" and chunk2 == mine[0]["row_chunk_bits"] and pdl2 == 1
