@@ -605,7 +605,7 @@ def test_autotune_keeps_results_and_caches(cdx, n, batch):
     assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][0], outs[2][0])
     pdl, chunk, report = outs[1][1]
     print(f"{n}^2 x{batch}: pdl={pdl} chunk={chunk}\n{report}")
-    assert pdl in (0, 1) and chunk >= 0 and report.count("us") >= 2
+    assert pdl in (0, 1, 2, 3) and chunk >= 0 and report.count("us") >= 2   # pdl: bit 0 column, bit 1 row pass
     assert outs[2][1][2] == "cached" and outs[2][1][:2] == (pdl, chunk)
     assert outs[0][1][:2] == (-1, -1)
 
