@@ -195,7 +195,8 @@ int cdx_tuning_load(const char* path, int* count);
  * parameters on the same device, returned to the state of a new context
  * before reuse (the reference keeps its memory pool and cuFFT plan for the
  * whole process, memManager.cc, cudaConfig.cu:137-159); concurrent calls
- * each get their own.  cdx_release_host_cache frees the kept context. */
+ * each get their own.  cdx_release_host_cache frees the kept context; call it
+ * before cudaDeviceReset, which would leave the kept context's memory invalid. */
 int cdx_phase_retrieve_host(const cdx_params* p, const char* algorithm, const float* intensity,
                             const float* psi0, unsigned long long seed, float* rho_out, float* psi_out,
                             float* support_out, cdx_stats* stats);
