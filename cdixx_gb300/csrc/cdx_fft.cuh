@@ -42,11 +42,49 @@ CDX_HD float2 rot90(float2 a) {
 }
 
 // ---------------------------------------------------------------- small DFTs
+// The butterflies issue Blackwell's paired FP32 instructions (FADD2 / FFMA2,
+// the __fadd2_rn / __ffma2_rn intrinsics of sm_100 and later): one instruction
+// adds or fuses both components of a complex value, rounded exactly as two
+// scalar operations would be, so the results are those of the scalar forms.
+// Only lane-uniform operations pair up; a product with +-i swaps and negates one
+// component, so those sums (add_rot / sub_rot) stay scalar.
+CDX_HD float2 padd(float2 a, float2 b) {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+  return __fadd2_rn(a, b);
+#else
+  return make_float2(a.x + b.x, a.y + b.y);
+#endif
+}
+CDX_HD float2 psub(float2 a, float2 b) {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+  return __fadd2_rn(a, make_float2(-b.x, -b.y));
+#else
+  return make_float2(a.x - b.x, a.y - b.y);
+#endif
+}
+// a * b + c per component, one rounding
+CDX_HD float2 pfma(float2 a, float2 b, float2 c) {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+  return __ffma2_rn(a, b, c);
+#else
+  return make_float2(fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y));
+#endif
+}
+// b + rot90(d) and b - rot90(d), rot90 the product with -i (forward) or +i (inverse)
+template <bool INV>
+CDX_HD float2 add_rot(float2 b, float2 d) {
+  return INV ? make_float2(b.x - d.y, b.y + d.x) : make_float2(b.x + d.y, b.y - d.x);
+}
+template <bool INV>
+CDX_HD float2 sub_rot(float2 b, float2 d) {
+  return INV ? make_float2(b.x + d.y, b.y - d.x) : make_float2(b.x - d.y, b.y + d.x);
+}
+
 template <bool INV>
 CDX_HD void dft2(float2& a, float2& b) {
   float2 t = a;
-  a = cadd(t, b);
-  b = csub(t, b);
+  a = padd(t, b);
+  b = psub(t, b);
 }
 
 template <bool INV>
@@ -63,12 +101,12 @@ CDX_HD void dft3(float2* v) {
 
 template <bool INV>
 CDX_HD void dft4(float2& x0, float2& x1, float2& x2, float2& x3) {
-  float2 a = cadd(x0, x2), b = csub(x0, x2);
-  float2 c = cadd(x1, x3), d = rot90<INV>(csub(x1, x3));
-  x0 = cadd(a, c);
-  x2 = csub(a, c);
-  x1 = cadd(b, d);
-  x3 = csub(b, d);
+  float2 a = padd(x0, x2), b = psub(x0, x2);
+  float2 c = padd(x1, x3), d = psub(x1, x3);
+  x0 = padd(a, c);
+  x2 = psub(a, c);
+  x1 = add_rot<INV>(b, d);
+  x3 = sub_rot<INV>(b, d);
 }
 
 template <bool INV>
@@ -79,16 +117,14 @@ CDX_HD void dft8(float2* v) {
   float2 o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
   dft4<INV>(e0, e1, e2, e3);
   dft4<INV>(o0, o1, o2, o3);
-  // W8^k, k = 1..3 (forward: exp(-i pi k/4))
-  float2 w1 = INV ? make_float2(h * (o1.x - o1.y), h * (o1.x + o1.y))
-                  : make_float2(h * (o1.x + o1.y), h * (o1.y - o1.x));
-  float2 w2 = rot90<INV>(o2);
-  float2 w3 = INV ? make_float2(-h * (o3.x + o3.y), h * (o3.x - o3.y))
-                  : make_float2(h * (o3.y - o3.x), -h * (o3.x + o3.y));
-  v[0] = cadd(e0, o0); v[4] = csub(e0, o0);
-  v[1] = cadd(e1, w1); v[5] = csub(e1, w1);
-  v[2] = cadd(e2, w2); v[6] = csub(e2, w2);
-  v[3] = cadd(e3, w3); v[7] = csub(e3, w3);
+  // W8^k o_k, k = 1..3 (forward: exp(-i pi k/4)): W8^1 o1 = h s1, W8^2 o2 = rot90(o2), W8^3 o3 = h s3
+  const float2 s1 = INV ? make_float2(o1.x - o1.y, o1.x + o1.y) : make_float2(o1.x + o1.y, o1.y - o1.x);
+  const float2 s3 = INV ? make_float2(-(o3.x + o3.y), o3.x - o3.y) : make_float2(o3.y - o3.x, -(o3.x + o3.y));
+  const float2 hh = make_float2(h, h), mh = make_float2(-h, -h);
+  v[0] = padd(e0, o0); v[4] = psub(e0, o0);
+  v[1] = pfma(hh, s1, e1); v[5] = pfma(mh, s1, e1);
+  v[2] = add_rot<INV>(e2, o2); v[6] = sub_rot<INV>(e2, o2);
+  v[3] = pfma(hh, s3, e3); v[7] = pfma(mh, s3, e3);
 }
 
 template <bool INV>

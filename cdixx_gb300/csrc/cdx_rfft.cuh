@@ -400,7 +400,18 @@ __global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_COL) col_pass_rk(Co
 // ------------------------------------------------------------------- row pass
 // Lines are rows (length N = cols).  Column-tiled arrays have tile width
 // 2^tile_log2 (the column pass's L for the row count).
-template <int N, int MODE, int ALGO>
+// SQ (ROW_ITER only): W is column-tiled on both sides with the tile width of a
+// column pass of length N (square patterns) and the butterflies use the default
+// chunk, so the layout is known at compile time: each butterfly's 16 elements
+// are one base address plus whole-tile strides, with no per-element index
+// arithmetic.  The launcher takes the general kernel otherwise.
+// The compile-time layout needs every pass's element stride to be whole tiles:
+// 2^log2(L) divides N/R for each radix R (true from 256 up; at 16..192 the
+// column tiles are wider than that).
+template <int N>
+__host__ __device__ constexpr bool row_sq_ok() { return Geom<N>::LOG2L <= rfft_cb_max<N>(); }
+
+template <int N, int MODE, int ALGO, bool SQ = false>
 __device__ __forceinline__ void row_pass_body(const RowArgs& a) {
   using G = Geom<N>;
   constexpr int L = G::L, T = G::T;
@@ -414,12 +425,16 @@ __device__ __forceinline__ void row_pass_body(const RowArgs& a) {
   const int row0 = blockIdx.x * L;
   const int nrows = min(L, a.rows - row0);
   constexpr bool iter = MODE == ROW_ITER;
-  const int tl = a.tile_log2;
+  constexpr bool CT = SQ && iter && row_sq_ok<N>();   // compile-time layout
+  constexpr int TLC = G::LOG2L;
+  constexpr int CBC = TLC < rfft_cb_max<N>() ? TLC : rfft_cb_max<N>();
+  const int tl = CT ? TLC : a.tile_log2;
   // tiled: four (or 2^tl) threads per tile row piece; row-major: consecutive
   // threads take consecutive columns
   const bool tiled = a.in_tiled || a.out_tiled;
-  const int cb = a.cb_plus1 > 0 ? min(a.cb_plus1 - 1, rfft_cb_max<N>())
-                                : (tiled ? min(tl, rfft_cb_max<N>()) : rfft_cb_max<N>());
+  const int cb = CT ? CBC
+                    : (a.cb_plus1 > 0 ? min(a.cb_plus1 - 1, rfft_cb_max<N>())
+                                      : (tiled ? min(tl, rfft_cb_max<N>()) : rfft_cb_max<N>()));
 
   // rho rows and support words of the CTA (ROW_ITER), landing during the inverse FFT
   // (RHO_IN_BUF: the rho rows land in the line buffer during its last pass)
@@ -486,9 +501,18 @@ __device__ __forceinline__ void row_pass_body(const RowArgs& a) {
     for (int b = 0; b < F0::B; ++b) {
       int l, j;
       if (!bfly_of<N, F0::R>(b, cb, l, j)) continue;
+      if constexpr (CT) {
+        // element j + r*NR: tile (j >> TLC) + r*(NR >> TLC), lane j & (2^TLC - 1)
+        static_assert(F0::NR % (1 << TLC) == 0, "first-pass stride is whole tiles");
+        const float2* p = in + ((((long long)(j >> TLC)) * R + row0 + l) << TLC) + (j & ((1 << TLC) - 1));
+        const long long st = ((long long)(F0::NR >> TLC) * R) << TLC;
 #pragma unroll
-      for (int r = 0; r < F0::R; ++r)
-        v0[b][r] = l < nrows ? __ldcg(in + goff(a.in_tiled, l, j + r * F0::NR)) : make_float2(0.f, 0.f);
+        for (int r = 0; r < F0::R; ++r) v0[b][r] = l < nrows ? __ldcg(p + r * st) : make_float2(0.f, 0.f);
+      } else {
+#pragma unroll
+        for (int r = 0; r < F0::R; ++r)
+          v0[b][r] = l < nrows ? __ldcg(in + goff(a.in_tiled, l, j + r * F0::NR)) : make_float2(0.f, 0.f);
+      }
     }
     if constexpr (iter && rho_in_buf) {
       rfft<N, 0, true>(v0, v, buf, tw, cb, [&]() {
@@ -550,11 +574,19 @@ __device__ __forceinline__ void row_pass_body(const RowArgs& a) {
       int l, j;
       if (!bfly_of<N, IL::R>(b, cb, l, j)) continue;
       if (l >= nrows) continue;
+      if constexpr (CT) {
+        static_assert(IL::NS % (1 << TLC) == 0, "last-pass stride is whole tiles");
+        float2* p = out + ((((long long)(j >> TLC)) * R + row0 + l) << TLC) + (j & ((1 << TLC) - 1));
+        const long long st = ((long long)(IL::NS >> TLC) * R) << TLC;
 #pragma unroll
-      for (int r = 0; r < IL::R; ++r) {
-        float2 y = o[b][r];
-        if (s != 1.f) { y.x *= s; y.y *= s; }
-        __stcg(out + goff(a.out_tiled, l, j + r * IL::NS), y);
+        for (int r = 0; r < IL::R; ++r) __stcg(p + r * st, o[b][r]);   // the iteration stores unscaled
+      } else {
+#pragma unroll
+        for (int r = 0; r < IL::R; ++r) {
+          float2 y = o[b][r];
+          if (s != 1.f) { y.x *= s; y.y *= s; }
+          __stcg(out + goff(a.out_tiled, l, j + r * IL::NS), y);
+        }
       }
     }
   }
@@ -562,11 +594,18 @@ __device__ __forceinline__ void row_pass_body(const RowArgs& a) {
 
 // One kernel per update (ALGO is ignored in ROW_FFT mode): the executed code
 // holds a single update and no switch.
-template <int N, int MODE, int ALGO>
+template <int N, int MODE, int ALGO, bool SQ = false>
 __global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_ROW) row_pass_rk(RowArgs a) {
   pdl_wait_and_release();
   if (a.state && (a.state[blockIdx.y].flags & 4)) return;   // frozen pattern
-  row_pass_body<N, MODE, ALGO>(a);
+  row_pass_body<N, MODE, ALGO, SQ>(a);
+}
+// the compile-time layout of row_pass_rk<..., true> applies to these arguments
+template <int N>
+__host__ __forceinline__ bool row_sq_layout(const RowArgs& a) {
+  constexpr int cbd = Geom<N>::LOG2L < rfft_cb_max<N>() ? Geom<N>::LOG2L : rfft_cb_max<N>();
+  return row_sq_ok<N>() && a.mode == ROW_ITER && a.in_tiled && a.out_tiled && a.tile_log2 == Geom<N>::LOG2L && a.scale == 1.f &&
+         (a.cb_plus1 == 0 || a.cb_plus1 - 1 == cbd);
 }
 
 }  // namespace cdx

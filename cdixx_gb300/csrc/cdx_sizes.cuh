@@ -48,6 +48,16 @@ cudaError_t prepare_rk() {
     if ((e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, RGeom<N>::SMEM_ROW_ITER)) !=
         cudaSuccess)
       return e;
+  if constexpr (row_sq_ok<N>()) {
+    const void* sq_kernels[] = {
+        (const void*)row_pass_rk<N, ROW_ITER, ALGO_HIO, true>, (const void*)row_pass_rk<N, ROW_ITER, ALGO_RAAR, true>,
+        (const void*)row_pass_rk<N, ROW_ITER, ALGO_ER, true>, (const void*)row_pass_rk<N, ROW_ITER, ALGO_POSER, true>,
+        (const void*)row_pass_rk<N, ROW_ITER, ALGO_POSHIO, true>, (const void*)row_pass_rk<N, ROW_ITER, ALGO_FHIO, true>};
+    for (const void* k : sq_kernels)
+      if ((e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, RGeom<N>::SMEM_ROW_ITER)) !=
+          cudaSuccess)
+        return e;
+  }
   if ((e = cudaFuncSetAttribute(col_pass_rk<N, COL_FFT, PROJ_MODABS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 G::SMEM_LINES)) != cudaSuccess)
     return e;
@@ -89,6 +99,14 @@ cudaError_t launch_row(const RowArgs& a, int batch, cudaStream_t st) {
   } else {
     constexpr int SM = RGeom<N>::SMEM_ROW_ITER;
     if (a.mode != ROW_ITER) return launch_pdl(row_pass_rk<N, ROW_FFT, ALGO_ER>, grid, G::T, G::SMEM_LINES, st, a, pdl_of<N>(a.pdl_mode));
+    if constexpr (row_sq_ok<N>()) if (row_sq_layout<N>(a)) switch (a.algo) {   // the compile-time layout of square patterns
+      case ALGO_HIO: return launch_pdl(row_pass_rk<N, ROW_ITER, ALGO_HIO, true>, grid, G::T, SM, st, a, pdl_of<N>(a.pdl_mode));
+      case ALGO_RAAR: return launch_pdl(row_pass_rk<N, ROW_ITER, ALGO_RAAR, true>, grid, G::T, SM, st, a, pdl_of<N>(a.pdl_mode));
+      case ALGO_ER: return launch_pdl(row_pass_rk<N, ROW_ITER, ALGO_ER, true>, grid, G::T, SM, st, a, pdl_of<N>(a.pdl_mode));
+      case ALGO_POSER: return launch_pdl(row_pass_rk<N, ROW_ITER, ALGO_POSER, true>, grid, G::T, SM, st, a, pdl_of<N>(a.pdl_mode));
+      case ALGO_POSHIO: return launch_pdl(row_pass_rk<N, ROW_ITER, ALGO_POSHIO, true>, grid, G::T, SM, st, a, pdl_of<N>(a.pdl_mode));
+      default: return launch_pdl(row_pass_rk<N, ROW_ITER, ALGO_FHIO, true>, grid, G::T, SM, st, a, pdl_of<N>(a.pdl_mode));
+    }
     switch (a.algo) {   // unknown codes take the FHIO branch, as applySupport does (cdi.cc:25-36)
       case ALGO_HIO: return launch_pdl(row_pass_rk<N, ROW_ITER, ALGO_HIO>, grid, G::T, SM, st, a, pdl_of<N>(a.pdl_mode));
       case ALGO_RAAR: return launch_pdl(row_pass_rk<N, ROW_ITER, ALGO_RAAR>, grid, G::T, SM, st, a, pdl_of<N>(a.pdl_mode));
