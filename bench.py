@@ -528,6 +528,58 @@ def comparator_section():
     return out
 
 
+def tc_section():
+    """The large single-pattern configuration's two FFT paths, on the same pattern:
+    the plain fused FP32 iteration (fft_mode 0) against the split-BF16 tensor-core
+    FFT on tcgen05 (fft_mode 1) and on mma.sync (fft_mode 2).  Per mode: us per RAAR
+    iteration (events, L2 flushed before each block of 50), the error of one 2-D
+    FFT against the float64 DFT (numpy), and the error of one RAAR iteration from
+    the same start against the FP32 path (longer runs diverge: RAAR amplifies any
+    rounding difference)."""
+    import torch
+    from cdixx_gb300 import native as cdx
+    I, psi0 = make_inputs()
+    stream = torch.cuda.Stream()
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    rng = np.random.default_rng(SEED)
+    x = (rng.standard_normal((N, N)) + 1j * rng.standard_normal((N, N))).astype(np.complex64)
+    ref = np.fft.fft2(x.astype(np.complex128))
+    xt = torch.from_numpy(x).cuda()
+    out = {"workload": WORKLOAD, "algorithm": f"{SW_EVERY}*RAAR per timed block", "modes": {}}
+    rho_fp32 = None
+    for mode, name in ((0, "fp32"), (1, "tc_bf16_tcgen05"), (2, "tc_bf16_mma_sync")):
+        y = torch.empty_like(xt)
+        cdx.fft2(xt, y, fft_mode=mode)
+        torch.cuda.synchronize()
+        fft_err = float(np.linalg.norm(y.cpu().numpy() - ref) / np.linalg.norm(ref))
+        p = cdx.default_params(N, N, oversampling_spt=4.0, beta=BETA, fft_mode=mode)
+        ctx = cdx.Context(p, stream=stream.cuda_stream)
+        ctx.set_pattern(0, I)
+        ctx.set_initial(0, psi0)
+        ctx.run("1*RAAR")
+        rho = ctx.get_object(0)
+        if mode == 0:
+            rho_fp32 = rho
+        vals = []
+        for _ in range(5):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            ctx.run_async(f"{SW_EVERY}*RAAR")
+            e1.record(stream)
+            torch.cuda.synchronize()
+            vals.append(e0.elapsed_time(e1) * 1000.0 / SW_EVERY)
+        ctx.close()
+        out["modes"][name] = {"us_per_iteration": float(np.median(vals)), "fft2_rel_l2_vs_fp64": fft_err,
+                              "rho_rel_l2_vs_fp32_one_iteration": float(np.linalg.norm(rho - rho_fp32) /
+                                                                   np.linalg.norm(rho_fp32))}
+    f = out["modes"]["fp32"]["us_per_iteration"]
+    for k in ("tc_bf16_tcgen05", "tc_bf16_mma_sync"):
+        out["modes"][k]["time_vs_fp32"] = out["modes"][k]["us_per_iteration"] / f
+    return out
+
+
 # Ptychography: the reference's own configuration (html/default/ptycho.cfg optics,
 # 512^2 probe, row_O = column_O = 1280, initScan_triangle with stepSize 250).
 PTY_R, PTY_RO, PTY_STEP = 512, 1280, 250.0
@@ -709,9 +761,11 @@ def run_gpu(args):
         cpu = {"value": v, "unit": "iter/s", "cores": threads, "kind": "port",
                "sample": "2 RAAR iterations of the 2048^2 pattern, float32 oracle, "
                          f"scipy.fft with {threads} workers ({dt:.2f} s)"}
-    warm = comb = batched = pty = cmpr = None
+    warm = comb = batched = pty = cmpr = tcs = None
     if rank == 0 and not args.no_comparator:
         cmpr = comparator_section()
+    if rank == 0 and not args.no_tc:
+        tcs = tc_section()
     if rank == 0 and not args.no_ptycho:
         pty = ptycho_section(cpu=not args.no_cpu)
     if rank == 0 and not args.no_warm:
@@ -737,6 +791,7 @@ def run_gpu(args):
             "clocks": clk,
             "gpu_launches": launches_per_step * args.steps,
             "gpu_comparator": cmpr,
+            "tc_fft": tcs,
             "warm_start": warm,
             "combined": comb,
             "batched": batched,
@@ -913,6 +968,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the uneven-size batch section")
     ap.add_argument("--no-ptycho", action="store_true", help="skip the ptychography section")
     ap.add_argument("--no-comparator", action="store_true", help="skip the cuFFT-structure comparator section")
+    ap.add_argument("--no-tc", action="store_true", help="skip the tensor-core FFT leg of the 2048^2 configuration")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
