@@ -816,11 +816,16 @@ def run_gpu(args):
 def case_pass(a):
     """A few fused iterations of one synthetic pattern through the C ABI, graph
     capture off: after the set-up launches each iteration is one column pass and
-    one row pass, then the final FFT, norm and reductions of the run."""
+    one row pass, then the final FFT, norm and reductions of the run.  At 2048^2
+    the pattern is the large single-pattern configuration's; other sizes take
+    uniform random intensities."""
     from cdixx_gb300 import native as cdx
-    rng = np.random.default_rng(0)
-    I = (rng.random((a.n, a.n)) * 100).astype(np.float32)
-    psi0 = (np.sqrt(I) * np.where(rng.random((a.n, a.n)) > 0.5, -1, 1)).astype(np.complex64)
+    if a.n == N:   # the large single-pattern configuration's own pattern (Poisson, 60 % zeros)
+        I, psi0 = make_inputs()
+    else:
+        rng = np.random.default_rng(0)
+        I = (rng.random((a.n, a.n)) * 100).astype(np.float32)
+        psi0 = (np.sqrt(I) * np.where(rng.random((a.n, a.n)) > 0.5, -1, 1)).astype(np.complex64)
     p = cdx.default_params(a.n, a.n, batch=a.batch, oversampling_spt=4.0, beta=0.9, use_graph=0,
                            fft_mode=a.fft_mode)
     with cdx.Context(p) as ctx:

@@ -192,9 +192,12 @@ __device__ __forceinline__ void rfft(float2 (&in)[RFirst<N, PLAN>::B][RFirst<N, 
 
 // Shared memory and resident CTAs per SM (register budget) of the
 // register-handoff kernels.  The column pass at 256 threads is budgeted for 4
-// CTAs per SM (64 registers, no spills; 2-4 % faster than 3); the row pass is
-// held to 3 by its shared memory (the staged rho rows: loading rho straight
-// from global memory instead was 4-30 % slower, its latency exposed).
+// CTAs per SM (64 registers, no spills; 2-4 % faster than 3).  The row pass
+// stages its rho rows in the line buffer (loading rho straight from global
+// memory instead was 4-30 % slower, its latency exposed) and is budgeted for 4
+// CTAs per SM below 1024 and 3 from 1024 up, where the radix-16 last passes
+// would spill at 64 registers (2048^2: 80 registers, 50.5 -> 49.7 us per
+// iteration; 512^2 x16 is faster at 4).
 #ifndef CDX_RK_MINB_COL
 #define CDX_RK_MINB_COL 4
 #endif
@@ -217,7 +220,7 @@ struct RGeom {
       G::SMEM_LINES + (RHO_IN_BUF ? 0 : G::L * G::LD * (int)sizeof(float2)) + G::L * ((N + 31) >> 5) * 4;
   static constexpr int MINB_COL = (CDX_RK_MINB_COL > 0 && G::T == 256) ? CDX_RK_MINB_COL : G::MINB;
   static constexpr int MINB_ROW =
-      (CDX_RK_MINB_ROW > 0 && G::T == 256) ? CDX_RK_MINB_ROW : (RHO_IN_BUF ? 4 : G::MINB);
+      (CDX_RK_MINB_ROW > 0 && G::T == 256) ? CDX_RK_MINB_ROW : (RHO_IN_BUF ? (N >= 1024 ? 3 : 4) : G::MINB);
 };
 
 // ------------------------------------------------------------- real-space updates
@@ -440,6 +443,19 @@ __device__ __forceinline__ void row_pass_body(const RowArgs& a) {
   // (RHO_IN_BUF: the rho rows land in the line buffer during its last pass)
   constexpr int RS = G::LD;                 // rho line stride in shared memory
   constexpr int WPR = (N + 31) >> 5;
+  // Support words in shared memory: with MT the words a butterfly of the update
+  // needs (columns j + r*NS, r < R: word (j >> 5) + r*NS/32) are staged next to
+  // one another, so a thread reads its R words with R/4 16-byte loads instead of R.
+  constexpr bool MT = FL::NS % 32 == 0 && FL::R % 4 == 0 && WPR % 4 == 0;
+  constexpr int MG = MT ? FL::NS / 32 : 1;   // word groups per row
+  auto mask_slot = [](int w) -> int {
+    if constexpr (MT) {
+      const int l = w / WPR, q = w - l * WPR;   // row l, word q = g + r*MG
+      return l * WPR + (q % MG) * FL::R + q / MG;
+    } else {
+      return w;
+    }
+  };
   constexpr bool rho_in_buf = RGeom<N>::RHO_IN_BUF;
   float2* rho_s = rho_in_buf ? smem : smem + L * G::LD;
   uint32_t* mask_s = reinterpret_cast<uint32_t*>(smem + L * G::LD + (rho_in_buf ? 0 : L * RS));
@@ -484,7 +500,7 @@ __device__ __forceinline__ void row_pass_body(const RowArgs& a) {
     const uint32_t* mask = a.mask + (long long)blockIdx.y * a.mask_stride + (long long)row0 * WPR;
     for (int w = threadIdx.x; w < L * WPR; w += T) {
       const bool ok = w / WPR < nrows;
-      cp_async4(mask_s + w, ok ? mask + w : mask, ok);
+      cp_async4(mask_s + mask_slot(w), ok ? mask + w : mask, ok);
     }
     cp_commit();
   }
@@ -550,16 +566,21 @@ __device__ __forceinline__ void row_pass_body(const RowArgs& a) {
     for (int b = 0; b < FL::B; ++b) {
       int l, j;
       if (!bfly_of<N, FL::R>(b, cb, l, j)) continue;
+      const uint4* m4 = reinterpret_cast<const uint4*>(mask_s + l * WPR + (j >> 5) * FL::R);
+      uint4 mq = make_uint4(0u, 0u, 0u, 0u);
 #pragma unroll
       for (int r = 0; r < FL::R; ++r) {
         const int c = j + r * FL::NS;
         float2 y = make_float2(0.f, 0.f);
+        if constexpr (MT) if ((r & 3) == 0) mq = m4[r >> 2];   // four words at a time
         if (l < nrows) {
           float2 p = v[b][r];
           p.x *= a.inv_n;
           p.y *= a.inv_n;
           const float2 x = rho_s[l * RS + c];
-          const bool inside = (mask_s[l * WPR + (c >> 5)] >> (c & 31)) & 1u;
+          const uint32_t word = MT ? ((r & 3) == 0 ? mq.x : (r & 3) == 1 ? mq.y : (r & 3) == 2 ? mq.z : mq.w)
+                                   : mask_s[l * WPR + (c >> 5)];
+          const bool inside = (word >> (c & 31)) & 1u;
           y = update_t<ALGO>(inside, x, p, a.beta);
           rho[l * N + c] = y;
         }
