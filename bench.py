@@ -56,7 +56,7 @@ METRIC = "iter/s"
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one 2048^2 iteration,
 # col_pass_rk<2048> + row_pass_rk<2048>, from one ncu capture of
 # `python bench.py case pass --n 2048 --iters 3` (profiles/pass_kernels_2048.md)
-PASS_TRAFFIC_2048 = 131_400_000
+PASS_TRAFFIC_2048 = 129_913_000
 WORKLOAD = "2048x2048 complex64 phase object, 1e9 photons, RAAR beta=0.9, shrinkwrap every 50"
 
 
