@@ -746,9 +746,11 @@ int run_impl(cdx_ctx* c, const char* algorithm) {
 
 }  // namespace
 
-// A set of contexts run as one CUDA graph, one parallel branch per context.
+// A set of contexts run as one CUDA graph, one branch per context: the branches
+// one after another (default) or side by side (concurrent).
 struct cdx_group {
   std::vector<cdx_ctx*> ctxs;
+  int concurrent = 0;
   cudaStream_t st = nullptr;
   cudaEvent_t fork = nullptr, ev0 = nullptr, ev1 = nullptr;
   std::vector<cudaEvent_t> joins;
@@ -763,6 +765,7 @@ int group_run_impl(cdx_group* g, const char* algorithm, double* gpu_ms) {
   std::vector<std::vector<int>> steps(n);
   std::vector<SwPlan> sw(n);
   std::string key = algorithm;
+  key += g->concurrent ? "|concurrent" : "|serial";
   for (size_t i = 0; i < n; ++i) {
     cdx_ctx* c = g->ctxs[i];
     int e = prepare_run(c, algorithm, steps[i], sw[i]);
@@ -780,7 +783,9 @@ int group_run_impl(cdx_group* g, const char* algorithm, double* gpu_ms) {
     cudaError_t ce = cudaEventRecord(g->fork, g->st);
     for (size_t i = 0; i < n && ce == cudaSuccess && !e; ++i) {
       cdx_ctx* c = g->ctxs[i];
-      ce = cudaStreamWaitEvent(c->st, g->fork, 0);   // the context's stream joins the capture
+      // the context's stream joins the capture: after the fork (side by side) or after the
+      // previous branch (one after another)
+      ce = cudaStreamWaitEvent(c->st, (g->concurrent || i == 0) ? g->fork : g->joins[i - 1], 0);
       if (ce == cudaSuccess) e = enqueue_run(c, steps[i], sw[i], c->psi_in_work);
       if (ce == cudaSuccess && !e) ce = cudaEventRecord(g->joins[i], c->st);
       if (ce == cudaSuccess && !e) ce = cudaStreamWaitEvent(g->st, g->joins[i], 0);
@@ -1224,6 +1229,12 @@ int cdx_group_create(cdx_ctx* const* ctxs, int n, cdx_group** out) {
 int cdx_group_run(cdx_group* g, const char* algorithm, double* gpu_ms) {
   if (!g) return set_error(CDX_ERR_ARG, "null group");
   return group_run_impl(g, algorithm, gpu_ms);
+}
+
+int cdx_group_set_concurrent(cdx_group* g, int concurrent) {
+  if (!g) return set_error(CDX_ERR_ARG, "null group");
+  g->concurrent = concurrent != 0;
+  return CDX_OK;
 }
 
 int cdx_group_destroy(cdx_group* g) {

@@ -77,6 +77,7 @@ _SIGS = {
     "cdx_group_create": [ctypes.POINTER(_P), _I, ctypes.POINTER(_P)],
     "cdx_group_run": [_P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double)],
     "cdx_group_destroy": [_P],
+    "cdx_group_set_concurrent": [_P, _I],
     "cdx_get_object": [_P, _I, _P, _I],
     "cdx_get_fourier": [_P, _I, _P, _I],
     "cdx_get_support": [_P, _I, _P, _I],
@@ -323,11 +324,17 @@ class Context:
 class Group:
     """Contexts of different pattern sizes run as one CUDA graph (cdx_group_*)."""
 
-    def __init__(self, contexts):
+    def __init__(self, contexts, concurrent=False):
         self.contexts = list(contexts)
         arr = (ctypes.c_void_p * len(self.contexts))(*[c._h.value for c in self.contexts])
         self._h = ctypes.c_void_p()
         check(lib().cdx_group_create(arr, len(self.contexts), ctypes.byref(self._h)))
+        if concurrent:
+            self.set_concurrent(True)
+
+    def set_concurrent(self, concurrent: bool):
+        """Branch order of the group's graph: side by side (True) or one after another."""
+        check(lib().cdx_group_set_concurrent(self._h, int(bool(concurrent))))
 
     def run(self, algorithm: str) -> float:
         ms = ctypes.c_double()

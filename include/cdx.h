@@ -152,15 +152,22 @@ int cdx_get_stats(cdx_ctx* ctx, int idx, cdx_stats* stats);
 /* ---------------------------------------------------------------- uneven batches */
 /* A group runs phaseRetrieve on several contexts (typically one per pattern
  * size, each holding a batch of equal-size patterns) as ONE CUDA graph with a
- * parallel branch per context, so patterns of uneven sizes share the GPU in a
- * single launch.  No reference counterpart (the reference runs one pattern at
- * a time).  The contexts must use distinct streams (created by cdx_create
- * with stream NULL) and stay alive while the group exists. */
+ * branch per context, so patterns of uneven sizes run in a single launch.  No
+ * reference counterpart (the reference runs one pattern at a time).  The
+ * contexts must use distinct streams (created by cdx_create with stream NULL)
+ * and stay alive while the group exists. */
 typedef struct cdx_group cdx_group;
 int cdx_group_create(cdx_ctx* const* ctxs, int n, cdx_group** out);
 /* Runs `algorithm` on every context; synchronises; *gpu_ms gets the graph's
  * device time (may be NULL).  Per-pattern results: cdx_get_stats / cdx_get_*. */
 int cdx_group_run(cdx_group* g, const char* algorithm, double* gpu_ms);
+/* Branch order of the group's graph: 0 (default) the contexts one after
+ * another, nonzero side by side.  Each size's pass kernels already fill the GPU
+ * from 192^2 x 100 up, and side-by-side branches then slow one another (the
+ * 512-pattern uneven batch: 648 ms side by side, 620 ms one after another);
+ * batches too small to fill the GPU gain from running side by side.  The next
+ * cdx_group_run captures the graph again. */
+int cdx_group_set_concurrent(cdx_group* g, int concurrent);
 int cdx_group_destroy(cdx_group* g);
 
 /* ---------------------------------------------------------------- outputs */

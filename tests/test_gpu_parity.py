@@ -434,9 +434,10 @@ def test_large_pattern_iterates(cdx):
     assert e <= bound
 
 
-def test_group_of_uneven_sizes_equals_separate_runs(cdx):
-    """Contexts of three sizes run as one CUDA graph give the same bits as
-    separate runs."""
+@pytest.mark.parametrize("concurrent", [False, True])
+def test_group_of_uneven_sizes_equals_separate_runs(cdx, concurrent):
+    """Contexts of three sizes run as one CUDA graph, their branches one after
+    another or side by side, give the same bits as separate runs."""
     sizes = [(128, 2), (192, 1), (256, 3)]
     alg = "6*HIO+1*shrinkWrap+4*RAAR+2*ER"
     data = {n: [blob_case(n=n, seed=10 * n + i) for i in range(b)] for n, b in sizes}
@@ -449,7 +450,7 @@ def test_group_of_uneven_sizes_equals_separate_runs(cdx):
         return ctx
 
     ctxs = [make(n, b) for n, b in sizes]
-    g = cdx.Group(ctxs)
+    g = cdx.Group(ctxs, concurrent=concurrent)
     ms = g.run(alg)
     assert ms > 0
     grouped = {n: [ctx.get_object(i) for i in range(b)] for ctx, (n, b) in zip(ctxs, sizes)}
