@@ -64,13 +64,15 @@ __device__ __forceinline__ float2 apply_update(int algo, bool inside, float2 x, 
 // applyModAbs with state == NULL (src/gpu/cudaConfig.cu:827-841); amp is
 // sqrt(I) precomputed (I <= 0 or NaN -> 0), bit-identical to the per-call sqrtf.
 // Where amp is zero (most of a Poisson pattern's far field) the quotient amp/mod
-// is that zero, so s * amp gives the same bits without the division, whose
-// zero-dividend case is far slower than its common path (2048^2 phase object,
-// 60 % zeros: column pass 29.8 -> 25.1 us).
+// is that zero, so s * amp gives the same values without the modulus and the
+// division, whose zero-dividend case is far slower than its common path
+// (2048^2 phase object, 60 % zeros: column pass 29.8 -> 25.1 us).  The one
+// difference is the sign of an exact zero: s = (-0, 0) gives (-0, 0) here and
+// (0, 0) in the reference, which every later sum treats alike.
 __device__ __forceinline__ float2 proj_modabs(float2 s, float amp) {
+  if (amp == 0.f) return make_float2(s.x * amp, s.y * amp);
   float mod = hypotf(s.x, s.y);
   if (mod == 0.f) return make_float2(amp, 0.f);
-  if (amp == 0.f) return make_float2(s.x * amp, s.y * amp);
   float rat = amp / mod;
   return make_float2(s.x * rat, s.y * rat);
 }
