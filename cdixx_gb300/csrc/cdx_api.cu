@@ -430,9 +430,8 @@ int enqueue_run(cdx_ctx* c, const std::vector<int>& steps, const SwPlan& sw, boo
   }
   // applyNorm(cuda_gkp1, sqrt(row*column)) (cdi.cc:406)
   CDX_CK(scale_complex(c->rho, sqn, n_all, c->st));
-  CDX_CK(residual(c->psi, c->inten, c->npx, c->batch, c->part, kRedBlocks, c->dstate, c->st));
-  CDX_CK(rfactor(c->psi, c->inten, c->npx, c->batch, c->part, kRedBlocks, c->dstate, c->st));
-  nl += 5;
+  CDX_CK(residual_rfactor(c->psi, c->inten, c->npx, c->batch, c->part, kRedBlocks, c->dstate, c->st));
+  nl += 3;
   c->last_launches = nl;
   return CDX_OK;
 }

@@ -303,14 +303,19 @@ __global__ void __launch_bounds__(256) k_blur_y(const float2* __restrict__ tmp, 
 // Threshold logic of the shrinkwrap block (src/post_gpu/cdi.cc:330-337):
 // maxs = findMax; first time avg = findSum*4/rows/cols; maxs = min(maxs, 5*avg);
 // threshold = maxs*shrinkThreshold.  |rho|^2 mode: threshold = max*shrinkThreshold.
+// One warp per pattern: lane i folds partials i, i + 32, ... in order, then a
+// butterfly across the lanes (a fixed order, so the same sum on every device).
 __global__ void k_shrink_finalize(const float* __restrict__ pmax, const double* __restrict__ psum, int nblk,
                                   PatState* __restrict__ stt, int rows, int cols, int mod2_first,
                                   double shrink_threshold) {
   const int p = blockIdx.x;
-  if (threadIdx.x != 0 || (stt[p].flags & 6)) return;   // converged: no partials this time
+  if (stt[p].flags & 6) return;   // converged: no partials this time
   float m = 0.f;
   double s = 0.0;
-  for (int i = 0; i < nblk; ++i) { m = fmaxf(m, pmax[p * nblk + i]); s += psum[p * nblk + i]; }
+  for (int i = threadIdx.x; i < nblk; i += 32) { m = fmaxf(m, pmax[p * nblk + i]); s += psum[p * nblk + i]; }
+  m = warp_max_f(m);
+  s = warp_sum_d(s);
+  if (threadIdx.x != 0) return;
   PatState& S = stt[p];
   S.maxv = m;
   S.sum = (float)s;
@@ -351,35 +356,55 @@ __global__ void k_sum_real(const float* __restrict__ x, long long npx, double* _
   double t = block_sum_d<256>(acc, red);
   if (threadIdx.x == 0) part[p * nblk + blockIdx.x] = t;
 }
-// Residual of src/post_gpu/cdi.cc:413-421: sum (|Psi|^2 - I)^2 over I < 0.99.
-__global__ void k_residual(const float2* __restrict__ psi, const float* __restrict__ inten, long long npx,
-                           double* __restrict__ part, int nblk) {
-  const long long p = blockIdx.y;
-  double acc = 0.0;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npx; i += (long long)nblk * blockDim.x) {
-    const float2 v = psi[p * npx + i];
-    const float I = inten[p * npx + i];
-    float d = v.x * v.x + v.y * v.y;
-    d = I < 0.99f ? d - I : 0.f;
-    acc += (double)d * (double)d;
-  }
-  __shared__ double red[8];
-  double t = block_sum_d<256>(acc, red);
-  if (threadIdx.x == 0) part[p * nblk + blockIdx.x] = t;
+// The closing sums of a run in one pass over the final Psi and I: the residual
+// of src/post_gpu/cdi.cc:413-421, sum (|Psi|^2 - I)^2 over I < 0.99, and the
+// R-factor numerator sum | |Psi| - sqrt(I) |.  Each thread takes two adjacent
+// pixels per step (one 16-byte load of Psi, one 8-byte load of I) with the
+// loop unrolled, so a CTA of 1024 threads per SM keeps enough loads in flight
+// to stream the pattern at HBM speed.  Partials per pattern: [0, nblk) the
+// residual, [nblk, 2 nblk) the R-factor; the order of every sum is fixed.
+__device__ __forceinline__ void res_rdiff_px(float2 v, float I, double& r, double& d) {
+  float q = v.x * v.x + v.y * v.y;
+  q = I < 0.99f ? q - I : 0.f;
+  r += (double)q * (double)q;
+  d += (double)fabsf(hypotf(v.x, v.y) - (I > 0.f ? sqrtf(I) : 0.f));
 }
-// R-factor of a complete Psi: sum | |Psi| - sqrt(I) |.
-__global__ void k_rdiff(const float2* __restrict__ psi, const float* __restrict__ inten, long long npx,
-                        double* __restrict__ part, int nblk) {
+constexpr int kResThreads = 1024;
+__global__ void __launch_bounds__(kResThreads) k_res_rdiff(const float2* __restrict__ psi, const float* __restrict__ inten,
+                                                           long long npx, double* __restrict__ part, int nblk) {
   const long long p = blockIdx.y;
-  double acc = 0.0;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npx; i += (long long)nblk * blockDim.x) {
-    const float2 v = psi[p * npx + i];
-    const float I = inten[p * npx + i];
-    acc += (double)fabsf(hypotf(v.x, v.y) - (I > 0.f ? sqrtf(I) : 0.f));
+  const float2* ps = psi + p * npx;
+  const float* in = inten + p * npx;
+  double r0 = 0.0, r1 = 0.0, d0 = 0.0, d1 = 0.0;
+  const long long step = 2LL * nblk * kResThreads;
+#pragma unroll 4
+  for (long long i = 2LL * (blockIdx.x * (long long)kResThreads + threadIdx.x); i < npx; i += step) {
+    const float4 v = *reinterpret_cast<const float4*>(ps + i);   // npx even: pixels i, i + 1
+    const float2 I = *reinterpret_cast<const float2*>(in + i);
+    res_rdiff_px(make_float2(v.x, v.y), I.x, r0, d0);
+    res_rdiff_px(make_float2(v.z, v.w), I.y, r1, d1);
   }
-  __shared__ double red[8];
-  double t = block_sum_d<256>(acc, red);
-  if (threadIdx.x == 0) part[p * nblk + blockIdx.x] = t;
+  __shared__ double red[kResThreads / 32];
+  const double tr = block_sum_d<kResThreads>(r0 + r1, red);
+  const double td = block_sum_d<kResThreads>(d0 + d1, red);
+  if (threadIdx.x == 0) {
+    part[p * 2 * nblk + blockIdx.x] = tr;
+    part[p * 2 * nblk + nblk + blockIdx.x] = td;
+  }
+}
+__global__ void k_res_rdiff_finalize(const double* __restrict__ part, int nblk, PatState* __restrict__ stt) {
+  const int p = blockIdx.x;
+  double r = 0.0, d = 0.0;
+  for (int i = threadIdx.x; i < nblk; i += 32) {
+    r += part[p * 2 * nblk + i];
+    d += part[p * 2 * nblk + nblk + i];
+  }
+  r = warp_sum_d(r);
+  d = warp_sum_d(d);
+  if (threadIdx.x == 0) {
+    stt[p].residual = r;
+    stt[p].rfactor = stt[p].amp_sum > 0.0 ? d / stt[p].amp_sum : 0.0;
+  }
 }
 
 // Fixed-order final sums.  what: 0 amp_sum, 1 residual, 2 rfactor (= sum / amp_sum).
@@ -388,13 +413,15 @@ __global__ void k_rdiff(const float2* __restrict__ psi, const float* __restrict_
 // pattern's own PatState::stop when set, else the run's `stop` (> 0 to act).
 // With plateau > 0 a pattern whose R-factor has not fallen below (1 - tol)
 // times its last improvement for `plateau` iterations freezes the same way.
+// One warp per pattern, lane-strided sums and a butterfly across the lanes (fixed order).
 __global__ void k_finalize_sum(const double* __restrict__ part, int nblk, PatState* __restrict__ stt, int what,
                                double stop, int iter, int plateau, float tol) {
   const int p = blockIdx.x;
-  if (threadIdx.x != 0) return;
   if (iter >= 0 && (stt[p].flags & 6)) return;   // already converged: partials are stale
   double s = 0.0;
-  for (int i = 0; i < nblk; ++i) s += part[p * nblk + i];
+  for (int i = threadIdx.x; i < nblk; i += 32) s += part[p * nblk + i];
+  s = warp_sum_d(s);
+  if (threadIdx.x != 0) return;
   if (what == 0) stt[p].amp_sum = s;
   else if (what == 1) stt[p].residual = s;
   else {
@@ -423,16 +450,11 @@ cudaError_t pattern_amp_sum(const float* amp, long long npx, int batch, double* 
   k_finalize_sum<<<batch, 32, 0, st>>>(part, nblk, stt, 0, 0.0, -1, 0, 0.f);
   return cudaGetLastError();
 }
-cudaError_t residual(const float2* psi, const float* inten, long long npx, int batch, double* part, int nblk,
-                     PatState* stt, cudaStream_t st) {
-  k_residual<<<dim3(nblk, batch), 256, 0, st>>>(psi, inten, npx, part, nblk);
-  k_finalize_sum<<<batch, 32, 0, st>>>(part, nblk, stt, 1, 0.0, -1, 0, 0.f);
-  return cudaGetLastError();
-}
-cudaError_t rfactor(const float2* psi, const float* inten, long long npx, int batch, double* part, int nblk,
-                    PatState* stt, cudaStream_t st) {
-  k_rdiff<<<dim3(nblk, batch), 256, 0, st>>>(psi, inten, npx, part, nblk);
-  k_finalize_sum<<<batch, 32, 0, st>>>(part, nblk, stt, 2, 0.0, -1, 0, 0.f);
+cudaError_t residual_rfactor(const float2* psi, const float* inten, long long npx, int batch, double* part, int nblk,
+                             PatState* stt, cudaStream_t st) {
+  if (npx % 2) return cudaErrorInvalidValue;
+  k_res_rdiff<<<dim3(nblk, batch), kResThreads, 0, st>>>(psi, inten, npx, part, nblk);
+  k_res_rdiff_finalize<<<batch, 32, 0, st>>>(part, nblk, stt);
   return cudaGetLastError();
 }
 cudaError_t rfactor_from_partials(const double* part, int nblk, int batch, PatState* stt, double stop, int iter,

@@ -26,10 +26,10 @@ cudaError_t shrinkwrap(const float2* rho, float2* tmp, float* spt, const float* 
                        int nblk, PatState* stt, double shrink_threshold, cudaStream_t st);
 cudaError_t pattern_amp_sum(const float* amp, long long npx, int batch, double* part, int nblk, PatState* stt,
                             cudaStream_t st);
-cudaError_t residual(const float2* psi, const float* inten, long long npx, int batch, double* part, int nblk,
-                     PatState* stt, cudaStream_t st);
-cudaError_t rfactor(const float2* psi, const float* inten, long long npx, int batch, double* part, int nblk,
-                    PatState* stt, cudaStream_t st);
+// The residual and the R-factor of the final Psi in one pass (2 * nblk partials per pattern;
+// the R-factor divides by the pattern's amp_sum).
+cudaError_t residual_rfactor(const float2* psi, const float* inten, long long npx, int batch, double* part, int nblk,
+                             PatState* stt, cudaStream_t st);
 cudaError_t rfactor_from_partials(const double* part, int nblk, int batch, PatState* stt, double stop, int iter,
                                   int plateau, float tol, cudaStream_t st);
 cudaError_t run_begin(PatState* stt, int batch, cudaStream_t st);
