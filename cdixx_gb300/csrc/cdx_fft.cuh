@@ -194,10 +194,11 @@ __host__ __device__ constexpr int radix_count(int n) {
   while (radix_desc(n, q) != 0) ++q;
   return q;
 }
-// Radix of pass p for length N: the radices in a V, the largest at both ends
-// and the smallest in the middle (the i-th largest goes to the front for even
-// i, to the back for odd i): 2048 = 16.8.16, 1024 = 16.4.16, 512 = 16.2.16,
-// 384 = 16.3.8, 3072 = 16.4.3.16.  Measured per 4.2 M-pixel iteration against
+// Radix of pass p for length N: the radices in a V, the 16s at both ends and
+// the smaller radices in the middle.  The i-th radix of radix_desc (16s, then
+// 8, 4, 2, then 3s) goes to the front for even i and to the back for odd i:
+// 2048 = 16.8.16, 1024 = 16.4.16, 512 = 16.2.16, 384 = 16.3.8, 96 = 16.3.2,
+// 3072 = 16.4.3.16.  Measured per 4.2 M-pixel iteration against
 // the largest-first order (16.16.8 etc.): 2048^2 -4.7 %, 1024^2 x4 -12.5 %,
 // 512^2 x16 -5.9 %, 384^2 x16 -3.5 %; a V that reads the same both ways is
 // also the inverse order, so both transforms share one twiddle table.
