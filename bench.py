@@ -54,8 +54,9 @@ JOB_ITERS = 40 * SW_EVERY
 ALG_BYTES_PER_PX_ITER = 21.0
 METRIC = "iter/s"
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one 2048^2 iteration,
-# col_pass_rk<2048> + row_pass_rk<2048>, from one ncu capture of
-# `python bench.py case pass --n 2048 --iters 3` (profiles/pass_kernels_2048.md)
+# col_pass_rk<2048> + row_pass_rk<2048>, from one `ncu --set full` capture of
+# `python bench.py case pass --n 2048 --iters 3` (-k regex:pass_rk -s 3 -c 2):
+# 50.41 + 0.05 + 67.68 + 11.77 MB, cold caches
 PASS_TRAFFIC_2048 = 129_913_000
 WORKLOAD = "2048x2048 complex64 phase object, 1e9 photons, RAAR beta=0.9, shrinkwrap every 50"
 
