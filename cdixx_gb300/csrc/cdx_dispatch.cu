@@ -42,7 +42,7 @@ int twiddle_count(int n) {
 int row_cb_max(int n) {
   switch (n) { CDX_FOR_EACH_SIZE(CASE_CB) default: return 0; }
 }
-int row_cb_default(int n, int tile_log2) { return std::min(tile_log2, row_cb_max(n)); }
+int row_cb_default(int n, int tile_log2) { return row_cb_pick(tile_log2, row_cb_max(n)); }
 
 // Entry (r-1)*NS + k of pass p's block = W_n^(r*k*n/(NS*R)), W_n = exp(-2 pi i/n),
 // evaluated in double with the exponent reduced mod n and rounded once to float;

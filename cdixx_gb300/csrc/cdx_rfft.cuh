@@ -38,6 +38,16 @@ struct RPass {
   static constexpr int TWO = tw_offset_x(N, PLAN, P);
 };
 
+// Default butterfly chunk bits of the row pass on column-tiled data: the tile
+// width (2^tl threads per tile row piece), except that 8-wide tiles take chunks
+// of 16 where the length allows: with chunks of 8 a half-warp spans two lines
+// whose stride is 2 mod 16 float2, so its shared-memory accesses conflict
+// (512^2: 2.6 M bank conflicts per row pass), while 16 keep each half-warp on
+// one line and still read whole 128-byte lines of W.
+__host__ __device__ constexpr int row_cb_pick(int tl, int cb_max) {
+  return tl == 3 && cb_max >= 4 ? 4 : (tl < cb_max ? tl : cb_max);
+}
+
 // largest chunk bits valid for every pass: NR = N / R is a multiple of 2^cb for
 // every radix R of the length (both plans have the same radices), so the map
 // below is a bijection onto (line, butterfly) in every pass; e.g. 2048 -> 7,
@@ -430,14 +440,14 @@ __device__ __forceinline__ void row_pass_body(const RowArgs& a) {
   constexpr bool iter = MODE == ROW_ITER;
   constexpr bool CT = SQ && iter && row_sq_ok<N>();   // compile-time layout
   constexpr int TLC = G::LOG2L;
-  constexpr int CBC = TLC < rfft_cb_max<N>() ? TLC : rfft_cb_max<N>();
+  constexpr int CBC = row_cb_pick(TLC, rfft_cb_max<N>());
   const int tl = CT ? TLC : a.tile_log2;
   // tiled: four (or 2^tl) threads per tile row piece; row-major: consecutive
   // threads take consecutive columns
   const bool tiled = a.in_tiled || a.out_tiled;
   const int cb = CT ? CBC
                     : (a.cb_plus1 > 0 ? min(a.cb_plus1 - 1, rfft_cb_max<N>())
-                                      : (tiled ? min(tl, rfft_cb_max<N>()) : rfft_cb_max<N>()));
+                                      : (tiled ? row_cb_pick(tl, rfft_cb_max<N>()) : rfft_cb_max<N>()));
 
   // rho rows and support words of the CTA (ROW_ITER), landing during the inverse FFT
   // (RHO_IN_BUF: the rho rows land in the line buffer during its last pass)
@@ -624,7 +634,7 @@ __global__ void __launch_bounds__(Geom<N>::T, RGeom<N>::MINB_ROW) row_pass_rk(Ro
 // the compile-time layout of row_pass_rk<..., true> applies to these arguments
 template <int N>
 __host__ __forceinline__ bool row_sq_layout(const RowArgs& a) {
-  constexpr int cbd = Geom<N>::LOG2L < rfft_cb_max<N>() ? Geom<N>::LOG2L : rfft_cb_max<N>();
+  constexpr int cbd = row_cb_pick(Geom<N>::LOG2L, rfft_cb_max<N>());
   return row_sq_ok<N>() && a.mode == ROW_ITER && a.in_tiled && a.out_tiled && a.tile_log2 == Geom<N>::LOG2L && a.scale == 1.f &&
          (a.cb_plus1 == 0 || a.cb_plus1 - 1 == cbd);
 }
