@@ -51,6 +51,20 @@ bool check_len() {
   for (int p = 0; p < m; ++p)
     if ((N / plan_radix(N, p)) % (1 << cb) != 0) fail("chunk bits too large");
   if (row_sq_ok<N>() != (Geom<N>::LOG2L <= cb)) fail("row_sq_ok");
+  // the butterfly -> (line, index) map of a pass is a bijection for every chunk width the
+  // row pass may take (the tuner's variants and the default of any tile width)
+  for (int c = 0; c <= cb; ++c)
+    for (int p = 0; p < m; ++p) {
+      const int R = plan_radix(N, p), L = Geom<N>::L, NR = N / R, NB = L * NR;
+      std::vector<char> seen(NB, 0);
+      for (int g = 0; g < NB; ++g) {
+        const int l = (g >> c) & (L - 1);
+        const int j = ((g >> (c + Geom<N>::LOG2L)) << c) | (g & ((1 << c) - 1));
+        if (l >= L || j >= NR || seen[l * NR + j]++) { fail("butterfly map is not a bijection"); break; }
+      }
+    }
+  for (int tl = 0; tl <= 8; ++tl)
+    if (row_cb_pick(tl, cb) > cb || row_cb_pick(tl, cb) < 0) fail("default chunk past the bound");
   std::printf("N=%d plan", N);
   for (int r : a) std::printf(" %d", r);
   std::printf(" twiddles %d%s cb_max %d sq %d\n", tw_count(N), same ? " (shared)" : "", cb, (int)row_sq_ok<N>());

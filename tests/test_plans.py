@@ -3,7 +3,9 @@ tests/cpp/plan_check.cu, built with nvcc as host code, checks for every
 supported length that the radices multiply to the length, that the inverse
 plan is the forward one reversed, that the two leading radices sit at the ends
 (the V order), that the twiddle blocks tile the table (shared by the two plans
-when the V reads the same both ways), and the row pass's chunk-bit bound."""
+when the V reads the same both ways), that the butterfly-to-thread map of every
+pass is a bijection for every chunk width up to the bound, and that the row
+pass's default chunk stays within it."""
 import shutil
 import subprocess
 from pathlib import Path
